@@ -1,0 +1,799 @@
+// fastpath.cu -- FP32 + guard-band form of the pixel pipeline.
+//
+// The vertical and horizontal resampling run in FP32.  Every output sample
+// carries a rigorous bound E on |v_fp32 - v_ref|, where v_ref is the value the
+// reference computes in double precision (with its float intermediate).  The
+// quantisation tail then decides the output code for the whole interval
+// [v - E, v + E]; if a decision boundary of the reference (a code bracket
+// edge, a nearest-colour midpoint, an ordered-dither threshold) lies inside,
+// the pixel is flagged and recomputed exactly in FP64 by k_fix_flagged
+// (pipeline.cu).  Output bytes therefore equal the plain form's.
+//
+// Error bound (u = 2^-24, per pass with n taps and weights w):
+//   decode   |a' - a| <= e_dec + r_dec * a          (e_dec measured over every code)
+//   vertical |I' - I_ref| <= e_dec*W1v + c1 * (|I'| + 2*Wneg_v)
+//   horizontal |v' - v_ref| <= K0 + K1 * sum_k |I'_k||w_k|
+// with c1 = (r_dec + 2u + gamma_nv + gamma_nv^(fp64)) and K0, K1 assembled on
+// the host below; unassociating alpha divides by the float alpha, whose own
+// bound is propagated.
+#include "iwg_internal.h"
+#include "device.cuh"
+#include "fastpath.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <vector>
+
+namespace iwg {
+
+using namespace dev;
+
+__global__ void k_fix_flagged_fwd(Job J, const int *count, const int *list);
+
+namespace {
+
+constexpr int kVThreads = 128;
+constexpr int kHThreads = 128;
+constexpr int kMaxPlanes = 4;
+
+struct FPlane {
+	int src;          // physical channel, -1: virtual (value 1)
+	int table;        // 1: decode through the shared table; 0: code * inv
+	int premul;       // multiply by the alpha value
+	float inv;        // 1 / maxcc for arithmetic decode
+};
+
+struct FTail {        // quantisation of one output channel, float tables
+	int P, M, cc, use_nc, dfam, dsub;
+	const float *U;   // P+2
+	const float *X;   // P+1
+	const int *code;  // P+2
+	const float *rev; // M+1
+	const float *nc;  // 255
+};
+
+struct FJob {
+	// input
+	const uint8_t *in;
+	unsigned long long in_bpr;
+	int crop_x, crop_y, nphys, depth;
+	int alpha_src;    // physical alpha channel, -1 virtual/none
+	float alpha_inv;
+	int npl;
+	FPlane pl[kMaxPlanes];
+	const float *dec_tab;      // 8-bit: 256 floats; 16-bit: 4096 (T0, slope) pairs
+	int dec_tab_floats;
+	// vertical pass
+	int mid_w, mid_h;
+	float *interm;
+	unsigned long long plane;
+	// streaming
+	int pmin, npos, ns;
+	const int2 *pinfo;        // per position: (first row finalised, count)
+	const float *sw;          // per position: ns slot weights (padded to 8)
+	const int *srcrow;        // per position: input row, -1 virtual
+	const int *first_pos, *last_pos;
+	int rows_per_band;
+	// gather (upscale) vertical pass
+	const int *voff, *vsrc;
+	const float *vw;
+	// horizontal pass
+	const int *hoff, *hsrc;
+	const float *hw;
+	int out_w, out_h, out_n, out_depth;
+	uint8_t *out;
+	unsigned long long out_bpr;
+	// per mid channel (processing order)
+	int mid_n;
+	int order[dev::kMaxCh];
+	int plane_of[dev::kMaxCh];
+	int out_of[dev::kMaxCh];
+	int is_alpha[dev::kMaxCh];
+	int unassoc[dev::kMaxCh];
+	int alpha_plane;
+	FTail tail[dev::kMaxCh];        // per output channel
+	int maxcc[dev::kMaxCh];
+	int out_alpha[dev::kMaxCh];     // output channel is an alpha channel
+	int negate, blacken;
+	// error model
+	float K0[kMaxPlanes], K1[kMaxPlanes];
+	// flags
+	int *flag_count;
+	int *flag_list;
+};
+
+// ---------------------------------------------------------------------------
+// decode
+// ---------------------------------------------------------------------------
+
+template<int DEPTH>
+__device__ __forceinline__ unsigned int fetch_code(const uint8_t *px, int ch)
+{
+	if(DEPTH == 8) return px[ch];
+	return ((unsigned int)px[2 * ch] << 8) | px[2 * ch + 1];
+}
+
+template<int DEPTH>
+__device__ __forceinline__ float dec_table(const float *tab, unsigned int code)
+{
+	if(DEPTH == 8) return tab[code];
+	float2 t = reinterpret_cast<const float2 *>(tab)[code >> 4];
+	return __fmaf_rn((float)(code & 15u), t.y, t.x);
+}
+
+template<int NPL, int DEPTH>
+__device__ __forceinline__ void decode_pixel(const FJob &F, const float *tab, const uint8_t *px, float *val)
+{
+	float a = 1.0f;
+	if(F.alpha_src >= 0) a = __fmul_rn((float)fetch_code<DEPTH>(px, F.alpha_src), F.alpha_inv);
+#pragma unroll
+	for(int c = 0; c < NPL; c++) {
+		const FPlane &P = F.pl[c];
+		float v;
+		if(P.src < 0) v = 1.0f;
+		else {
+			unsigned int code = fetch_code<DEPTH>(px, P.src);
+			v = P.table ? dec_table<DEPTH>(tab, code) : __fmul_rn((float)code, P.inv);
+		}
+		val[c] = P.premul ? __fmul_rn(v, a) : v;
+	}
+}
+
+// ---------------------------------------------------------------------------
+// vertical pass, streaming: each thread owns one column; input rows are read
+// once, in order, and accumulated into NS register slots, one per output row
+// whose window is open (slot = row mod NS).
+// ---------------------------------------------------------------------------
+template<int NS, int NPL, int DEPTH>
+__global__ void __launch_bounds__(kVThreads) k_vstream(FJob F)
+{
+	extern __shared__ float s_tab[];
+	for(int k = threadIdx.x; k < F.dec_tab_floats; k += blockDim.x) s_tab[k] = F.dec_tab[k];
+	__syncthreads();
+
+	const int x = blockIdx.x * blockDim.x + threadIdx.x;
+	const bool active = x < F.mid_w;
+	const int jb = blockIdx.y * F.rows_per_band;
+	const int je = min(jb + F.rows_per_band, F.mid_h);
+	if(jb >= je) return;
+	const int p0 = F.first_pos[jb], p1 = F.last_pos[je - 1];
+	const int bpp = F.nphys * (DEPTH / 8);
+	const uint8_t *colbase = F.in + (size_t)(F.crop_x + (active ? x : 0)) * bpp;
+
+	float acc[NS][NPL];
+#pragma unroll
+	for(int s = 0; s < NS; s++)
+#pragma unroll
+		for(int c = 0; c < NPL; c++) acc[s][c] = 0.0f;
+
+	for(int p = p0; p <= p1; p++) {
+		const int q = p - F.pmin;
+		const int row = __ldg(F.srcrow + q);
+		float val[NPL];
+		if(row >= 0 && active) {
+			const uint8_t *px = colbase + (unsigned long long)(F.crop_y + row) * F.in_bpr;
+			decode_pixel<NPL, DEPTH>(F, s_tab, px, val);
+		}
+		else {
+#pragma unroll
+			for(int c = 0; c < NPL; c++) val[c] = 0.0f;   // transparent edge: value 0
+		}
+		const float *w = F.sw + (size_t)q * 8;
+#pragma unroll
+		for(int s = 0; s < NS; s++) {
+			float ws = __ldg(w + s);
+#pragma unroll
+			for(int c = 0; c < NPL; c++) acc[s][c] = __fmaf_rn(val[c], ws, acc[s][c]);
+		}
+		const int2 fin = __ldg(F.pinfo + q);
+		for(int k = 0; k < fin.y; k++) {
+			const int j = fin.x + k;
+			const int sj = j % NS;
+#pragma unroll
+			for(int s = 0; s < NS; s++) {
+				if(s == sj) {
+					if(active && j >= jb && j < je) {
+#pragma unroll
+						for(int c = 0; c < NPL; c++)
+							F.interm[(unsigned long long)c * F.plane + (unsigned long long)j * F.mid_w + x] = acc[s][c];
+					}
+#pragma unroll
+					for(int c = 0; c < NPL; c++) acc[s][c] = 0.0f;
+				}
+			}
+		}
+	}
+}
+
+// vertical pass, gather (upsampling or wide windows): one thread per (x, j).
+template<int NPL, int DEPTH>
+__global__ void __launch_bounds__(kVThreads) k_vgather(FJob F)
+{
+	extern __shared__ float s_tab[];
+	for(int k = threadIdx.x; k < F.dec_tab_floats; k += blockDim.x) s_tab[k] = F.dec_tab[k];
+	__syncthreads();
+	const int x = blockIdx.x * blockDim.x + threadIdx.x;
+	const int j = blockIdx.y;
+	if(x >= F.mid_w || j >= F.mid_h) return;
+	const int bpp = F.nphys * (DEPTH / 8);
+	const uint8_t *colbase = F.in + (size_t)(F.crop_x + x) * bpp;
+	float acc[NPL];
+#pragma unroll
+	for(int c = 0; c < NPL; c++) acc[c] = 0.0f;
+	for(int t = F.voff[j]; t < F.voff[j + 1]; t++) {
+		int row = F.vsrc[t];
+		if(row < 0) continue;   // transparent edge contributes 0
+		float val[NPL];
+		decode_pixel<NPL, DEPTH>(F, s_tab, colbase + (unsigned long long)(F.crop_y + row) * F.in_bpr, val);
+		float w = F.vw[t];
+#pragma unroll
+		for(int c = 0; c < NPL; c++) acc[c] = __fmaf_rn(val[c], w, acc[c]);
+	}
+#pragma unroll
+	for(int c = 0; c < NPL; c++) F.interm[(unsigned long long)c * F.plane + (unsigned long long)j * F.mid_w + x] = acc[c];
+}
+
+// ---------------------------------------------------------------------------
+// horizontal pass + guarded quantisation
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ int count_le_f(const float *t, int n, float v)
+{
+	int lo = 0, hi = n;
+	while(lo < hi) {
+		int mid = (lo + hi) >> 1;
+		if(t[mid] <= v) lo = mid + 1; else hi = mid;
+	}
+	return lo;
+}
+
+// Decides the output code for every value in [v - E, v + E]; returns -1 if
+// the interval straddles a decision of the reference.
+__device__ __forceinline__ int quantize_guarded(const FTail &T, float v, float E, int x, int y)
+{
+	v = fminf(fmaxf(v, 0.0f), 1.0f);
+	// slack for float rounding of the tables and of this arithmetic
+	const float Ep = __fmaf_rn(E, 1.0000001f, __fmaf_rn(fabsf(v), 2.4e-7f, 1e-37f));
+	const float lo_v = __fsub_rn(v, Ep), hi_v = __fadd_rn(v, Ep);
+	if(T.use_nc) {
+		int c = count_le_f(T.nc, 255, v);
+		if(c > 0 && !(T.nc[c - 1] < lo_v)) return -1;
+		if(c < 255 && !(T.nc[c] > hi_v)) return -1;
+		return c;
+	}
+	int k = count_le_f(T.U + 1, T.P, v);
+	bool near_lo = k > 0 && !(T.U[k] < lo_v);          // v within E of the bracket's lower edge
+	bool near_hi = k < T.P && !(T.U[k + 1] > hi_v);    // ... or of the next bracket
+	if(near_lo || near_hi) {
+		// With all codes available, the code at a bracket edge U[k] is k from
+		// both sides (the fraction is ~0 above it and ~1 below it), provided
+		// the uncertainty is far smaller than the distance to the thresholds.
+		if(T.cc != 0 || (near_lo && near_hi)) return -1;
+		int kk = near_lo ? k : k + 1;
+		// distance to the neighbouring codes on both sides of code kk
+		float step = fminf(__fsub_rn(T.rev[kk], T.rev[kk - 1]), kk < T.M ? __fsub_rn(T.rev[kk + 1], T.rev[kk]) : 1.0f);
+		if(!(__fmul_rn(Ep, 512.0f) < step)) return -1;
+		return T.code[kk];
+	}
+	const int lo = T.code[k], hi = T.code[k + 1];
+	if(k == T.P) return lo;
+	const float a = T.rev[lo], b = T.rev[hi];
+	const float den = __fsub_rn(b, a);
+	const float f = __fdiv_rn(__fsub_rn(v, a), den);
+	const float mf = __fdiv_rn(__fmaf_rn(fabsf(a) + fabsf(b), 1.2e-7f, Ep), den) + 1e-6f;
+	float thr = 0.5f;
+	if(T.dfam == IW_DITHERFAMILY_ORDERED) thr = ((float)dither_rank(T.dsub, x, y) + 0.5f) * 0.015625f;
+	int decided;
+	if(f >= thr + mf) decided = hi;
+	else if(f < thr - mf) decided = lo;
+	else return -1;
+	// inside the exactly-representable region the reference always picks lo
+	if(decided != lo && !(T.X[k] <= lo_v)) return -1;
+	return decided;
+}
+
+__device__ __forceinline__ void store_code_f(const FJob &F, int ch, int x, int y, unsigned int code)
+{
+	uint8_t *row = F.out + (unsigned long long)y * F.out_bpr;
+	if(F.out_depth == 8) row[F.out_n * x + ch] = (uint8_t)code;
+	else {
+		uint8_t *p = row + (size_t)(F.out_n * x + ch) * 2;
+		p[0] = (uint8_t)(code >> 8);
+		p[1] = (uint8_t)(code & 0xff);
+	}
+}
+
+template<int NPL>
+__global__ void __launch_bounds__(kHThreads) k_hpass_fast(FJob F)
+{
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	const int j = blockIdx.y;
+	if(i >= F.out_w || j >= F.out_h) return;
+	float v[NPL], T[NPL];
+#pragma unroll
+	for(int c = 0; c < NPL; c++) { v[c] = 0.0f; T[c] = 0.0f; }
+	const int t0 = F.hoff[i], t1 = F.hoff[i + 1];
+	for(int t = t0; t < t1; t++) {
+		const int src = __ldg(F.hsrc + t);
+		if(src < 0) continue;   // transparent edge: value 0
+		const float w = __ldg(F.hw + t), aw = fabsf(w);
+#pragma unroll
+		for(int c = 0; c < NPL; c++) {
+			const float I = __ldg(F.interm + (unsigned long long)c * F.plane + (unsigned long long)j * F.mid_w + src);
+			v[c] = __fmaf_rn(I, w, v[c]);
+			T[c] = __fmaf_rn(fabsf(I), aw, T[c]);
+		}
+	}
+	float E[NPL];
+#pragma unroll
+	for(int c = 0; c < NPL; c++) E[c] = __fmaf_rn(F.K1[c], T[c], F.K0[c]);
+
+	int codes[dev::kMaxCh];
+	int alpha_code = -1;
+	bool flag = false;
+	float A = 0.0f, EA = 0.0f;
+	for(int k = 0; k < F.mid_n; k++) {
+		const int m = F.order[k];
+		const int pl = F.plane_of[m];
+		float val = 0.0f, err = 0.0f;
+#pragma unroll
+		for(int c = 0; c < NPL; c++) if(c == pl) { val = v[c]; err = E[c]; }
+		const int oc = F.out_of[m];
+		if(F.is_alpha[m]) {
+			A = val;
+			// the reference divides by the float-rounded alpha: widen by one rounding
+			EA = __fmaf_rn(fabsf(val) + err, 6.0e-8f, err);
+		}
+		else if(F.unassoc[m]) {
+			if(alpha_code == 0 && F.blacken) { codes[oc] = 0; continue; }
+			const float den = __fsub_rn(A, EA);
+			if(!(den > 0.0f)) { flag = true; break; }
+			const float q = __fdiv_rn(val, A);
+			err = __fdiv_rn(__fmaf_rn(fabsf(q), EA, err), den);
+			err = __fmaf_rn(fabsf(q), 1.2e-7f, err);
+			val = q;
+		}
+		const int c = quantize_guarded(F.tail[oc], val, err, i, j);
+		if(c < 0) { flag = true; break; }
+		if(F.is_alpha[m]) alpha_code = c;
+		codes[oc] = c;
+	}
+	if(flag) {
+		int slot = atomicAdd(F.flag_count, 1);
+		F.flag_list[slot] = j * F.out_w + i;
+		return;
+	}
+	for(int oc = 0; oc < F.out_n; oc++) {
+		int c = codes[oc];
+		if(!F.out_alpha[oc]) {
+			if(F.negate) c = F.maxcc[oc] - c;
+			if(F.blacken && alpha_code == 0) c = 0;
+		}
+		store_code_f(F, oc, i, j, (unsigned int)c);
+	}
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+
+// Device copies of host tables.  The host tables are cached process-wide
+// (tables.cpp), so keying by their address is stable; derived float versions
+// are cached under (address, kind) together with a reference that keeps the
+// source alive.
+struct Cache {
+	std::mutex mu;
+	struct Entry { std::shared_ptr<const void> keep; std::shared_ptr<const void> derived; void *dev; };
+	std::map<std::pair<const void *, int>, Entry> dev;
+	void *scratch = nullptr;
+	size_t scratch_cap = 0;
+};
+
+Cache &cache()
+{
+	static Cache *c = new Cache();
+	return *c;
+}
+
+template<class T>
+const T *upload_vec(const std::vector<T> &v)
+{
+	void *d = nullptr;
+	if(cudaMalloc(&d, std::max<size_t>(16, v.size() * sizeof(T))) != cudaSuccess) return nullptr;
+	cudaMemcpy(d, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice);
+	return (const T *)d;
+}
+
+// Device copy of a persistent host table.
+template<class T>
+const T *dev_table(const std::shared_ptr<const std::vector<T>> &v)
+{
+	Cache &C = cache();
+	auto key = std::make_pair((const void *)v.get(), 0);
+	auto it = C.dev.find(key);
+	if(it != C.dev.end()) return (const T *)it->second.dev;
+	const T *d = upload_vec(*v);
+	if(d) C.dev[key] = {std::static_pointer_cast<const void>(v), nullptr, (void *)d};
+	return d;
+}
+
+// Device copy of a float table derived from a persistent double table.
+template<class Fn>
+const float *dev_derived(const std::shared_ptr<const std::vector<double>> &v, int kind, Fn make)
+{
+	Cache &C = cache();
+	auto key = std::make_pair((const void *)v.get(), kind);
+	auto it = C.dev.find(key);
+	if(it != C.dev.end()) return (const float *)it->second.dev;
+	std::shared_ptr<std::vector<float>> f = make(*v);
+	const float *d = upload_vec(*f);
+	if(d) C.dev[key] = {std::static_pointer_cast<const void>(v), std::static_pointer_cast<const void>(f), (void *)d};
+	return d;
+}
+
+std::shared_ptr<std::vector<float>> as_float(const std::vector<double> &v)
+{
+	auto f = std::make_shared<std::vector<float>>(v.size());
+	for(size_t i = 0; i < v.size(); i++) (*f)[i] = (float)v[i];   // +-inf stay infinite
+	return f;
+}
+
+// Decode table for the fast form, and its exactly measured error against the
+// double table (every code is evaluated with the same float operations the
+// device uses).
+struct DecodeTab {
+	std::shared_ptr<std::vector<float>> f;
+	double err = 0;
+};
+
+DecodeTab make_decode_tab(const std::vector<double> &t, int depth)
+{
+	DecodeTab r;
+	auto f = std::make_shared<std::vector<float>>();
+	if(depth == 8) {
+		f->resize(256);
+		for(int c = 0; c < 256; c++) {
+			(*f)[c] = (float)t[c];
+			r.err = std::max(r.err, fabs((double)(*f)[c] - t[c]));
+		}
+	}
+	else {
+		f->resize(8192);
+		for(int s = 0; s < 4096; s++) {
+			double a = t[s * 16], b = s < 4095 ? t[s * 16 + 16] : t[65535] + (t[65535] - t[65535 - 15]) / 15.0;
+			(*f)[2 * s] = (float)a;
+			(*f)[2 * s + 1] = (float)((b - a) / 16.0);
+		}
+		for(int c = 0; c < 65536; c++) {
+			float v = fmaf((float)(c & 15), (*f)[2 * (c >> 4) + 1], (*f)[2 * (c >> 4)]);
+			r.err = std::max(r.err, fabs((double)v - t[c]));
+		}
+	}
+	r.f = f;
+	return r;
+}
+
+// Streaming layout of a vertical weight set.
+struct StreamTab {
+	bool ok = false;
+	int pmin = 0, npos = 0, ns = 0;
+	std::vector<int> first_pos, last_pos, srcrow;
+	std::vector<int> pinfo;     // pairs
+	std::vector<float> sw;      // npos * 8
+};
+
+StreamTab make_stream(const Weights &W)
+{
+	StreamTab S;
+	if(W.kind != RowKind::Sum) return S;
+	const int n = W.n_out;
+	S.first_pos.resize(n);
+	S.last_pos.resize(n);
+	int pmin = INT32_MAX, pmax = INT32_MIN;
+	for(int j = 0; j < n; j++) {
+		if(W.off[j + 1] == W.off[j]) return S;   // empty window: use the gather kernel
+		int a = INT32_MAX, b = INT32_MIN;
+		for(int t = W.off[j]; t < W.off[j + 1]; t++) { a = std::min(a, W.pos[t]); b = std::max(b, W.pos[t]); }
+		S.first_pos[j] = a;
+		S.last_pos[j] = b;
+		if(j > 0 && (a < S.first_pos[j - 1] || b < S.last_pos[j - 1])) return S;   // not monotone
+		pmin = std::min(pmin, a);
+		pmax = std::max(pmax, b);
+	}
+	S.pmin = pmin;
+	S.npos = pmax - pmin + 1;
+	// widest set of simultaneously open windows
+	int ns = 0;
+	{
+		int lo = 0;
+		for(int j = 0; j < n; j++) {
+			while(S.last_pos[lo] < S.first_pos[j]) lo++;
+			ns = std::max(ns, j - lo + 1);
+		}
+	}
+	if(ns > 8) return S;
+	S.ns = ns <= 4 ? 4 : (ns <= 6 ? 6 : 8);
+	S.srcrow.assign(S.npos, -1);
+	S.sw.assign((size_t)S.npos * 8, 0.0f);
+	S.pinfo.assign((size_t)S.npos * 2, 0);
+	for(int j = 0; j < n; j++) {
+		for(int t = W.off[j]; t < W.off[j + 1]; t++) {
+			int q = W.pos[t] - pmin;
+			S.srcrow[q] = W.src[t];
+			S.sw[(size_t)q * 8 + (j % S.ns)] = (float)W.w[t];
+		}
+		int q = S.last_pos[j] - pmin;
+		if(S.pinfo[2 * q + 1] == 0) S.pinfo[2 * q] = j;
+		S.pinfo[2 * q + 1]++;
+	}
+	S.ok = true;
+	return S;
+}
+
+double gamma_n(int n, double u) { return n * u / (1.0 - n * u); }
+
+}  // namespace
+
+bool fast_eligible(const Plan &P, const Job &J, FastInfo &fi)
+{
+	if(P.in_sampletype != IW_SAMPLETYPE_UINT || (P.in_depth != 8 && P.in_depth != 16)) return false;
+	if(P.orient != 0 || P.reduced_in || P.apply_bk || P.intclamp) return false;
+	if(P.out_sampletype != IW_SAMPLETYPE_UINT || P.wsets[0].size() != 1 || P.wsets[1].size() != 1) return false;
+	for(int m = 0; m < P.mid_n; m++) {
+		if(P.mid[m].to_gray || P.mid[m].out_ch < 0) return false;
+	}
+	for(int oc = 0; oc < P.out_n; oc++) {
+		int f = P.out[oc].q.dfam;
+		if(f != IW_DITHERFAMILY_NONE && f != IW_DITHERFAMILY_ORDERED) return false;
+		if(P.out[oc].q.P > 65535) return false;
+	}
+	if(P.wsets[0][0]->edge_value != 0.0 || P.wsets[1][0]->edge_value != 0.0) return false;
+	(void)J;
+	fi.streaming = 0;
+	fi.slots = 0;
+	return true;
+}
+
+struct FastState {
+	FJob F;
+	Job J;
+	const void *vkernel = nullptr, *hkernel = nullptr;
+	dim3 vgrid, hgrid;
+	size_t vsmem = 0;
+};
+
+void fast_launch_impl(cudaStream_t st, void *state, void (*mark)(void *), void *markarg)
+{
+	FastState &S = *static_cast<FastState *>(state);
+	cudaMemsetAsync(S.F.flag_count, 0, sizeof(int), st);
+	void *fargs[] = {&S.F};
+	cudaLaunchKernel(S.vkernel, S.vgrid, dim3(kVThreads), fargs, S.vsmem, st);
+	mark(markarg);
+	cudaLaunchKernel(S.hkernel, S.hgrid, dim3(kHThreads), fargs, 0, st);
+	mark(markarg);
+	// exact re-evaluation of flagged pixels (recomputes the vertical pass too)
+	k_fix_flagged_fwd<<<2 * 152, 64, 0, st>>>(S.J, S.F.flag_count, S.F.flag_list);
+	mark(markarg);
+}
+
+void fast_release(FastInfo &fi)
+{
+	delete static_cast<FastState *>(fi.state);
+	fi.state = nullptr;
+}
+
+bool fast_prepare(cudaStream_t st, const Plan &P, Job &J, FastInfo &fi, std::string &err)
+{
+	Cache &C = cache();
+	std::lock_guard<std::mutex> lk(C.mu);
+	FJob F;
+	memset(&F, 0, sizeof(F));
+	const Weights &WV = *P.wsets[1][0], &WH = *P.wsets[0][0];
+
+	// ---- planes: distinct (input channel, transfer, premultiply) combinations
+	int nplanes = 0;
+	struct PK { int src, lin, premul; };
+	PK keys[kMaxPlanes];
+	std::shared_ptr<const std::vector<double>> coltab;
+	int alpha_plane = -1;
+	for(int m = 0; m < P.mid_n; m++) {
+		const MidChannel &mc = P.mid[m];
+		PK k{mc.in_ch < P.in_nphys ? mc.in_ch : -1, mc.lin_cs || P.cs_in.cstype == IW_CSTYPE_LINEAR, mc.unassoc};
+		int found = -1;
+		for(int q = 0; q < nplanes; q++)
+			if(keys[q].src == k.src && keys[q].lin == k.lin && keys[q].premul == k.premul) found = q;
+		if(found < 0) {
+			found = nplanes++;
+			keys[found] = k;
+			FPlane &pl = F.pl[found];
+			pl.src = k.src;
+			pl.premul = k.premul;
+			pl.table = !k.lin && k.src >= 0;
+			pl.inv = (float)(1.0 / (double)P.in_max);
+			if(pl.table) coltab = input_table(P.cs_in.cstype, P.cs_in.gamma, P.in_max, 1 << P.in_depth, false);
+		}
+		F.plane_of[m] = found;
+		F.out_of[m] = mc.out_ch;
+		F.is_alpha[m] = mc.ctype == IW_CHANNELTYPE_ALPHA;
+		F.unassoc[m] = mc.unassoc;
+		if(F.is_alpha[m]) alpha_plane = found;
+	}
+	F.npl = nplanes;
+	F.alpha_plane = alpha_plane;
+	F.alpha_src = (IW_IMGTYPE_HAS_ALPHA(P.in_logtype) && P.in_alpha < P.in_nphys) ? P.in_alpha : -1;
+	F.alpha_inv = (float)(1.0 / (double)P.in_max);
+
+	// decode error: table interpolation / rounding, or code*inv rounding
+	double e_dec = 0.0;
+	const double u = 1.0 / 16777216.0, ud = 1.0 / 9007199254740992.0;
+	const float *dec_tab = nullptr;
+	int dec_floats = 0;
+	if(coltab) {
+		static std::map<std::pair<const void *, int>, double> dec_err;   // measured once per table
+		double e = 0.0;
+		dec_tab = dev_derived(coltab, 100 + P.in_depth, [&](const std::vector<double> &t) {
+			DecodeTab dt = make_decode_tab(t, P.in_depth);
+			e = dt.err;
+			dec_err[std::make_pair((const void *)coltab.get(), P.in_depth)] = dt.err;
+			return dt.f;
+		});
+		e_dec = dec_err[std::make_pair((const void *)coltab.get(), P.in_depth)];
+		dec_floats = P.in_depth == 8 ? 256 : 8192;
+		if(!dec_tab) { err = "Out of GPU memory (fast tables)"; return false; }
+	}
+	e_dec = std::max(e_dec, 2.0 * u);   // code*inv: 1/maxcc rounded, product rounded
+	F.dec_tab = dec_tab;
+	F.dec_tab_floats = dec_floats;
+
+	// ---- error model constants per plane
+	const int nv = std::max(1, WV.max_taps), nh = std::max(1, WH.max_taps);
+	const double W1v = WV.kind == RowKind::Copy ? 1.0 : WV.wsum_abs_max, W1h = WH.kind == RowKind::Copy ? 1.0 : WH.wsum_abs_max;
+	const double Wnv = WV.kind == RowKind::Copy ? 0.0 : WV.wsum_neg_max;
+	for(int q = 0; q < nplanes; q++) {
+		double r_dec = keys[q].premul ? 3.0 * u : 0.0;
+		double c1 = (r_dec + 2.0 * u + gamma_n(nv + 1, u) + gamma_n(nv + 1, ud)) * 1.01;
+		double c2 = (u + gamma_n(nh + 1, u) + gamma_n(nh + 1, ud)) * 1.01;
+		double ed = e_dec * (keys[q].premul ? 1.0 : 1.0);
+		double K0 = (ed * W1v * W1h + 2.02 * c1 * Wnv * W1h) * 1.05;
+		double K1 = (1.01 * c1 + c2) * 1.05;
+		F.K0[q] = (float)K0;
+		F.K1[q] = (float)K1;
+	}
+
+	// ---- geometry and buffers (shared with the plain form's Job)
+	F.in = J.in;
+	F.in_bpr = J.in_bpr;
+	F.crop_x = P.crop_x;
+	F.crop_y = P.crop_y;
+	F.nphys = P.in_nphys;
+	F.depth = P.in_depth;
+	F.mid_w = J.mid_w;
+	F.mid_h = J.mid_h;
+	F.interm = J.interm;
+	F.plane = J.interm_plane;
+	F.out_w = J.out_w; F.out_h = J.out_h; F.out_n = J.out_n; F.out_depth = J.out_depth;
+	F.out = J.out;
+	F.out_bpr = J.out_bpr;
+	F.mid_n = P.mid_n;
+	for(int k = 0; k < P.mid_n; k++) F.order[k] = J.order[k];
+	F.negate = P.negate;
+	F.blacken = P.blacken;
+
+	// ---- per-call device arrays (weights, streaming tables)
+	StreamTab S = make_stream(WV);
+	std::vector<uint8_t> blob;
+	auto add = [&](const void *p, size_t n) {
+		size_t off = (blob.size() + 255) & ~(size_t)255;
+		blob.resize(off + n);
+		if(n) memcpy(blob.data() + off, p, n);
+		return off;
+	};
+	std::vector<float> hwf(WH.w.begin(), WH.w.end()), vwf(WV.w.begin(), WV.w.end());
+	size_t o_hoff = add(WH.off.data(), WH.off.size() * 4), o_hsrc = add(WH.src.data(), WH.src.size() * 4);
+	size_t o_hw = add(hwf.data(), hwf.size() * 4);
+	size_t o_voff = add(WV.off.data(), WV.off.size() * 4), o_vsrc = add(WV.src.data(), WV.src.size() * 4);
+	size_t o_vw = add(vwf.data(), vwf.size() * 4);
+	size_t o_fp = 0, o_lp = 0, o_src = 0, o_pi = 0, o_sw = 0;
+	if(S.ok) {
+		o_fp = add(S.first_pos.data(), S.first_pos.size() * 4);
+		o_lp = add(S.last_pos.data(), S.last_pos.size() * 4);
+		o_src = add(S.srcrow.data(), S.srcrow.size() * 4);
+		o_pi = add(S.pinfo.data(), S.pinfo.size() * 4);
+		o_sw = add(S.sw.data(), S.sw.size() * 4);
+	}
+	const size_t flag_bytes = 256 + (size_t)J.out_w * J.out_h * 4;
+	size_t need = blob.size() + 256 + flag_bytes;
+	if(need > C.scratch_cap) {
+		if(C.scratch) cudaFree(C.scratch);
+		C.scratch = nullptr;
+		C.scratch_cap = 0;
+		if(cudaMalloc(&C.scratch, need + need / 8) != cudaSuccess) { err = "Out of GPU memory (fast form)"; return false; }
+		C.scratch_cap = need + need / 8;
+	}
+	uint8_t *base = (uint8_t *)C.scratch;
+	cudaMemcpyAsync(base, blob.data(), blob.size(), cudaMemcpyHostToDevice, st);
+	size_t flag_off = (blob.size() + 255) & ~(size_t)255;
+	F.flag_count = (int *)(base + flag_off);
+	F.flag_list = (int *)(base + flag_off + 256);
+	F.hoff = (const int *)(base + o_hoff);
+	F.hsrc = (const int *)(base + o_hsrc);
+	F.hw = (const float *)(base + o_hw);
+	F.voff = (const int *)(base + o_voff);
+	F.vsrc = (const int *)(base + o_vsrc);
+	F.vw = (const float *)(base + o_vw);
+	if(S.ok) {
+		F.first_pos = (const int *)(base + o_fp);
+		F.last_pos = (const int *)(base + o_lp);
+		F.srcrow = (const int *)(base + o_src);
+		F.pinfo = (const int2 *)(base + o_pi);
+		F.sw = (const float *)(base + o_sw);
+		F.pmin = S.pmin;
+		F.npos = S.npos;
+		F.ns = S.ns;
+	}
+
+	// ---- quantisation tables (float copies, cached)
+	for(int oc = 0; oc < P.out_n; oc++) {
+		const Quant &q = P.out[oc].q;
+		FTail &T = F.tail[oc];
+		T.P = q.P; T.M = q.maxcc; T.cc = q.cc; T.use_nc = q.use_nc; T.dfam = q.dfam; T.dsub = q.dsub;
+		T.U = dev_derived(q.U, 1, as_float);
+		T.X = dev_derived(q.X, 1, as_float);
+		T.code = dev_table(q.code);
+		T.rev = dev_derived(q.rev, 1, as_float);
+		T.nc = q.use_nc ? dev_derived(q.nc, 1, as_float) : nullptr;
+		if(!T.U || !T.X || !T.code || !T.rev || (q.use_nc && !T.nc)) { err = "Out of GPU memory (fast tables)"; return false; }
+		F.maxcc[oc] = P.out[oc].maxcc;
+		F.out_alpha[oc] = P.out[oc].ctype == IW_CHANNELTYPE_ALPHA;
+	}
+
+	// ---- kernel selection
+	auto *FS = new FastState();
+	const int gx = (F.mid_w + kVThreads - 1) / kVThreads;
+	FS->vsmem = (size_t)dec_floats * sizeof(float);
+	FS->vgrid = dim3(gx, F.mid_h);
+#define IWG_VSTREAM(NS_, NPL_, D_) \
+	if(!FS->vkernel && S.ns == NS_ && nplanes == NPL_ && P.in_depth == D_) { \
+		int bands = std::max(1, std::min(F.mid_h, (4 * 152 + gx - 1) / gx)); \
+		F.rows_per_band = (F.mid_h + bands - 1) / bands; \
+		bands = (F.mid_h + F.rows_per_band - 1) / F.rows_per_band; \
+		FS->vkernel = (const void *)k_vstream<NS_, NPL_, D_>; \
+		FS->vgrid = dim3(gx, bands); \
+	}
+#define IWG_VGATHER(NPL_, D_) \
+	if(!FS->vkernel && nplanes == NPL_ && P.in_depth == D_) FS->vkernel = (const void *)k_vgather<NPL_, D_>;
+	if(S.ok) {
+		IWG_VSTREAM(4, 1, 8) IWG_VSTREAM(4, 2, 8) IWG_VSTREAM(4, 3, 8) IWG_VSTREAM(4, 4, 8)
+		IWG_VSTREAM(6, 1, 8) IWG_VSTREAM(6, 2, 8) IWG_VSTREAM(6, 3, 8) IWG_VSTREAM(6, 4, 8)
+		IWG_VSTREAM(8, 1, 8) IWG_VSTREAM(8, 2, 8) IWG_VSTREAM(8, 3, 8) IWG_VSTREAM(8, 4, 8)
+		IWG_VSTREAM(4, 1, 16) IWG_VSTREAM(4, 2, 16) IWG_VSTREAM(4, 3, 16) IWG_VSTREAM(4, 4, 16)
+		IWG_VSTREAM(6, 1, 16) IWG_VSTREAM(6, 2, 16) IWG_VSTREAM(6, 3, 16) IWG_VSTREAM(6, 4, 16)
+		IWG_VSTREAM(8, 1, 16) IWG_VSTREAM(8, 2, 16) IWG_VSTREAM(8, 3, 16) IWG_VSTREAM(8, 4, 16)
+	}
+	IWG_VGATHER(1, 8) IWG_VGATHER(2, 8) IWG_VGATHER(3, 8) IWG_VGATHER(4, 8)
+	IWG_VGATHER(1, 16) IWG_VGATHER(2, 16) IWG_VGATHER(3, 16) IWG_VGATHER(4, 16)
+#undef IWG_VSTREAM
+#undef IWG_VGATHER
+	if(!FS->vkernel) { delete FS; err = "fast form: no kernel for this layout"; return false; }
+	switch(nplanes) {
+	case 1: FS->hkernel = (const void *)k_hpass_fast<1>; break;
+	case 2: FS->hkernel = (const void *)k_hpass_fast<2>; break;
+	case 3: FS->hkernel = (const void *)k_hpass_fast<3>; break;
+	default: FS->hkernel = (const void *)k_hpass_fast<4>; break;
+	}
+	FS->hgrid = dim3((F.out_w + kHThreads - 1) / kHThreads, F.out_h);
+	FS->F = F;
+	FS->J = J;
+	fi.state = FS;
+	fi.launches = 3;
+	fi.launch_fn = fast_launch_impl;
+	fi.streaming = S.ok;
+	fi.slots = S.ns;
+	fi.flag_count_dev = F.flag_count;
+	return true;
+}
+
+}  // namespace iwg

@@ -1,0 +1,41 @@
+// fastpath.cuh -- interface of the FP32 + guard-band form (fastpath.cu).
+#pragma once
+
+#include <string>
+#include <cuda_runtime.h>
+
+#include "device.cuh"
+
+namespace iwg {
+
+struct Plan;
+
+struct FastInfo {
+	int streaming = 0;   // vertical pass streams input rows into register slots
+	int slots = 0;       // register slots per column (streaming)
+	int *flag_count_dev = nullptr;   // device counter of pixels re-evaluated exactly
+	void *state = nullptr;            // prepared launch state (fastpath.cu)
+	int launches = 0;
+	void (*launch_fn)(cudaStream_t, void *, void (*)(void *), void *) = nullptr;
+};
+
+// Whether the plan can run in the fast form (and how).
+bool fast_eligible(const Plan &P, const dev::Job &J, FastInfo &fi);
+
+// Uploads the fast form's per-call tables on 'st' and prepares its launches.
+bool fast_prepare(cudaStream_t st, const Plan &P, dev::Job &J, FastInfo &fi, std::string &err);
+
+// Launches the prepared fast form: vertical pass, horizontal pass with the
+// guarded tail, exact re-evaluation of flagged pixels.  'mark' is called after
+// each launch group.  Returns the number of kernel launches.
+template<class Mark>
+int fast_launch(cudaStream_t st, FastInfo &fi, Mark mark)
+{
+	fi.launch_fn(st, fi.state, [](void *m) { (*static_cast<Mark *>(m))(); }, &mark);
+	return fi.launches;
+}
+
+// Frees the prepared state.
+void fast_release(FastInfo &fi);
+
+}  // namespace iwg

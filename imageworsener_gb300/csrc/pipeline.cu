@@ -1,0 +1,690 @@
+// pipeline.cu -- the GPU pixel pipeline of iw_process_image().
+//
+// Two forms compute the same bytes:
+//   * plain  (FP64): the reference's arithmetic sample for sample -- a
+//     vertical pass into a float intermediate (src/imagew-main.c:831-927), a
+//     horizontal pass fused with the quantisation tail
+//     (src/imagew-main.c:929-1155), and a serial scan for error-diffusion and
+//     random dither, whose order the reference fixes;
+//   * fast  (FP32 + guard band, fastpath.cu): FP32 resampling with a
+//     rigorous per-sample error bound; samples whose error interval touches a
+//     quantisation decision are recomputed here in FP64.  Integer output is
+//     identical to the plain form's.
+// Host code here packs the plan into a device Job, manages device memory and
+// launches the kernels on the library's stream.
+#include "iwg_internal.h"
+#include "device.cuh"
+#include "fastpath.cuh"
+#include "imagew_gb300.h"
+
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+namespace iwg {
+
+using namespace dev;
+
+// ===========================================================================
+// Plain-form kernels
+// ===========================================================================
+
+// Vertical pass: one thread per (column x, intermediate row j), all channels.
+__global__ void k_vpass_exact(Job J)
+{
+	int x = blockIdx.x * blockDim.x + threadIdx.x;
+	int j = blockIdx.y;
+	if(x >= J.mid_w || j >= J.mid_h) return;
+	for(int m = 0; m < J.mid_n; m++) {
+		const DMid &mc = J.mid[m];
+		const DWeights &W = J.wv[mc.wv];
+		double s = 0.0;
+		if(W.kind == 1) {
+			int src = W.src[j];
+			s = src < 0 ? 0.0 : decode_exact(J, mc, x, src);
+		}
+		else {
+			for(int t = W.off[j]; t < W.off[j + 1]; t++) {
+				int src = W.src[t];
+				double v = src >= 0 ? decode_exact(J, mc, x, src) : W.edge_value;
+				s = dadd(s, dmul(v, W.w[t]));
+			}
+		}
+		if(J.intclamp) s = s < 0.0 ? 0.0 : (s > 1.0 ? 1.0 : s);
+		J.interm[(unsigned long long)m * J.interm_plane + (unsigned long long)j * J.mid_w + x] = __double2float_rn(s);
+	}
+}
+
+// Exact intermediate value of channel m at (column x, row j): read from the
+// plain form's vertical pass, or recomputed (the fast form keeps FP32 values
+// in its intermediate buffer).
+template<bool RECOMPUTE>
+__device__ __forceinline__ double interm_exact(const Job &J, int m, int x, int j)
+{
+	if(!RECOMPUTE) return (double)J.interm[(unsigned long long)m * J.interm_plane + (unsigned long long)j * J.mid_w + x];
+	const DMid &mc = J.mid[m];
+	const DWeights &W = J.wv[mc.wv];
+	double s = 0.0;
+	if(W.kind == 1) {
+		int src = W.src[j];
+		s = src < 0 ? 0.0 : decode_exact(J, mc, x, src);
+	}
+	else {
+		for(int t = W.off[j]; t < W.off[j + 1]; t++) {
+			int src = W.src[t];
+			double v = src >= 0 ? decode_exact(J, mc, x, src) : W.edge_value;
+			s = dadd(s, dmul(v, W.w[t]));
+		}
+	}
+	if(J.intclamp) s = s < 0.0 ? 0.0 : (s > 1.0 ? 1.0 : s);
+	return (double)__double2float_rn(s);
+}
+
+// Horizontal pass of one channel for output pixel (i, j).
+template<bool RECOMPUTE>
+__device__ __forceinline__ double hsum_exact(const Job &J, int m, int i, int j)
+{
+	const DWeights &W = J.wh[J.mid[m].wh];
+	double s = 0.0;
+	if(W.kind == 1) {
+		int src = W.src[i];
+		s = src < 0 ? 0.0 : interm_exact<RECOMPUTE>(J, m, src, j);
+	}
+	else {
+		for(int t = W.off[i]; t < W.off[i + 1]; t++) {
+			int src = W.src[t];
+			double v = src >= 0 ? interm_exact<RECOMPUTE>(J, m, src, j) : W.edge_value;
+			s = dadd(s, dmul(v, W.w[t]));
+		}
+	}
+	if(J.intclamp) s = s < 0.0 ? 0.0 : (s > 1.0 ? 1.0 : s);
+	return s;
+}
+
+// Unassociate alpha and composite a late background
+// (src/imagew-main.c:1079-1115).  'a' is the float-rounded resampled alpha.
+__device__ __forceinline__ double unassoc_and_bkgd(const Job &J, const DMid &mc, const DOut &oc, double v,
+	double a, int alt, bool is_alpha)
+{
+	double bka = J.bk_trns ? (alt ? J.bk2_alpha : J.bk1_alpha) : 0.0;
+	if(mc.unassoc) {
+		if(a != 0.0) v = ddiv(v, a);
+		if(J.bk_late) {
+			double bc = alt ? oc.bk2 : oc.bk1;
+			if(J.bk_trns) v = dadd(dmul(v, a), dmul(dmul(bc, bka), dsub(1.0, a)));
+			else v = dadd(dmul(v, a), dmul(bc, dsub(1.0, a)));
+		}
+	}
+	else if(is_alpha && J.bk_trns) {
+		v = dadd(v, dmul(bka, dsub(1.0, v)));
+	}
+	return v;
+}
+
+// Quantise / store every channel of output pixel (i, j) exactly.  Used by the
+// plain form for all pixels and by the fast form for flagged pixels.
+template<bool RECOMPUTE>
+__device__ void pixel_exact(const Job &J, int i, int j, bool apply_post)
+{
+	double a = 0.0;
+	int alpha_code = -1;
+	int codes[dev::kMaxCh];
+	int alt = checker_alt(J, i, j);
+	for(int k = 0; k < J.mid_n; k++) {
+		int m = J.order[k];
+		const DMid &mc = J.mid[m];
+		bool is_alpha = mc.ctype == IW_CHANNELTYPE_ALPHA;
+		double s = hsum_exact<RECOMPUTE>(J, m, i, j);
+		if(is_alpha) a = (double)__double2float_rn(s);
+		int oc = mc.out_ch;
+		if(oc < 0) continue;
+		const DOut &o = J.outc[oc];
+		double v = unassoc_and_bkgd(J, mc, o, s, a, alt, is_alpha);
+		if(J.out_float) {
+			float f = __double2float_rn(v);
+			if(J.negate && !is_alpha) f = __fsub_rn(1.0f, f);
+			store_float(J, oc, i, j, f);
+			continue;
+		}
+		if(o.scan) {
+			J.scanbuf[((unsigned long long)oc * J.out_h + j) * J.out_w + i] = v;
+			codes[oc] = -1;
+			continue;
+		}
+		int c = quantize_exact(o.q, v, i, j);
+		if(is_alpha) alpha_code = c;
+		codes[oc] = c;
+	}
+	if(J.out_float) return;
+	for(int oc = 0; oc < J.out_n; oc++) {
+		int c = codes[oc];
+		if(c < 0) continue;
+		if(apply_post) {
+			bool is_alpha = J.outc[oc].ctype == IW_CHANNELTYPE_ALPHA;
+			if(!is_alpha) {
+				if(J.negate) c = J.outc[oc].maxcc - c;
+				if(J.blacken && alpha_code == 0) c = 0;
+			}
+		}
+		store_code(J, oc, i, j, (unsigned int)c);
+	}
+}
+
+__global__ void k_hpass_exact(Job J)
+{
+	int i = blockIdx.x * blockDim.x + threadIdx.x;
+	int j = blockIdx.y;
+	if(i >= J.out_w || j >= J.out_h) return;
+	pixel_exact<false>(J, i, j, !J.any_scan);
+}
+
+// Serial scan for error-diffusion and random dither of one output channel
+// (src/imagew-main.c:487-567, :1072-1136).  The reference visits samples in a
+// fixed order (serpentine rows for error diffusion) and each decision depends
+// on the previous ones, so one thread walks the whole channel.
+__device__ unsigned int prng_next(unsigned int &mult, unsigned int &carry)
+{
+	unsigned long long x = 0xfff0bf23ULL * mult + carry;
+	carry = (unsigned int)(x >> 32);
+	mult = 0xffffffffU - (unsigned int)(x & 0xffffffffULL);
+	return mult;
+}
+
+__global__ void k_scan(Job J, int oc)
+{
+	if(threadIdx.x != 0) return;
+	const DOut &o = J.outc[oc];
+	const DQuant &q = o.q;
+	const int W = J.out_w;
+	const bool errdiff = q.dfam == IW_DITHERFAMILY_ERRDIFF;
+	double *e0 = J.errbuf + (unsigned long long)oc * 3 * W, *e1 = e0 + W, *e2 = e1 + W;
+	unsigned int mult = 0, carry = 0;
+	if(q.dfam == IW_DITHERFAMILY_RANDOM) {
+		int s = (q.dsub == IW_DITHERSUBTYPE_SAMEPATTERN && o.ctype != IW_CHANNELTYPE_ALPHA) ? J.seed : J.seed + o.ctype;
+		mult = 0x03333333U + (unsigned int)s;
+		carry = 0x05555555U + (unsigned int)s;
+	}
+	// error-diffusion kernels: numerators over a denominator
+	// (positions: x+1 x+2 / x-2 x-1 x x+1 x+2 / same on the row after)
+	const signed char num[8][12] = {
+		{7,0, 0,3,5,1,0, 0,0,0,0,0}, {7,5, 3,5,7,5,3, 1,3,5,3,1}, {8,4, 2,4,8,4,2, 1,2,4,2,1},
+		{8,4, 2,4,8,4,2, 0,0,0,0,0}, {5,3, 2,4,5,4,2, 0,2,3,2,0}, {4,3, 1,2,3,2,1, 0,0,0,0,0},
+		{2,0, 0,1,1,0,0, 0,0,0,0,0}, {1,1, 0,1,1,1,0, 0,0,1,0,0}};
+	const double den[8] = {16.0, 48.0, 42.0, 32.0, 32.0, 16.0, 4.0, 8.0};
+	int sub = (q.dsub >= 0 && q.dsub <= 7) ? q.dsub : 0;
+	double c[12];
+	for(int k = 0; k < 12; k++) c[k] = ddiv((double)num[sub][k], den[sub]);
+	if(errdiff)
+		for(int x = 0; x < 3 * W; x++) e0[x] = 0.0;
+
+	for(int y = 0; y < J.out_h; y++) {
+		const int f = (y % 2) ? -1 : 1;
+		for(int z = 0; z < W; z++) {
+			int x = (errdiff && (y % 2)) ? W - 1 - z : z;
+			double v = J.scanbuf[((unsigned long long)oc * J.out_h + y) * W + x];
+			if(v < 0.0) v = 0.0;
+			if(v > 1.0) v = 1.0;
+			int code;
+			if(errdiff) {
+				v = dadd(v, e0[x]);
+				if(v > 1.0) v = 1.0;
+				else if(v < 0.0) v = 0.0;
+			}
+			if(v != v) {
+				code = 0;
+				if(!errdiff) (void)prng_next(mult, carry);
+			}
+			else {
+				Bracket b = bracket_exact(q, v);
+				if(b.exact) {
+					code = b.lo;
+					if(!errdiff) (void)prng_next(mult, carry);   // one draw per sample
+				}
+				else if(errdiff) {
+					double err;
+					if(b.d_hi <= b.d_lo) { err = -b.d_hi; code = b.hi; }
+					else { err = b.d_lo; code = b.lo; }
+					// scatter the error (src/imagew-main.c:545-566)
+					if(x - f >= 0 && x - f < W) {
+						if(x - 2 * f >= 0 && x - 2 * f < W) {
+							e1[x - 2 * f] = dadd(e1[x - 2 * f], dmul(err, c[2]));
+							e2[x - 2 * f] = dadd(e2[x - 2 * f], dmul(err, c[7]));
+						}
+						e1[x - f] = dadd(e1[x - f], dmul(err, c[3]));
+						e2[x - f] = dadd(e2[x - f], dmul(err, c[8]));
+					}
+					e1[x] = dadd(e1[x], dmul(err, c[4]));
+					e2[x] = dadd(e2[x], dmul(err, c[9]));
+					if(x + f >= 0 && x + f < W) {
+						e0[x + f] = dadd(e0[x + f], dmul(err, c[0]));
+						e1[x + f] = dadd(e1[x + f], dmul(err, c[5]));
+						e2[x + f] = dadd(e2[x + f], dmul(err, c[10]));
+						if(x + 2 * f >= 0 && x + 2 * f < W) {
+							e0[x + 2 * f] = dadd(e0[x + 2 * f], dmul(err, c[1]));
+							e1[x + 2 * f] = dadd(e1[x + 2 * f], dmul(err, c[6]));
+							e2[x + 2 * f] = dadd(e2[x + 2 * f], dmul(err, c[11]));
+						}
+					}
+				}
+				else {
+					double fr = ddiv(b.d_lo, dadd(b.d_lo, b.d_hi));
+					double thr = ddiv((double)prng_next(mult, carry), (double)0xffffffffU);
+					code = fr >= thr ? b.hi : b.lo;
+				}
+			}
+			store_code(J, oc, x, y, (unsigned int)code);
+		}
+		if(errdiff) {
+			for(int x = 0; x < W; x++) {
+				e0[x] = e1[x];
+				e1[x] = e2[x];
+				e2[x] = 0.0;
+			}
+		}
+	}
+}
+
+// Negation and blackening of fully transparent pixels, for outputs whose
+// channels were (partly) quantised by the serial scan.
+__global__ void k_finalize(Job J)
+{
+	int i = blockIdx.x * blockDim.x + threadIdx.x;
+	int j = blockIdx.y;
+	if(i >= J.out_w || j >= J.out_h) return;
+	int alpha_oc = -1;
+	for(int oc = 0; oc < J.out_n; oc++) if(J.outc[oc].ctype == IW_CHANNELTYPE_ALPHA) alpha_oc = oc;
+	bool clear = J.blacken && alpha_oc >= 0 && load_code(J, alpha_oc, i, j) == 0;
+	for(int oc = 0; oc < J.out_n; oc++) {
+		if(oc == alpha_oc) continue;
+		unsigned int c = load_code(J, oc, i, j);
+		if(J.negate) c = (unsigned int)J.outc[oc].maxcc - c;
+		if(clear) c = 0;
+		store_code(J, oc, i, j, c);
+	}
+}
+
+// Exact re-evaluation of the pixels the fast form flagged: the vertical pass
+// is recomputed in FP64 for just the columns those pixels read.
+__global__ void k_fix_flagged_fwd(Job J, const int *count, const int *list)
+{
+	int n = *count;
+	for(int f = blockIdx.x * blockDim.x + threadIdx.x; f < n; f += gridDim.x * blockDim.x) {
+		int p = list[f];
+		pixel_exact<true>(J, p % J.out_w, p / J.out_w, true);
+	}
+}
+
+// ===========================================================================
+// Host side: device memory, tables, launches
+// ===========================================================================
+
+namespace {
+
+struct DevBuf {
+	void *p = nullptr;
+	size_t cap = 0;
+	bool ensure(size_t n)
+	{
+		if(n <= cap) return true;
+		if(p) cudaFree(p);
+		p = nullptr;
+		cap = 0;
+		size_t want = n + n / 8 + 4096;
+		if(cudaMalloc(&p, want) != cudaSuccess) { p = nullptr; return false; }
+		cap = want;
+		return true;
+	}
+};
+
+// Per-process device state: one stream, grow-only buffers and a cache of
+// device copies of the shared host tables.  Calls are serialised on it.
+struct DeviceState {
+	std::mutex mu;
+	bool init = false;
+	std::string init_error;
+	int device = 0;
+	cudaStream_t stream = nullptr;
+	DevBuf in, interm, out, scan, err, params, flags;
+	std::map<const void *, std::pair<std::shared_ptr<const void>, void *>> table_cache;
+	std::vector<uint8_t> staging;
+};
+
+DeviceState &state()
+{
+	static DeviceState *s = new DeviceState();   // never destroyed: outlives other statics
+	return *s;
+}
+
+bool ensure_init(DeviceState &S, std::string &err)
+{
+	if(S.init) return true;
+	int n = 0;
+	cudaError_t e = cudaGetDeviceCount(&n);
+	if(e != cudaSuccess || n < 1) {
+		err = std::string("No CUDA device available: ") + cudaGetErrorString(e);
+		return false;
+	}
+	cudaGetDevice(&S.device);
+	if(cudaStreamCreateWithFlags(&S.stream, cudaStreamNonBlocking) != cudaSuccess) {
+		err = "cudaStreamCreate failed";
+		return false;
+	}
+	S.init = true;
+	return true;
+}
+
+template<class T>
+const T *cached_table(DeviceState &S, const std::shared_ptr<const std::vector<T>> &v)
+{
+	if(!v) return nullptr;
+	auto it = S.table_cache.find(v.get());
+	if(it != S.table_cache.end()) return (const T *)it->second.second;
+	void *d = nullptr;
+	size_t n = v->size() * sizeof(T);
+	if(cudaMalloc(&d, n ? n : 16) != cudaSuccess) return nullptr;
+	cudaMemcpy(d, v->data(), n, cudaMemcpyHostToDevice);
+	S.table_cache[v.get()] = {std::static_pointer_cast<const void>(v), d};
+	return (const T *)d;
+}
+
+// Packs per-call arrays into one staging block uploaded with a single copy.
+struct Packer {
+	std::vector<uint8_t> &buf;
+	explicit Packer(std::vector<uint8_t> &b) : buf(b) { buf.clear(); }
+	template<class T>
+	size_t add(const T *p, size_t n)
+	{
+		size_t off = (buf.size() + 255) & ~(size_t)255;
+		buf.resize(off + n * sizeof(T));
+		if(n) memcpy(buf.data() + off, p, n * sizeof(T));
+		return off;
+	}
+};
+
+struct Fixup { size_t off; const void **slot; };
+
+}  // namespace
+
+template<class Mark>
+int plain_launch(cudaStream_t st, const Plan &P, const Job &J, Mark mark);
+
+bool run_pipeline(iw_context *ctx, Plan &P, int warmup, int iters)
+{
+	DeviceState &S = state();
+	std::lock_guard<std::mutex> lk(S.mu);
+	std::string err;
+	if(!ensure_init(S, err)) {
+		iw_set_error(ctx, err.c_str());
+		return false;
+	}
+
+	// host output image, owned by the context
+	ctx->img2.bpr = P.out_bpr;
+	ctx->img2.pixels = (iw_byte *)iw_malloc_large(ctx, P.out_bpr, P.out_h);
+	if(!ctx->img2.pixels) return false;
+
+	Job J;
+	memset(&J, 0, sizeof(J));
+	const int phys_h = P.orient >= 4 ? P.img1_w : P.img1_h;
+	const size_t in_bytes = P.in_bpr * (size_t)phys_h;
+	J.in_bpr = P.in_bpr;
+	J.in_depth = P.in_depth;
+	J.in_float = P.in_sampletype == IW_SAMPLETYPE_FLOATINGPOINT;
+	J.in_nphys = P.in_nphys;
+	J.orient = P.orient;
+	J.img1_w = P.img1_w;
+	J.img1_h = P.img1_h;
+	J.crop_x = P.crop_x; J.crop_y = P.crop_y; J.crop_w = P.crop_w; J.crop_h = P.crop_h;
+	J.in_alpha = P.in_alpha;
+	J.mid_n = P.mid_n;
+	J.mid_alpha = P.mid_alpha;
+	J.mid_w = P.crop_w;
+	J.mid_h = P.out_h;
+	J.interm_plane = (unsigned long long)J.mid_w * J.mid_h;
+	J.out_bpr = P.out_bpr;
+	J.out_w = P.out_w; J.out_h = P.out_h; J.out_n = P.out_n; J.out_depth = P.out_depth;
+	J.out_float = P.out_sampletype == IW_SAMPLETYPE_FLOATINGPOINT;
+	J.apply_bk = P.apply_bk;
+	J.bk_late = P.apply_bk && P.bk_strategy == BK_LATE;
+	J.bk_early = P.apply_bk && P.bk_strategy == BK_EARLY;
+	J.bk_checker = P.apply_bk && P.bk_checker;
+	J.bk_trns = P.bk_trns;
+	J.bk1_alpha = P.bk1_alpha; J.bk2_alpha = P.bk2_alpha;
+	J.check_size = P.check_size < 1 ? 1 : P.check_size;
+	J.check_ox = P.check_origin[0]; J.check_oy = P.check_origin[1];
+	J.gsf = P.gsf;
+	for(int k = 0; k < 3; k++) J.gsw[k] = P.gsw[k];
+	J.intclamp = P.intclamp;
+	J.negate = P.negate;
+	J.blacken = P.blacken;
+	J.seed = ctx->seed;
+
+	// processing order: alpha first, then the others in channel order
+	{
+		int n = 0;
+		if(P.mid_alpha >= 0) J.order[n++] = P.mid_alpha;
+		for(int m = 0; m < P.mid_n; m++) if(m != P.mid_alpha) J.order[n++] = m;
+	}
+
+	// ---- tables ----
+	Packer pk(S.staging);
+	std::vector<Fixup> fix;
+	auto put = [&](const void **slot, size_t off) { fix.push_back({off, slot}); };
+	std::vector<std::vector<float>> wf_store;
+	for(int d = 0; d < 2; d++) {
+		for(size_t k = 0; k < P.wsets[d].size(); k++) {
+			const Weights &W = *P.wsets[d][k];
+			DWeights &D = d == 0 ? J.wh[k] : J.wv[k];
+			D.kind = (int)W.kind;
+			D.n_in = W.n_in;
+			D.n_out = W.n_out;
+			D.max_taps = W.max_taps;
+			D.edge_value = W.edge_value;
+			wf_store.emplace_back(W.w.begin(), W.w.end());
+			put((const void **)&D.off, pk.add(W.off.data(), W.off.size()));
+			put((const void **)&D.src, pk.add(W.src.data(), W.src.size()));
+			put((const void **)&D.w, pk.add(W.w.data(), W.w.size()));
+			put((const void **)&D.wf, pk.add(wf_store.back().data(), wf_store.back().size()));
+			put((const void **)&D.pos, pk.add(W.pos.data(), W.pos.size()));
+		}
+	}
+	// decode tables (cached): per input channel, with the transfer each
+	// intermediate channel uses
+	auto decode_tab = [&](int ch, bool linear) -> const double * {
+		if(ch >= P.in_nphys || P.in_sampletype == IW_SAMPLETYPE_FLOATINGPOINT) return nullptr;
+		int ncodes = 1 << P.in_depth;
+		int maxcc = P.reduced_in ? (int)P.in_maxcc_d[ch] : P.in_max;
+		return cached_table(S, input_table(P.cs_in.cstype, P.cs_in.gamma, maxcc, ncodes, linear));
+	};
+	for(int m = 0; m < P.mid_n; m++) {
+		const MidChannel &mc = P.mid[m];
+		DMid &D = J.mid[m];
+		D.ctype = mc.ctype; D.in_ch = mc.in_ch; D.to_gray = mc.to_gray; D.out_ch = mc.out_ch;
+		D.unassoc = mc.unassoc; D.wh = mc.wset_h; D.wv = mc.wset_v; D.bk_early = mc.bk_early;
+		for(int t = 0; t < (mc.to_gray ? 3 : 1); t++) {
+			D.tab[t] = decode_tab(mc.in_ch + t, mc.lin_cs);
+			if(!D.tab[t] && mc.in_ch + t < P.in_nphys && P.in_sampletype != IW_SAMPLETYPE_FLOATINGPOINT) {
+				iw_set_error(ctx, "Out of GPU memory (tables)");
+				return false;
+			}
+		}
+	}
+	J.alpha_tab = decode_tab(P.in_alpha, true);
+	if(!J.alpha_tab && P.in_alpha < P.in_nphys && P.in_sampletype != IW_SAMPLETYPE_FLOATINGPOINT &&
+		IW_IMGTYPE_HAS_ALPHA(P.in_logtype)) {
+		iw_set_error(ctx, "Out of GPU memory (tables)");
+		return false;
+	}
+
+	bool any_scan = false;
+	for(int oc = 0; oc < P.out_n; oc++) {
+		const OutChannel &o = P.out[oc];
+		DOut &D = J.outc[oc];
+		D.ctype = o.ctype;
+		D.maxcc = o.maxcc;
+		D.bk1 = o.bk1;
+		D.bk2 = o.bk2;
+		const Quant &q = o.q;
+		D.q.float_out = q.float_out;
+		if(q.float_out) continue;
+		D.q.use_nc = q.use_nc; D.q.dfam = q.dfam; D.q.dsub = q.dsub; D.q.maxcc = q.maxcc; D.q.P = q.P;
+		D.q.U = cached_table(S, q.U);
+		D.q.X = cached_table(S, q.X);
+		D.q.code = cached_table(S, q.code);
+		D.q.rev = cached_table(S, q.rev);
+		D.q.nc = cached_table(S, q.nc);
+		if(!D.q.U || !D.q.X || !D.q.code || !D.q.rev || (q.use_nc && !D.q.nc)) {
+			iw_set_error(ctx, "Out of GPU memory (tables)");
+			return false;
+		}
+		D.scan = q.dfam == IW_DITHERFAMILY_ERRDIFF || q.dfam == IW_DITHERFAMILY_RANDOM;
+		if(D.scan) any_scan = true;
+	}
+	J.any_scan = any_scan;
+
+	// ---- buffers ----
+	const size_t interm_bytes = (size_t)P.mid_n * J.interm_plane * sizeof(float);
+	const size_t out_bytes = P.out_bpr * (size_t)P.out_h;
+	if(!S.in.ensure(in_bytes ? in_bytes : 16) || !S.interm.ensure(interm_bytes) || !S.out.ensure(out_bytes) ||
+		!S.params.ensure(S.staging.size() + 256)) {
+		iw_set_error(ctx, "Out of GPU memory");
+		return false;
+	}
+	if(any_scan) {
+		if(!S.scan.ensure((size_t)P.out_n * P.out_w * P.out_h * sizeof(double)) ||
+			!S.err.ensure((size_t)P.out_n * 3 * P.out_w * sizeof(double))) {
+			iw_set_error(ctx, "Out of GPU memory");
+			return false;
+		}
+		J.scanbuf = (double *)S.scan.p;
+		J.errbuf = (double *)S.err.p;
+	}
+	J.in = (const uint8_t *)S.in.p;
+	J.interm = (float *)S.interm.p;
+	J.out = (uint8_t *)S.out.p;
+	for(const Fixup &f : fix) *f.slot = (const uint8_t *)S.params.p + f.off;
+
+	cudaStream_t st = S.stream;
+	cudaMemcpyAsync(S.params.p, S.staging.data(), S.staging.size(), cudaMemcpyHostToDevice, st);
+	cudaMemcpyAsync(S.in.p, ctx->img1.pixels, in_bytes, cudaMemcpyHostToDevice, st);
+
+	const char *prec = get_option(ctx, "gpu:precision");
+	bool want_plain = prec && !strcmp(prec, "fp64");
+	FastInfo fi;
+	bool fast = !want_plain && fast_eligible(P, J, fi);
+	ctx->stats.form = fast ? 1 : 0;
+	if(fast && !fast_prepare(st, P, J, fi, err)) {
+		iw_set_error(ctx, err.c_str());
+		return false;
+	}
+
+	// The device passes, launched warmup+iters times; the input stays resident.
+	// Events bracket every launch group of the timed iterations.
+	const int total_it = warmup + (iters < 1 ? 1 : iters);
+	const int nt = total_it - warmup;
+	std::vector<cudaEvent_t> ev;
+	auto mark = [&](bool timed) {
+		if(!timed) return;
+		cudaEvent_t e;
+		cudaEventCreate(&e);
+		cudaEventRecord(e, st);
+		ev.push_back(e);
+	};
+	int launches = 0, marks_per_it = 0;
+	for(int it = 0; it < total_it; it++) {
+		bool timed = it >= warmup;
+		size_t before = ev.size();
+		mark(timed);
+		int l;
+		if(fast) l = fast_launch(st, fi, [&]() { mark(timed); });
+		else l = plain_launch(st, P, J, [&]() { mark(timed); });
+		if(timed) marks_per_it = (int)(ev.size() - before);
+		launches = l;
+	}
+	cudaMemcpyAsync(ctx->img2.pixels, S.out.p, out_bytes, cudaMemcpyDeviceToHost, st);
+	cudaError_t ce = cudaStreamSynchronize(st);
+	if(ce == cudaSuccess) ce = cudaGetLastError();
+	ctx->stats.flagged = 0;
+	if(ce == cudaSuccess && fast && fi.flag_count_dev) {
+		int nflag = 0;
+		ce = cudaMemcpy(&nflag, fi.flag_count_dev, sizeof(int), cudaMemcpyDeviceToHost);
+		ctx->stats.flagged = nflag;
+	}
+	double total_ms = 0, part[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+	if(ce == cudaSuccess && marks_per_it >= 2) {
+		for(int it = 0; it < nt; it++) {
+			cudaEvent_t *e = ev.data() + (size_t)it * marks_per_it;
+			float ms = 0;
+			cudaEventElapsedTime(&ms, e[0], e[marks_per_it - 1]);
+			total_ms += ms;
+			for(int k = 0; k + 1 < marks_per_it && k < 8; k++) {
+				cudaEventElapsedTime(&ms, e[k], e[k + 1]);
+				part[k] += ms;
+			}
+		}
+	}
+	for(cudaEvent_t e : ev) cudaEventDestroy(e);
+	fast_release(fi);
+	if(ce != cudaSuccess) {
+		iw_set_errorf(ctx, "CUDA error: %s", cudaGetErrorString(ce));
+		return false;
+	}
+	ctx->stats.ms_device = total_ms / nt;
+	for(int k = 0; k < 4; k++) ctx->stats.ms_part[k] = part[k] / nt;
+	ctx->stats.kernels = launches;
+	return true;
+}
+
+// The plain form's launches; 'mark' is called after each launch group.
+template<class Mark>
+int plain_launch(cudaStream_t st, const Plan &P, const Job &J, Mark mark)
+{
+	int launches = 0;
+	dim3 bv(128), gv((J.mid_w + 127) / 128, J.mid_h);
+	k_vpass_exact<<<gv, bv, 0, st>>>(J);
+	mark();
+	dim3 bh(128), gh((J.out_w + 127) / 128, J.out_h);
+	k_hpass_exact<<<gh, bh, 0, st>>>(J);
+	mark();
+	launches += 2;
+	if(J.any_scan) {
+		for(int oc = 0; oc < P.out_n; oc++)
+			if(J.outc[oc].scan) { k_scan<<<1, 32, 0, st>>>(J, oc); launches++; }
+		if(J.negate || J.blacken) { k_finalize<<<gh, bh, 0, st>>>(J); launches++; }
+		mark();
+	}
+	return launches;
+}
+
+}  // namespace iwg
+
+// ===== additive ABI (include/imagew_gb300.h) ================================
+
+extern "C" int iwg_get_stats(struct iw_context *ctx, struct iwg_stats *out)
+{
+	out->ms_total = ctx->stats.ms_total;
+	out->ms_device = ctx->stats.ms_device;
+	for(int k = 0; k < 4; k++) out->ms_part[k] = ctx->stats.ms_part[k];
+	out->flagged = ctx->stats.flagged;
+	out->form = ctx->stats.form;
+	out->kernels = ctx->stats.kernels;
+	return 1;
+}
+
+extern "C" int iwg_device_info(char *buf, int buflen)
+{
+	int dev = 0, n = 0;
+	if(buflen < 1) return 0;
+	buf[0] = '\0';
+	if(cudaGetDeviceCount(&n) != cudaSuccess || n < 1) return 0;
+	cudaGetDevice(&dev);
+	cudaDeviceProp p;
+	if(cudaGetDeviceProperties(&p, dev) != cudaSuccess) return 0;
+	snprintf(buf, buflen, "%s sm_%d%d, %d SMs, %.1f GiB", p.name, p.major, p.minor, p.multiProcessorCount,
+		p.totalGlobalMem / 1073741824.0);
+	return 1;
+}

@@ -195,6 +195,16 @@ class Result:
         return (self.ok, self.error, self.imgtype, self.bit_depth, self.sampletype, self.width, self.height,
                 self.bpr, self.pixels, self.palette, self.colorkey, self.bkgdlabel, self.reduced_maxcolors)
 
+    def digest(self) -> str:
+        """SHA-256 over :meth:`key` in a canonical encoding."""
+        import hashlib
+        h = hashlib.sha256()
+        k = self.key()
+        h.update(repr(k[:8]).encode())
+        h.update(k[8])
+        h.update(repr(k[9:]).encode())
+        return h.hexdigest()
+
 
 def _convert_arg(a):
     if isinstance(a, tuple) and len(a) == 3 and a[0] == "cs":
