@@ -63,7 +63,7 @@ WORKLOADS = {
 
 class Stats(C.Structure):
     _fields_ = [("ms_total", C.c_double), ("ms_device", C.c_double), ("ms_part", C.c_double * 4),
-                ("flagged", C.c_longlong), ("form", C.c_int), ("kernels", C.c_int)]
+                ("flagged", C.c_longlong), ("form", C.c_int), ("kernels", C.c_int), ("zero_copy", C.c_int)]
 
 
 def dist_env():
@@ -175,25 +175,41 @@ def device_timed(lib: IWLib, job, warmup: int, steps: int, form: str):
 
 
 def e2e_timed(lib: IWLib, job, warmup: int, steps: int):
-    """Per step: the C-ABI call sequence with host buffers (wall clock)."""
-    times = []
-    dig = None
+    """Per step, wall clock: the C-ABI call sequence a caller makes with its
+    image already in a malloc'd host buffer -- iw_create_context,
+    iw_set_input_image (ownership passes to the library), the settings,
+    iw_process_image (upload or zero-copy read, device passes, output in host
+    memory, post-pass) and iw_get_output_image.  Buffers are filled before the
+    timed region; contexts are destroyed after it."""
+    lib.dll.iwg_get_stats.argtypes = [C.c_void_p, C.POINTER(Stats)]
+    n = job.bpr * job.height
+    times, dig, zc = [], None, 0
     for s in range(warmup + steps):
+        buf = _libc.malloc(n)
+        C.memmove(buf, job.pixels, n)
+        img = Image()
+        img.imgtype, img.bit_depth, img.sampletype = job.imgtype, job.bit_depth, job.sampletype
+        img.width, img.height, img.pixels, img.bpr = job.width, job.height, buf, job.bpr
         t0 = time.perf_counter()
-        ctx = make_ctx(lib, job)
+        ctx = lib.iw_create_context(None)
+        lib.iw_set_input_image(ctx, C.byref(img))
+        for call in job.calls:
+            getattr(lib, call[0])(ctx, *[_convert_arg(a) for a in call[1:]])
         ok = lib.iw_process_image(ctx)
         out = Image()
         lib.iw_get_output_image(ctx, C.byref(out))
-        _ = C.string_at(out.pixels, min(64, out.bpr * out.height))   # the caller touches its result
         t1 = time.perf_counter()
         if not ok:
             raise RuntimeError("iw_process_image failed")
         if s == warmup + steps - 1:
             dig = output_digest(lib, ctx)
+            st = Stats()
+            lib.dll.iwg_get_stats(ctx, C.byref(st))
+            zc = st.zero_copy
         lib.iw_destroy_context(ctx)
         if s >= warmup:
             times.append(t1 - t0)
-    return times, dig
+    return times, dig, zc
 
 
 def cpu_oracle_sample(job, seconds_hint="one full image, one thread"):
@@ -307,7 +323,7 @@ def main():
         barrier()
         st64, dig_plain = device_timed(lib, job, 1, max(2, min(args.steps, 5)), "fp64")
         barrier()
-        e2e_times, dig_e2e = e2e_timed(lib, job, 2, max(3, min(args.steps, 10)))
+        e2e_times, dig_e2e, e2e_zc = e2e_timed(lib, job, 2, max(3, min(args.steps, 10)))
         barrier()
 
     ms = st.ms_device
@@ -345,8 +361,9 @@ def main():
                    "output_px": out_px, "parallelism": f"replicas x{world}",
                    "l2": "input (134 MB) larger than L2; passes back to back"},
         "e2e": {"value": world * out_px / 1e6 / (e2e_ms / 1000.0), "unit": "Mpix/s", "h2d_bytes_per_step": in_bytes,
-                "d2h_bytes_per_step": out_bytes, "ms_per_step": e2e_ms,
-                "host_buffers": "pageable (caller-malloc'd, as the libimagew ownership model requires)"},
+                "d2h_bytes_per_step": out_bytes, "ms_per_step": e2e_ms, "p50_ms": 1000 * statistics.median(e2e_times),
+                "host_buffers": "pageable (caller-malloc'd, as the libimagew ownership model requires)",
+                "transfer": "zero-copy (GPU reads/writes host memory over NVLink-C2C)" if e2e_zc else "cudaMemcpy"},
         "roofline": {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None, "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)",
                      "traffic": None, "algorithmic_bytes_per_launch": comp[dom],

@@ -31,7 +31,7 @@ namespace iwg {
 
 using namespace dev;
 
-__global__ void k_fix_flagged_fwd(Job J, const int *count, const int *list);
+void launch_fix_flagged(cudaStream_t st, const Job &J, const int *count, const int *list);
 
 namespace {
 
@@ -64,6 +64,7 @@ struct FJob {
 	float alpha_inv;
 	int npl;
 	FPlane pl[kMaxPlanes];
+	int vec;                   // 8 / 4: pixels load as one aligned 8- / 4-byte word; 0: bytes
 	const float *dec_tab;      // 8-bit: 256 floats; 16-bit: 4096 (T0, slope) pairs
 	int dec_tab_floats;
 	// vertical pass
@@ -147,9 +148,69 @@ __device__ __forceinline__ void decode_pixel(const FJob &F, const float *tab, co
 // once, in order, and accumulated into NS register slots, one per output row
 // whose window is open (slot = row mod NS).
 // ---------------------------------------------------------------------------
+// Raw bytes of one input pixel (at most 8: four 16-bit channels).
+struct Raw {
+	uint32_t lo, hi;
+};
+
+__device__ __forceinline__ Raw load_raw(const FJob &F, const uint8_t *px, int bpp)
+{
+	Raw r{0u, 0u};
+	if(F.vec == 8) {
+		uint2 v = __ldg(reinterpret_cast<const uint2 *>(px));
+		r.lo = v.x;
+		r.hi = v.y;
+	}
+	else if(F.vec == 4) r.lo = __ldg(reinterpret_cast<const unsigned int *>(px));
+	else {
+		for(int b = 0; b < bpp; b++) {
+			uint32_t byte = __ldg(px + b);
+			if(b < 4) r.lo |= byte << (8 * b);
+			else r.hi |= byte << (8 * (b - 4));
+		}
+	}
+	return r;
+}
+
+__device__ __forceinline__ unsigned int raw_byte(const Raw &r, int b)
+{
+	return ((b < 4 ? (r.lo >> (8 * b)) : (r.hi >> (8 * (b - 4))))) & 0xffu;
+}
+
+template<int DEPTH>
+__device__ __forceinline__ unsigned int raw_code(const Raw &r, int ch)
+{
+	if(DEPTH == 8) return raw_byte(r, ch);
+	return (raw_byte(r, 2 * ch) << 8) | raw_byte(r, 2 * ch + 1);   // big-endian samples
+}
+
+template<int NPL, int DEPTH>
+__device__ __forceinline__ void decode_raw(const FJob &F, const float *tab, const Raw &px, float *val)
+{
+	float a = 1.0f;
+	if(F.alpha_src >= 0) a = __fmul_rn((float)raw_code<DEPTH>(px, F.alpha_src), F.alpha_inv);
+#pragma unroll
+	for(int c = 0; c < NPL; c++) {
+		const FPlane &P = F.pl[c];
+		float v;
+		if(P.src < 0) v = 1.0f;
+		else {
+			unsigned int code = raw_code<DEPTH>(px, P.src);
+			v = P.table ? dec_table<DEPTH>(tab, code) : __fmul_rn((float)code, P.inv);
+		}
+		val[c] = P.premul ? __fmul_rn(v, a) : v;
+	}
+}
+
+// Vertical pass, streaming.  Each thread owns one column and walks the input
+// rows of its band once, in order, keeping PF rows of loads in flight; every
+// row is decoded once and accumulated into NS register slots, one per output
+// row whose window is open (slot = row mod NS).  A slot is stored and cleared
+// when its row's window closes.
 template<int NS, int NPL, int DEPTH>
 __global__ void __launch_bounds__(kVThreads) k_vstream(FJob F)
 {
+	constexpr int PF = 8;
 	extern __shared__ float s_tab[];
 	for(int k = threadIdx.x; k < F.dec_tab_floats; k += blockDim.x) s_tab[k] = F.dec_tab[k];
 	__syncthreads();
@@ -161,7 +222,8 @@ __global__ void __launch_bounds__(kVThreads) k_vstream(FJob F)
 	if(jb >= je) return;
 	const int p0 = F.first_pos[jb], p1 = F.last_pos[je - 1];
 	const int bpp = F.nphys * (DEPTH / 8);
-	const uint8_t *colbase = F.in + (size_t)(F.crop_x + (active ? x : 0)) * bpp;
+	const uint8_t *colbase = F.in + (size_t)(F.crop_x + (active ? x : 0)) * bpp +
+		(unsigned long long)F.crop_y * F.in_bpr;
 
 	float acc[NS][NPL];
 #pragma unroll
@@ -169,39 +231,58 @@ __global__ void __launch_bounds__(kVThreads) k_vstream(FJob F)
 #pragma unroll
 		for(int c = 0; c < NPL; c++) acc[s][c] = 0.0f;
 
-	for(int p = p0; p <= p1; p++) {
-		const int q = p - F.pmin;
-		const int row = __ldg(F.srcrow + q);
-		float val[NPL];
-		if(row >= 0 && active) {
-			const uint8_t *px = colbase + (unsigned long long)(F.crop_y + row) * F.in_bpr;
-			decode_pixel<NPL, DEPTH>(F, s_tab, px, val);
-		}
-		else {
+	Raw buf[PF];
+	int rows[PF];
 #pragma unroll
-			for(int c = 0; c < NPL; c++) val[c] = 0.0f;   // transparent edge: value 0
-		}
-		const float *w = F.sw + (size_t)q * 8;
+	for(int u = 0; u < PF; u++) {
+		const int p = p0 + u;
+		const int r = p <= p1 ? __ldg(F.srcrow + (p - F.pmin)) : -1;
+		rows[u] = r;
+		buf[u] = (r >= 0 && active) ? load_raw(F, colbase + (unsigned long long)r * F.in_bpr, bpp) : Raw{0u, 0u};
+	}
+
+	for(int p = p0; p <= p1; p += PF) {
 #pragma unroll
-		for(int s = 0; s < NS; s++) {
-			float ws = __ldg(w + s);
+		for(int u = 0; u < PF; u++) {
+			const int pp = p + u;
+			if(pp > p1) break;
+			const Raw cur = buf[u];
+			const int row = rows[u];
+			{   // refill this slot of the ring with the row PF positions ahead
+				const int pn = pp + PF;
+				const int r = pn <= p1 ? __ldg(F.srcrow + (pn - F.pmin)) : -1;
+				rows[u] = r;
+				buf[u] = (r >= 0 && active) ? load_raw(F, colbase + (unsigned long long)r * F.in_bpr, bpp) : Raw{0u, 0u};
+			}
+			const int q = pp - F.pmin;
+			float val[NPL];
+			if(row >= 0 && active) decode_raw<NPL, DEPTH>(F, s_tab, cur, val);
+			else {
 #pragma unroll
-			for(int c = 0; c < NPL; c++) acc[s][c] = __fmaf_rn(val[c], ws, acc[s][c]);
-		}
-		const int2 fin = __ldg(F.pinfo + q);
-		for(int k = 0; k < fin.y; k++) {
-			const int j = fin.x + k;
-			const int sj = j % NS;
+				for(int c = 0; c < NPL; c++) val[c] = 0.0f;   // transparent edge: value 0
+			}
+			const float4 *w4 = reinterpret_cast<const float4 *>(F.sw + (size_t)q * 8);
+			const float4 wa = __ldg(w4), wb = __ldg(w4 + 1);
+			const float ws[8] = {wa.x, wa.y, wa.z, wa.w, wb.x, wb.y, wb.z, wb.w};
 #pragma unroll
-			for(int s = 0; s < NS; s++) {
-				if(s == sj) {
-					if(active && j >= jb && j < je) {
+			for(int s = 0; s < NS; s++)
 #pragma unroll
-						for(int c = 0; c < NPL; c++)
-							F.interm[(unsigned long long)c * F.plane + (unsigned long long)j * F.mid_w + x] = acc[s][c];
+				for(int c = 0; c < NPL; c++) acc[s][c] = __fmaf_rn(val[c], ws[s], acc[s][c]);
+			const int2 fin = __ldg(F.pinfo + q);
+			for(int k = 0; k < fin.y; k++) {
+				const int j = fin.x + k;
+				const int sj = j % NS;
+#pragma unroll
+				for(int s = 0; s < NS; s++) {
+					if(s == sj) {
+						if(active && j >= jb && j < je) {
+#pragma unroll
+							for(int c = 0; c < NPL; c++)
+								F.interm[(unsigned long long)c * F.plane + (unsigned long long)j * F.mid_w + x] = acc[s][c];
+						}
+#pragma unroll
+						for(int c = 0; c < NPL; c++) acc[s][c] = 0.0f;
 					}
-#pragma unroll
-					for(int c = 0; c < NPL; c++) acc[s][c] = 0.0f;
 				}
 			}
 		}
@@ -575,7 +656,7 @@ void fast_launch_impl(cudaStream_t st, void *state, void (*mark)(void *), void *
 	cudaLaunchKernel(S.hkernel, S.hgrid, dim3(kHThreads), fargs, 0, st);
 	mark(markarg);
 	// exact re-evaluation of flagged pixels (recomputes the vertical pass too)
-	k_fix_flagged_fwd<<<2 * 152, 64, 0, st>>>(S.J, S.F.flag_count, S.F.flag_list);
+	launch_fix_flagged(st, S.J, S.F.flag_count, S.F.flag_list);
 	mark(markarg);
 }
 
@@ -670,6 +751,12 @@ bool fast_prepare(cudaStream_t st, const Plan &P, Job &J, FastInfo &fi, std::str
 	F.crop_y = P.crop_y;
 	F.nphys = P.in_nphys;
 	F.depth = P.in_depth;
+	{
+		const int bpp = P.in_nphys * P.in_depth / 8;
+		const uintptr_t base = (uintptr_t)J.in + (uintptr_t)P.crop_x * bpp + (uintptr_t)P.crop_y * P.in_bpr;
+		F.vec = 0;
+		if((bpp == 8 || bpp == 4) && base % bpp == 0 && P.in_bpr % bpp == 0) F.vec = bpp;
+	}
 	F.mid_w = J.mid_w;
 	F.mid_h = J.mid_h;
 	F.interm = J.interm;

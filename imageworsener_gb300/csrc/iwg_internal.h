@@ -166,6 +166,7 @@ struct Stats {   // per call, readable through the iwg_* extension API
 	long long flagged = 0;       // samples re-evaluated exactly (fast form)
 	int form = 0;                // 0 = plain FP64, 1 = FP32 + guard band
 	int kernels = 0;             // kernel launches issued
+	int zero_copy = 0;           // kernels read/wrote the host image buffers directly
 };
 
 }  // namespace iwg

@@ -84,20 +84,22 @@ __device__ __forceinline__ double interm_exact(const Job &J, int m, int x, int j
 	return (double)__double2float_rn(s);
 }
 
-// Horizontal pass of one channel for output pixel (i, j).
-template<bool RECOMPUTE>
-__device__ __forceinline__ double hsum_exact(const Job &J, int m, int i, int j)
+// Horizontal pass of one channel for output pixel (i, j).  interm(m, k, x)
+// returns the exact intermediate value of channel m at column x, the k-th tap.
+template<class Interm>
+__device__ __forceinline__ double hsum_exact(const Job &J, int m, int i, int j, Interm interm)
 {
 	const DWeights &W = J.wh[J.mid[m].wh];
 	double s = 0.0;
+	const int t0 = W.off[i];
 	if(W.kind == 1) {
 		int src = W.src[i];
-		s = src < 0 ? 0.0 : interm_exact<RECOMPUTE>(J, m, src, j);
+		s = src < 0 ? 0.0 : interm(m, 0, src);
 	}
 	else {
-		for(int t = W.off[i]; t < W.off[i + 1]; t++) {
+		for(int t = t0; t < W.off[i + 1]; t++) {
 			int src = W.src[t];
-			double v = src >= 0 ? interm_exact<RECOMPUTE>(J, m, src, j) : W.edge_value;
+			double v = src >= 0 ? interm(m, t - t0, src) : W.edge_value;
 			s = dadd(s, dmul(v, W.w[t]));
 		}
 	}
@@ -127,8 +129,8 @@ __device__ __forceinline__ double unassoc_and_bkgd(const Job &J, const DMid &mc,
 
 // Quantise / store every channel of output pixel (i, j) exactly.  Used by the
 // plain form for all pixels and by the fast form for flagged pixels.
-template<bool RECOMPUTE>
-__device__ void pixel_exact(const Job &J, int i, int j, bool apply_post)
+template<class Interm>
+__device__ void pixel_exact(const Job &J, int i, int j, bool apply_post, Interm interm)
 {
 	double a = 0.0;
 	int alpha_code = -1;
@@ -138,7 +140,7 @@ __device__ void pixel_exact(const Job &J, int i, int j, bool apply_post)
 		int m = J.order[k];
 		const DMid &mc = J.mid[m];
 		bool is_alpha = mc.ctype == IW_CHANNELTYPE_ALPHA;
-		double s = hsum_exact<RECOMPUTE>(J, m, i, j);
+		double s = hsum_exact(J, m, i, j, interm);
 		if(is_alpha) a = (double)__double2float_rn(s);
 		int oc = mc.out_ch;
 		if(oc < 0) continue;
@@ -179,7 +181,7 @@ __global__ void k_hpass_exact(Job J)
 	int i = blockIdx.x * blockDim.x + threadIdx.x;
 	int j = blockIdx.y;
 	if(i >= J.out_w || j >= J.out_h) return;
-	pixel_exact<false>(J, i, j, !J.any_scan);
+	pixel_exact(J, i, j, !J.any_scan, [&](int m, int, int x) { return interm_exact<false>(J, m, x, j); });
 }
 
 // Serial scan for error-diffusion and random dither of one output channel
@@ -307,15 +309,56 @@ __global__ void k_finalize(Job J)
 	}
 }
 
-// Exact re-evaluation of the pixels the fast form flagged: the vertical pass
-// is recomputed in FP64 for just the columns those pixels read.
-__global__ void k_fix_flagged_fwd(Job J, const int *count, const int *list)
+// Exact re-evaluation of the pixels the fast form flagged.  One warp per
+// pixel: the lanes recompute, in FP64, the intermediate values the pixel's
+// horizontal taps read (each one a vertical sum), then lane 0 finishes the
+// pixel in the reference's order.  Scratch: 'maxt' floats per channel per warp.
+__global__ void k_fix_flagged_warp(Job J, const int *count, const int *list, int maxt)
 {
-	int n = *count;
-	for(int f = blockIdx.x * blockDim.x + threadIdx.x; f < n; f += gridDim.x * blockDim.x) {
-		int p = list[f];
-		pixel_exact<true>(J, p % J.out_w, p / J.out_w, true);
+	extern __shared__ float fix_cache[];
+	const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, wpb = blockDim.x >> 5;
+	float *my = fix_cache + (size_t)wib * dev::kMaxCh * maxt;
+	const int n = *count;
+	for(int f = blockIdx.x * wpb + wib; f < n; f += gridDim.x * wpb) {
+		const int p = list[f];
+		const int i = p % J.out_w, j = p / J.out_w;
+		for(int k = lane; k < J.mid_n * maxt; k += 32) {
+			const int m = k / maxt, t = k % maxt;
+			const DWeights &W = J.wh[J.mid[m].wh];
+			const int t0 = W.kind == 1 ? i : W.off[i];
+			const int nt = W.kind == 1 ? 1 : W.off[i + 1] - t0;
+			if(t < nt) {
+				const int src = W.src[t0 + t];
+				if(src >= 0) my[m * maxt + t] = (float)interm_exact<true>(J, m, src, j);
+			}
+		}
+		__syncwarp();
+		if(lane == 0) pixel_exact(J, i, j, true, [&](int m, int k, int) { return (double)my[m * maxt + k]; });
+		__syncwarp();
 	}
+}
+
+// Fallback for very wide horizontal windows: one thread per flagged pixel.
+__global__ void k_fix_flagged_thread(Job J, const int *count, const int *list)
+{
+	const int n = *count;
+	for(int f = blockIdx.x * blockDim.x + threadIdx.x; f < n; f += gridDim.x * blockDim.x) {
+		const int p = list[f];
+		const int j = p / J.out_w;
+		pixel_exact(J, p % J.out_w, j, true, [&](int m, int, int x) { return interm_exact<true>(J, m, x, j); });
+	}
+}
+
+// Launches the exact re-evaluation of flagged pixels on 'st'.
+void launch_fix_flagged(cudaStream_t st, const Job &J, const int *count, const int *list)
+{
+	int maxt = 1;
+	for(int m = 0; m < J.mid_n; m++) maxt = maxt > J.wh[J.mid[m].wh].max_taps ? maxt : J.wh[J.mid[m].wh].max_taps;
+	const size_t per_warp = (size_t)dev::kMaxCh * maxt * sizeof(float);
+	int wpb = 4;
+	while(wpb > 1 && per_warp * wpb > 48 * 1024) wpb >>= 1;
+	if(per_warp * wpb <= 48 * 1024) k_fix_flagged_warp<<<2 * 152, 32 * wpb, per_warp * wpb, st>>>(J, count, list, maxt);
+	else k_fix_flagged_thread<<<2 * 152, 64, 0, st>>>(J, count, list);
 }
 
 // ===========================================================================
@@ -347,6 +390,7 @@ struct DeviceState {
 	bool init = false;
 	std::string init_error;
 	int device = 0;
+	int pageable = 0;          // kernels may access pageable host memory (Grace: NVLink-C2C + ATS)
 	cudaStream_t stream = nullptr;
 	DevBuf in, interm, out, scan, err, params, flags;
 	std::map<const void *, std::pair<std::shared_ptr<const void>, void *>> table_cache;
@@ -369,6 +413,7 @@ bool ensure_init(DeviceState &S, std::string &err)
 		return false;
 	}
 	cudaGetDevice(&S.device);
+	cudaDeviceGetAttribute(&S.pageable, cudaDevAttrPageableMemoryAccess, S.device);
 	if(cudaStreamCreateWithFlags(&S.stream, cudaStreamNonBlocking) != cudaSuccess) {
 		err = "cudaStreamCreate failed";
 		return false;
@@ -547,10 +592,16 @@ bool run_pipeline(iw_context *ctx, Plan &P, int warmup, int iters)
 	J.any_scan = any_scan;
 
 	// ---- buffers ----
+	// Zero copy: where the GPU can access pageable host memory coherently
+	// (cudaDevAttrPageableMemoryAccess), the kernels read the caller's input
+	// image and write the output image in place, over the CPU-GPU link, instead
+	// of staging copies.  Timed runs keep the input resident in device memory.
+	const char *upl = get_option(ctx, "gpu:upload");
+	const bool zero_copy = S.pageable && !(upl && !strcmp(upl, "copy")) && warmup == 0 && iters <= 1;
 	const size_t interm_bytes = (size_t)P.mid_n * J.interm_plane * sizeof(float);
 	const size_t out_bytes = P.out_bpr * (size_t)P.out_h;
-	if(!S.in.ensure(in_bytes ? in_bytes : 16) || !S.interm.ensure(interm_bytes) || !S.out.ensure(out_bytes) ||
-		!S.params.ensure(S.staging.size() + 256)) {
+	if((!zero_copy && (!S.in.ensure(in_bytes ? in_bytes : 16) || !S.out.ensure(out_bytes))) ||
+		!S.interm.ensure(interm_bytes) || !S.params.ensure(S.staging.size() + 256)) {
 		iw_set_error(ctx, "Out of GPU memory");
 		return false;
 	}
@@ -563,14 +614,15 @@ bool run_pipeline(iw_context *ctx, Plan &P, int warmup, int iters)
 		J.scanbuf = (double *)S.scan.p;
 		J.errbuf = (double *)S.err.p;
 	}
-	J.in = (const uint8_t *)S.in.p;
+	J.in = zero_copy ? (const uint8_t *)ctx->img1.pixels : (const uint8_t *)S.in.p;
 	J.interm = (float *)S.interm.p;
-	J.out = (uint8_t *)S.out.p;
+	J.out = zero_copy ? (uint8_t *)ctx->img2.pixels : (uint8_t *)S.out.p;
+	ctx->stats.zero_copy = zero_copy;
 	for(const Fixup &f : fix) *f.slot = (const uint8_t *)S.params.p + f.off;
 
 	cudaStream_t st = S.stream;
 	cudaMemcpyAsync(S.params.p, S.staging.data(), S.staging.size(), cudaMemcpyHostToDevice, st);
-	cudaMemcpyAsync(S.in.p, ctx->img1.pixels, in_bytes, cudaMemcpyHostToDevice, st);
+	if(!zero_copy) cudaMemcpyAsync(S.in.p, ctx->img1.pixels, in_bytes, cudaMemcpyHostToDevice, st);
 
 	const char *prec = get_option(ctx, "gpu:precision");
 	bool want_plain = prec && !strcmp(prec, "fp64");
@@ -605,7 +657,7 @@ bool run_pipeline(iw_context *ctx, Plan &P, int warmup, int iters)
 		if(timed) marks_per_it = (int)(ev.size() - before);
 		launches = l;
 	}
-	cudaMemcpyAsync(ctx->img2.pixels, S.out.p, out_bytes, cudaMemcpyDeviceToHost, st);
+	if(!zero_copy) cudaMemcpyAsync(ctx->img2.pixels, S.out.p, out_bytes, cudaMemcpyDeviceToHost, st);
 	cudaError_t ce = cudaStreamSynchronize(st);
 	if(ce == cudaSuccess) ce = cudaGetLastError();
 	ctx->stats.flagged = 0;
@@ -672,6 +724,7 @@ extern "C" int iwg_get_stats(struct iw_context *ctx, struct iwg_stats *out)
 	out->flagged = ctx->stats.flagged;
 	out->form = ctx->stats.form;
 	out->kernels = ctx->stats.kernels;
+	out->zero_copy = ctx->stats.zero_copy;
 	return 1;
 }
 
@@ -684,7 +737,10 @@ extern "C" int iwg_device_info(char *buf, int buflen)
 	cudaGetDevice(&dev);
 	cudaDeviceProp p;
 	if(cudaGetDeviceProperties(&p, dev) != cudaSuccess) return 0;
-	snprintf(buf, buflen, "%s sm_%d%d, %d SMs, %.1f GiB", p.name, p.major, p.minor, p.multiProcessorCount,
-		p.totalGlobalMem / 1073741824.0);
+	int pageable = 0, hostpt = 0;
+	cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, dev);
+	cudaDeviceGetAttribute(&hostpt, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev);
+	snprintf(buf, buflen, "%s sm_%d%d, %d SMs, %.1f GiB, pageable host memory access %d (host page tables %d)",
+		p.name, p.major, p.minor, p.multiProcessorCount, p.totalGlobalMem / 1073741824.0, pageable, hostpt);
 	return 1;
 }

@@ -32,6 +32,8 @@ struct iwg_stats {
 	long long flagged;     /* pixels recomputed in FP64 by the fp32 form */
 	int form;              /* 0 = fp64, 1 = fp32 + guard band */
 	int kernels;           /* kernel launches per pass */
+	int zero_copy;         /* 1: kernels read the input and wrote the output in
+	                          host memory directly (no staging copies) */
 };
 
 /* Copies the statistics of the context's last run into *out.  Returns 1. */
