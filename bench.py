@@ -183,7 +183,7 @@ def e2e_timed(lib: IWLib, job, warmup: int, steps: int):
     timed region; contexts are destroyed after it."""
     lib.dll.iwg_get_stats.argtypes = [C.c_void_p, C.POINTER(Stats)]
     n = job.bpr * job.height
-    times, dig, zc = [], None, 0
+    times, dig, zc = [], None, {}
     for s in range(warmup + steps):
         buf = _libc.malloc(n)
         C.memmove(buf, job.pixels, n)
@@ -205,7 +205,9 @@ def e2e_timed(lib: IWLib, job, warmup: int, steps: int):
             dig = output_digest(lib, ctx)
             st = Stats()
             lib.dll.iwg_get_stats(ctx, C.byref(st))
-            zc = st.zero_copy
+            zc = {"zero_copy": st.zero_copy, "device_ms": st.ms_device,
+                  "kernel_ms": {"vertical": st.ms_part[0], "horizontal": st.ms_part[1], "fixup": st.ms_part[2]},
+                  "host_ms_total": st.ms_total}
         lib.iw_destroy_context(ctx)
         if s >= warmup:
             times.append(t1 - t0)
@@ -363,7 +365,8 @@ def main():
         "e2e": {"value": world * out_px / 1e6 / (e2e_ms / 1000.0), "unit": "Mpix/s", "h2d_bytes_per_step": in_bytes,
                 "d2h_bytes_per_step": out_bytes, "ms_per_step": e2e_ms, "p50_ms": 1000 * statistics.median(e2e_times),
                 "host_buffers": "pageable (caller-malloc'd, as the libimagew ownership model requires)",
-                "transfer": "zero-copy (GPU reads/writes host memory over NVLink-C2C)" if e2e_zc else "cudaMemcpy"},
+                "transfer": "zero-copy (GPU reads/writes host memory over NVLink-C2C)" if e2e_zc.get("zero_copy") else "cudaMemcpy",
+                "last_call": e2e_zc},
         "roofline": {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None, "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)",
                      "traffic": None, "algorithmic_bytes_per_launch": comp[dom],

@@ -182,18 +182,18 @@ __device__ __forceinline__ double decode_exact(const Job &J, const DMid &m, int 
 	return s;
 }
 
-// Ordered-dither threshold rank at (x,y); threshold = (rank + 0.5) / 64
-// (8x8 patterns of src/imagew-main.c:461-483).
+// Ordered-dither threshold ranks; threshold = (rank + 0.5) / 64 (8x8
+// dispersed and "halftone" patterns of src/imagew-main.c:461-483).  In global
+// memory (read through L1): lanes of a warp index different entries.
+static __device__ const unsigned char kDitherRank[2][64] = {
+	{0,48,12,60, 3,51,15,63, 32,16,44,28,35,19,47,31,  8,56, 4,52,11,59, 7,55, 40,24,36,20,43,27,39,23,
+	 2,50,14,62, 1,49,13,61, 34,18,46,30,33,17,45,29, 10,58, 6,54, 9,57, 5,53, 42,26,38,22,41,25,37,21},
+	{3, 9,17,27,25,15, 7, 1, 11,29,37,45,43,35,23, 5, 19,39,51,57,55,49,33,13, 31,47,59,63,61,53,41,21,
+	 30,46,58,62,60,52,40,20, 18,38,50,56,54,48,32,12, 10,28,36,44,42,34,22, 4,  2, 8,16,26,24,14, 6, 0}};
+
 __device__ __forceinline__ int dither_rank(int sub, int x, int y)
 {
-	const unsigned char r0[64] = {
-		0,48,12,60, 3,51,15,63, 32,16,44,28,35,19,47,31,  8,56, 4,52,11,59, 7,55, 40,24,36,20,43,27,39,23,
-		2,50,14,62, 1,49,13,61, 34,18,46,30,33,17,45,29, 10,58, 6,54, 9,57, 5,53, 42,26,38,22,41,25,37,21};
-	const unsigned char r1[64] = {
-		3, 9,17,27,25,15, 7, 1, 11,29,37,45,43,35,23, 5, 19,39,51,57,55,49,33,13, 31,47,59,63,61,53,41,21,
-		30,46,58,62,60,52,40,20, 18,38,50,56,54,48,32,12, 10,28,36,44,42,34,22, 4,  2, 8,16,26,24,14, 6, 0};
-	int i = (x % 8) + 8 * (y % 8);
-	return sub ? r1[i] : r0[i];
+	return kDitherRank[sub ? 1 : 0][(x % 8) + 8 * (y % 8)];
 }
 
 // Number of entries of the ascending table t[0..n-1] that are <= v.

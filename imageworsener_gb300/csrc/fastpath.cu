@@ -37,6 +37,7 @@ namespace {
 
 constexpr int kVThreads = 128;
 constexpr int kHThreads = 128;
+constexpr int kVPxThreads = 128;
 constexpr int kMaxPlanes = 4;
 
 struct FPlane {
@@ -78,6 +79,7 @@ struct FJob {
 	const int *srcrow;        // per position: input row, -1 virtual
 	const int *first_pos, *last_pos;
 	int rows_per_band;
+	int in_rows;              // crop height: input rows of the vertical pass
 	// gather (upscale) vertical pass
 	const int *voff, *vsrc;
 	const float *vw;
@@ -87,17 +89,16 @@ struct FJob {
 	int out_w, out_h, out_n, out_depth;
 	uint8_t *out;
 	unsigned long long out_bpr;
-	// per mid channel (processing order)
+	// per processing slot k (alpha first), so kernels index these statically
 	int mid_n;
-	int order[dev::kMaxCh];
-	int plane_of[dev::kMaxCh];
-	int out_of[dev::kMaxCh];
-	int is_alpha[dev::kMaxCh];
-	int unassoc[dev::kMaxCh];
+	int k_plane[dev::kMaxCh];   // plane holding the channel's intermediate
+	int k_out[dev::kMaxCh];     // output channel
+	int k_alpha[dev::kMaxCh];   // 1: the alpha channel
+	int k_unassoc[dev::kMaxCh]; // 1: colour channel divided by alpha
+	int k_maxcc[dev::kMaxCh];   // output max code (negation)
+	unsigned int k_bit[dev::kMaxCh];  // bit of the intermediate channel in re-evaluation masks
 	int alpha_plane;
-	FTail tail[dev::kMaxCh];        // per output channel
-	int maxcc[dev::kMaxCh];
-	int out_alpha[dev::kMaxCh];     // output channel is an alpha channel
+	const FTail *tail;         // per output channel (device memory)
 	int negate, blacken;
 	// error model
 	float K0[kMaxPlanes], K1[kMaxPlanes];
@@ -289,6 +290,182 @@ __global__ void __launch_bounds__(kVThreads) k_vstream(FJob F)
 	}
 }
 
+// Exact float of a small unsigned integer (< 2^23) without an I2F: the code
+// is placed in the mantissa of 2^23 and 2^23 is subtracted.
+__device__ __forceinline__ float u2f(unsigned int v)
+{
+	return __fsub_rn(__uint_as_float(0x4b000000u | v), 8388608.0f);
+}
+
+
+// Vertical pass, streaming, PX pixels per thread.  Same scheme as
+// k_vstream, arranged for memory-level parallelism and few instructions
+// per sample:
+//   * each thread reads PX adjacent pixels of a row as one aligned 4/8/16-byte
+//     word group, and keeps PF rows of those loads in flight;
+//   * a row's address is computed from its position (positions map to rows by
+//     clamping, which the host checked for this weight set), so no load waits
+//     on another load;
+//   * the band's schedule (slot weights, rows finished per position) is staged
+//     in shared memory once per block.
+template<int NS, int NCH, bool ALPHA, int DEPTH, int PX>
+__global__ void __launch_bounds__(kVPxThreads) k_vstream_px(FJob F)
+{
+	constexpr int PF = 8;
+	constexpr int BPP = NCH * (DEPTH / 8);
+	constexpr int NW = PX * BPP / 4;              // 32-bit words per thread per row
+	static_assert(PX * BPP % 4 == 0, "thread group must be whole words");
+	extern __shared__ float s_dyn[];
+	float *s_tab = s_dyn;
+	const int jb = blockIdx.y * F.rows_per_band;
+	const int je = min(jb + F.rows_per_band, F.mid_h);
+	if(jb >= je) return;
+	const int p0 = F.first_pos[jb], p1 = F.last_pos[je - 1];
+	const int nq = p1 - p0 + 1;
+	float *s_w = s_dyn + F.dec_tab_floats;         // nq * NS
+	int2 *s_fin = reinterpret_cast<int2 *>(s_w + (size_t)nq * NS);
+	for(int k = threadIdx.x; k < F.dec_tab_floats; k += blockDim.x) s_tab[k] = F.dec_tab[k];
+	for(int k = threadIdx.x; k < nq * NS; k += blockDim.x) {
+		const int q = k / NS, sl = k - q * NS;
+		s_w[k] = F.sw[(size_t)(p0 - F.pmin + q) * 8 + sl];
+	}
+	for(int k = threadIdx.x; k < nq; k += blockDim.x) s_fin[k] = F.pinfo[p0 - F.pmin + k];
+	__syncthreads();
+
+	const int x0 = (blockIdx.x * blockDim.x + threadIdx.x) * PX;
+	if(x0 >= F.mid_w) return;
+	const bool full = x0 + PX <= F.mid_w;
+	const int valid_bytes = (F.mid_w - x0) * BPP;
+	const uint8_t *colbase = F.in + (size_t)(F.crop_x + x0) * BPP + (unsigned long long)F.crop_y * F.in_bpr;
+	const int last_row = F.in_rows - 1;
+	const float ainv = F.alpha_inv;
+
+	float acc[NS][PX][NCH];
+#pragma unroll
+	for(int s = 0; s < NS; s++)
+#pragma unroll
+		for(int px = 0; px < PX; px++)
+#pragma unroll
+			for(int c = 0; c < NCH; c++) acc[s][px][c] = 0.0f;
+
+	auto load_row = [&](int p, uint32_t *w) {
+		const int row = min(max(p, 0), last_row);
+		const uint8_t *a = colbase + (unsigned long long)row * F.in_bpr;
+		if(full) {
+			if(NW % 4 == 0) {
+#pragma unroll
+				for(int k = 0; k < NW; k += 4) {
+					const uint4 v = __ldcs(reinterpret_cast<const uint4 *>(a) + k / 4);
+					w[k] = v.x; w[k + 1] = v.y; w[k + 2] = v.z; w[k + 3] = v.w;
+				}
+			}
+			else if(NW % 2 == 0) {
+#pragma unroll
+				for(int k = 0; k < NW; k += 2) {
+					const uint2 v = __ldcs(reinterpret_cast<const uint2 *>(a) + k / 2);
+					w[k] = v.x; w[k + 1] = v.y;
+				}
+			}
+			else {
+#pragma unroll
+				for(int k = 0; k < NW; k++) w[k] = __ldcs(reinterpret_cast<const unsigned int *>(a) + k);
+			}
+		}
+		else {
+#pragma unroll
+			for(int k = 0; k < NW; k++)
+				w[k] = 4 * k < valid_bytes ? __ldcs(reinterpret_cast<const unsigned int *>(a) + k) : 0u;
+		}
+	};
+
+	uint32_t ring[PF][NW];
+#pragma unroll
+	for(int u = 0; u < PF; u++) {
+		if(p0 + u <= p1) load_row(p0 + u, ring[u]);
+		else {
+#pragma unroll
+			for(int k = 0; k < NW; k++) ring[u][k] = 0u;
+		}
+	}
+
+	for(int p = p0; p <= p1; p += PF) {
+#pragma unroll
+		for(int u = 0; u < PF; u++) {
+			const int pp = p + u;
+			if(pp > p1) break;
+			uint32_t cur[NW];
+#pragma unroll
+			for(int k = 0; k < NW; k++) cur[k] = ring[u][k];
+			if(pp + PF <= p1) load_row(pp + PF, ring[u]);
+			const int q = pp - p0;
+			float val[PX][NCH];
+#pragma unroll
+			for(int px = 0; px < PX; px++) {
+				float a = 1.0f;
+#pragma unroll
+				for(int c = 0; c < NCH; c++) {
+					const int sidx = px * NCH + c;      // sample index within the group
+					unsigned int code;
+					if(DEPTH == 8) code = __byte_perm(cur[sidx >> 2], 0u, 0x4440u + (sidx & 3));
+					else code = __byte_perm(cur[sidx >> 1], 0u, (sidx & 1) ? 0x4423u : 0x4401u);
+					if(ALPHA && c == NCH - 1) {
+						a = __fmul_rn(u2f(code), ainv);
+						val[px][c] = a;
+					}
+					else val[px][c] = dec_table<DEPTH>(s_tab, code);
+				}
+				if(ALPHA) {
+#pragma unroll
+					for(int c = 0; c < NCH - 1; c++) val[px][c] = __fmul_rn(val[px][c], a);
+				}
+			}
+			float ws[NS];
+			if(NS == 4) {
+				const float4 w4 = reinterpret_cast<const float4 *>(s_w)[q];
+				ws[0] = w4.x; ws[1] = w4.y; ws[2] = w4.z; ws[3] = w4.w;
+			}
+			else {
+#pragma unroll
+				for(int s = 0; s < NS; s += 2) {
+					const float2 w2 = reinterpret_cast<const float2 *>(s_w)[(q * NS + s) / 2];
+					ws[s] = w2.x; ws[s + 1] = w2.y;
+				}
+			}
+#pragma unroll
+			for(int s = 0; s < NS; s++)
+#pragma unroll
+				for(int px = 0; px < PX; px++)
+#pragma unroll
+					for(int c = 0; c < NCH; c++) acc[s][px][c] = __fmaf_rn(val[px][c], ws[s], acc[s][px][c]);
+			const int2 fin = s_fin[q];
+			for(int k = 0; k < fin.y; k++) {
+				const int j = fin.x + k;
+				const int sj = j % NS;
+				const bool keep = j >= jb && j < je;
+#pragma unroll
+				for(int s = 0; s < NS; s++) {
+					if(s == sj) {
+						if(keep) {
+							float *o = F.interm + (unsigned long long)j * F.mid_w + x0;
+#pragma unroll
+							for(int px = 0; px < PX; px++) {
+								if(full || x0 + px < F.mid_w) {
+#pragma unroll
+									for(int c = 0; c < NCH; c++) o[(unsigned long long)c * F.plane + px] = acc[s][px][c];
+								}
+							}
+						}
+#pragma unroll
+						for(int px = 0; px < PX; px++)
+#pragma unroll
+							for(int c = 0; c < NCH; c++) acc[s][px][c] = 0.0f;
+					}
+				}
+			}
+		}
+	}
+}
+
 // vertical pass, gather (upsampling or wide windows): one thread per (x, j).
 template<int NPL, int DEPTH>
 __global__ void __launch_bounds__(kVThreads) k_vgather(FJob F)
@@ -412,48 +589,65 @@ __global__ void __launch_bounds__(kHThreads) k_hpass_fast(FJob F)
 #pragma unroll
 	for(int c = 0; c < NPL; c++) E[c] = __fmaf_rn(F.K1[c], T[c], F.K0[c]);
 
+	// Decide every sample; 'redo' collects the intermediate channels that
+	// must be re-evaluated exactly.  An undecided colour sample needs its own
+	// channel and the exact alpha (the reference divides by the float alpha);
+	// an undecided alpha makes blackening undecided, so the whole pixel is redone.
+	// codes are kept per processing slot k (registers); out_of maps k to the channel
 	int codes[dev::kMaxCh];
 	int alpha_code = -1;
-	bool flag = false;
+	unsigned int redo = 0;
+	const unsigned int all = (1u << F.mid_n) - 1u;
 	float A = 0.0f, EA = 0.0f;
-	for(int k = 0; k < F.mid_n; k++) {
-		const int m = F.order[k];
-		const int pl = F.plane_of[m];
+#pragma unroll
+	for(int k = 0; k < dev::kMaxCh; k++) {
+		codes[k] = -1;
+		if(k >= F.mid_n || redo == all) continue;
+		const int pl = F.k_plane[k];
 		float val = 0.0f, err = 0.0f;
 #pragma unroll
 		for(int c = 0; c < NPL; c++) if(c == pl) { val = v[c]; err = E[c]; }
-		const int oc = F.out_of[m];
-		if(F.is_alpha[m]) {
+		const int oc = F.k_out[k];
+		const bool is_alpha = F.k_alpha[k];
+		if(is_alpha) {
 			A = val;
 			// the reference divides by the float-rounded alpha: widen by one rounding
 			EA = __fmaf_rn(fabsf(val) + err, 6.0e-8f, err);
 		}
-		else if(F.unassoc[m]) {
-			if(alpha_code == 0 && F.blacken) { codes[oc] = 0; continue; }
+		else if(F.k_unassoc[k]) {
+			if(alpha_code == 0 && F.blacken) { codes[k] = 0; continue; }
 			const float den = __fsub_rn(A, EA);
-			if(!(den > 0.0f)) { flag = true; break; }
+			if(!(den > 0.0f)) { redo |= F.k_bit[k] | F.k_bit[0]; continue; }
 			const float q = __fdiv_rn(val, A);
 			err = __fdiv_rn(__fmaf_rn(fabsf(q), EA, err), den);
 			err = __fmaf_rn(fabsf(q), 1.2e-7f, err);
 			val = q;
 		}
 		const int c = quantize_guarded(F.tail[oc], val, err, i, j);
-		if(c < 0) { flag = true; break; }
-		if(F.is_alpha[m]) alpha_code = c;
-		codes[oc] = c;
+		if(c < 0) {
+			if(is_alpha) redo = all;
+			else redo |= F.k_bit[k] | (F.k_unassoc[k] ? F.k_bit[0] : 0u);
+			continue;
+		}
+		if(is_alpha) alpha_code = c;
+		codes[k] = c;
 	}
-	if(flag) {
-		int slot = atomicAdd(F.flag_count, 1);
-		F.flag_list[slot] = j * F.out_w + i;
-		return;
+	if(redo) {
+		const int slot = atomicAdd(F.flag_count, 1);
+		F.flag_list[2 * slot] = j * F.out_w + i;
+		F.flag_list[2 * slot + 1] = (int)redo;
+		if(redo == all) return;
 	}
-	for(int oc = 0; oc < F.out_n; oc++) {
-		int c = codes[oc];
-		if(!F.out_alpha[oc]) {
-			if(F.negate) c = F.maxcc[oc] - c;
+#pragma unroll
+	for(int k = 0; k < dev::kMaxCh; k++) {
+		if(k >= F.mid_n) continue;
+		if(redo & F.k_bit[k]) continue;
+		int c = codes[k];
+		if(!F.k_alpha[k]) {
+			if(F.negate) c = F.k_maxcc[k] - c;
 			if(F.blacken && alpha_code == 0) c = 0;
 		}
-		store_code_f(F, oc, i, j, (unsigned int)c);
+		store_code_f(F, F.k_out[k], i, j, (unsigned int)c);
 	}
 }
 
@@ -560,6 +754,7 @@ DecodeTab make_decode_tab(const std::vector<double> &t, int depth)
 // Streaming layout of a vertical weight set.
 struct StreamTab {
 	bool ok = false;
+	bool arith = false;         // every referenced position p reads row clamp(p, 0, n_in-1)
 	int pmin = 0, npos = 0, ns = 0;
 	std::vector<int> first_pos, last_pos, srcrow;
 	std::vector<int> pinfo;     // pairs
@@ -610,6 +805,13 @@ StreamTab make_stream(const Weights &W)
 		if(S.pinfo[2 * q + 1] == 0) S.pinfo[2 * q] = j;
 		S.pinfo[2 * q + 1]++;
 	}
+	S.arith = true;
+	for(int q = 0; q < S.npos && S.arith; q++) {
+		bool used = false;
+		for(int k = 0; k < S.ns; k++) used = used || S.sw[(size_t)q * 8 + k] != 0.0f;
+		const int row = std::min(std::max(q + pmin, 0), W.n_in - 1);
+		if(used && S.srcrow[q] != row) S.arith = false;
+	}
 	S.ok = true;
 	return S;
 }
@@ -643,6 +845,7 @@ struct FastState {
 	Job J;
 	const void *vkernel = nullptr, *hkernel = nullptr;
 	dim3 vgrid, hgrid;
+	int vthreads = kVThreads;
 	size_t vsmem = 0;
 };
 
@@ -651,7 +854,7 @@ void fast_launch_impl(cudaStream_t st, void *state, void (*mark)(void *), void *
 	FastState &S = *static_cast<FastState *>(state);
 	cudaMemsetAsync(S.F.flag_count, 0, sizeof(int), st);
 	void *fargs[] = {&S.F};
-	cudaLaunchKernel(S.vkernel, S.vgrid, dim3(kVThreads), fargs, S.vsmem, st);
+	cudaLaunchKernel(S.vkernel, S.vgrid, dim3(S.vthreads), fargs, S.vsmem, st);
 	mark(markarg);
 	cudaLaunchKernel(S.hkernel, S.hgrid, dim3(kHThreads), fargs, 0, st);
 	mark(markarg);
@@ -676,6 +879,7 @@ bool fast_prepare(cudaStream_t st, const Plan &P, Job &J, FastInfo &fi, std::str
 
 	// ---- planes: distinct (input channel, transfer, premultiply) combinations
 	int nplanes = 0;
+	int plane_of[dev::kMaxCh] = {0, 0, 0, 0};
 	struct PK { int src, lin, premul; };
 	PK keys[kMaxPlanes];
 	std::shared_ptr<const std::vector<double>> coltab;
@@ -696,11 +900,8 @@ bool fast_prepare(cudaStream_t st, const Plan &P, Job &J, FastInfo &fi, std::str
 			pl.inv = (float)(1.0 / (double)P.in_max);
 			if(pl.table) coltab = input_table(P.cs_in.cstype, P.cs_in.gamma, P.in_max, 1 << P.in_depth, false);
 		}
-		F.plane_of[m] = found;
-		F.out_of[m] = mc.out_ch;
-		F.is_alpha[m] = mc.ctype == IW_CHANNELTYPE_ALPHA;
-		F.unassoc[m] = mc.unassoc;
-		if(F.is_alpha[m]) alpha_plane = found;
+		plane_of[m] = found;
+		if(mc.ctype == IW_CHANNELTYPE_ALPHA) alpha_plane = found;
 	}
 	F.npl = nplanes;
 	F.alpha_plane = alpha_plane;
@@ -759,13 +960,23 @@ bool fast_prepare(cudaStream_t st, const Plan &P, Job &J, FastInfo &fi, std::str
 	}
 	F.mid_w = J.mid_w;
 	F.mid_h = J.mid_h;
+	F.in_rows = P.crop_h;
 	F.interm = J.interm;
 	F.plane = J.interm_plane;
 	F.out_w = J.out_w; F.out_h = J.out_h; F.out_n = J.out_n; F.out_depth = J.out_depth;
 	F.out = J.out;
 	F.out_bpr = J.out_bpr;
 	F.mid_n = P.mid_n;
-	for(int k = 0; k < P.mid_n; k++) F.order[k] = J.order[k];
+	for(int k = 0; k < P.mid_n; k++) {
+		const int m = J.order[k];
+		const MidChannel &mc = P.mid[m];
+		F.k_plane[k] = plane_of[m];
+		F.k_out[k] = mc.out_ch;
+		F.k_alpha[k] = mc.ctype == IW_CHANNELTYPE_ALPHA;
+		F.k_unassoc[k] = mc.unassoc;
+		F.k_maxcc[k] = P.out[mc.out_ch].maxcc;
+		F.k_bit[k] = 1u << m;
+	}
 	F.negate = P.negate;
 	F.blacken = P.blacken;
 
@@ -791,8 +1002,8 @@ bool fast_prepare(cudaStream_t st, const Plan &P, Job &J, FastInfo &fi, std::str
 		o_pi = add(S.pinfo.data(), S.pinfo.size() * 4);
 		o_sw = add(S.sw.data(), S.sw.size() * 4);
 	}
-	const size_t flag_bytes = 256 + (size_t)J.out_w * J.out_h * 4;
-	size_t need = blob.size() + 256 + flag_bytes;
+	const size_t flag_bytes = 256 + (size_t)J.out_w * J.out_h * 8;
+	size_t need = blob.size() + 256 + flag_bytes + 256 + sizeof(FTail) * dev::kMaxCh;
 	if(need > C.scratch_cap) {
 		if(C.scratch) cudaFree(C.scratch);
 		C.scratch = nullptr;
@@ -823,9 +1034,11 @@ bool fast_prepare(cudaStream_t st, const Plan &P, Job &J, FastInfo &fi, std::str
 	}
 
 	// ---- quantisation tables (float copies, cached)
+	FTail tails[dev::kMaxCh];
+	memset(tails, 0, sizeof(tails));
 	for(int oc = 0; oc < P.out_n; oc++) {
 		const Quant &q = P.out[oc].q;
-		FTail &T = F.tail[oc];
+		FTail &T = tails[oc];
 		T.P = q.P; T.M = q.maxcc; T.cc = q.cc; T.use_nc = q.use_nc; T.dfam = q.dfam; T.dsub = q.dsub;
 		T.U = dev_derived(q.U, 1, as_float);
 		T.X = dev_derived(q.X, 1, as_float);
@@ -833,8 +1046,11 @@ bool fast_prepare(cudaStream_t st, const Plan &P, Job &J, FastInfo &fi, std::str
 		T.rev = dev_derived(q.rev, 1, as_float);
 		T.nc = q.use_nc ? dev_derived(q.nc, 1, as_float) : nullptr;
 		if(!T.U || !T.X || !T.code || !T.rev || (q.use_nc && !T.nc)) { err = "Out of GPU memory (fast tables)"; return false; }
-		F.maxcc[oc] = P.out[oc].maxcc;
-		F.out_alpha[oc] = P.out[oc].ctype == IW_CHANNELTYPE_ALPHA;
+	}
+	{
+		const size_t tail_off = (flag_off + 256 + flag_bytes + 255) & ~(size_t)255;
+		cudaMemcpyAsync(base + tail_off, tails, sizeof(tails), cudaMemcpyHostToDevice, st);
+		F.tail = (const FTail *)(base + tail_off);
 	}
 
 	// ---- kernel selection
@@ -852,6 +1068,56 @@ bool fast_prepare(cudaStream_t st, const Plan &P, Job &J, FastInfo &fi, std::str
 	}
 #define IWG_VGATHER(NPL_, D_) \
 	if(!FS->vkernel && nplanes == NPL_ && P.in_depth == D_) FS->vkernel = (const void *)k_vgather<NPL_, D_>;
+	// identity layout: plane c reads input channel c, the last one alpha when present
+	bool ident = S.ok && nplanes == P.in_nphys && dec_tab != nullptr;
+	for(int q = 0; q < nplanes && ident; q++) {
+		bool is_a = (F.alpha_src >= 0 && q == nplanes - 1);
+		if(F.pl[q].src != q) ident = false;
+		else if(is_a && (F.pl[q].table || F.pl[q].premul)) ident = false;
+		else if(!is_a && (!F.pl[q].table || F.pl[q].premul != (F.alpha_src >= 0))) ident = false;
+	}
+	if(F.alpha_src >= 0 && F.alpha_src != nplanes - 1) ident = false;
+	// PX pixels per thread, one aligned word group per row
+	const int v_bpp = P.in_nphys * P.in_depth / 8;
+	const uintptr_t v_base = (uintptr_t)J.in + (uintptr_t)P.crop_x * v_bpp + (uintptr_t)P.crop_y * P.in_bpr;
+#define IWG_VPX(NS_, NCH_, A_, D_, PX_) \
+	if(!FS->vkernel && ident && S.arith && S.ns == NS_ && nplanes == NCH_ && (F.alpha_src >= 0) == A_ && \
+		P.in_depth == D_) { \
+		constexpr int nw_ = PX_ * NCH_ * (D_ / 8) / 4; \
+		constexpr uintptr_t va_ = nw_ % 4 == 0 ? 16 : (nw_ % 2 == 0 ? 8 : 4); \
+		if(v_base % va_ == 0 && P.in_bpr % va_ == 0) { \
+			const int threads_ = (F.mid_w + PX_ - 1) / PX_; \
+			const int gxp_ = (threads_ + kVPxThreads - 1) / kVPxThreads; \
+			int bands = std::max(1, std::min(F.mid_h, (5 * 152 + gxp_ / 2) / gxp_)); \
+			F.rows_per_band = (F.mid_h + bands - 1) / bands; \
+			bands = (F.mid_h + F.rows_per_band - 1) / F.rows_per_band; \
+			int nq_max = 0; \
+			for(int b_ = 0; b_ < bands; b_++) { \
+				const int jb_ = b_ * F.rows_per_band, je_ = std::min(jb_ + F.rows_per_band, F.mid_h); \
+				nq_max = std::max(nq_max, S.last_pos[je_ - 1] - S.first_pos[jb_] + 1); \
+			} \
+			const size_t sm_ = (size_t)dec_floats * sizeof(float) + (size_t)nq_max * (NS_ * sizeof(float) + sizeof(int2)); \
+			const void *k_ = (const void *)k_vstream_px<NS_, NCH_, A_, D_, PX_>; \
+			if(sm_ <= 48 * 1024 || (sm_ <= 200 * 1024 && \
+				cudaFuncSetAttribute(k_, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_) == cudaSuccess)) { \
+				FS->vkernel = k_; \
+				FS->vgrid = dim3(gxp_, bands); \
+				FS->vthreads = kVPxThreads; \
+				FS->vsmem = sm_; \
+			} \
+		} \
+	}
+	{
+		IWG_VPX(4, 4, true, 16, 2) IWG_VPX(6, 4, true, 16, 2) IWG_VPX(8, 4, true, 16, 2)
+		IWG_VPX(4, 3, false, 16, 2) IWG_VPX(6, 3, false, 16, 2) IWG_VPX(8, 3, false, 16, 2)
+		IWG_VPX(4, 2, true, 16, 4) IWG_VPX(6, 2, true, 16, 4) IWG_VPX(8, 2, true, 16, 4)
+		IWG_VPX(4, 1, false, 16, 8) IWG_VPX(6, 1, false, 16, 8) IWG_VPX(8, 1, false, 16, 8)
+		IWG_VPX(4, 4, true, 8, 2) IWG_VPX(6, 4, true, 8, 2) IWG_VPX(8, 4, true, 8, 2)
+		IWG_VPX(4, 3, false, 8, 4)
+		IWG_VPX(4, 2, true, 8, 4) IWG_VPX(6, 2, true, 8, 4) IWG_VPX(8, 2, true, 8, 4)
+		IWG_VPX(4, 1, false, 8, 8) IWG_VPX(6, 1, false, 8, 8) IWG_VPX(8, 1, false, 8, 8)
+	}
+#undef IWG_VPX
 	if(S.ok) {
 		IWG_VSTREAM(4, 1, 8) IWG_VSTREAM(4, 2, 8) IWG_VSTREAM(4, 3, 8) IWG_VSTREAM(4, 4, 8)
 		IWG_VSTREAM(6, 1, 8) IWG_VSTREAM(6, 2, 8) IWG_VSTREAM(6, 3, 8) IWG_VSTREAM(6, 4, 8)

@@ -245,10 +245,22 @@ double gray_of(const Plan &P, double r, double g, double b);
 // weights.cpp
 std::shared_ptr<const Weights> build_weights(iw_context *ctx, const DimRequest &d, int ctype,
 	int n_in, int n_out, double edge_bkgd_value);
+// Fills caller arrays without allocating: off (n_out+1), src/w/pos (cap; pos may
+// be null).  Returns the tap count, -1 if cap is too small, -2 for an unknown
+// filter family.
+int weights_into(const DimRequest &d, int ctype, int n_in, int n_out, double edge_bkgd_value,
+	int *off, int *src, double *w, int *pos, int cap, int *kind, double *edge_value);
+// Upper bound on the taps of one output (-1: unknown family).
+int weights_max_taps(const DimRequest &d, int n_in, int n_out);
 
 // tables.cpp
 std::shared_ptr<const std::vector<double>> input_table(int cstype, double gamma, int maxcc, int ncodes, bool linear);
 void build_quant(Quant &q);
+// Non-allocating fills of the quantisation tables for one output channel:
+// U (P+2), X (P+1), code (P+2), rev (maxcc+1), with P = cc ? cc-1 : maxcc.
+void quant_fill(int cstype, double gamma, int maxcc, int cc, double *U, double *X, int *code, double *rev);
+// The 255 nearest-colour midpoints of an 8-bit channel.
+void nc_fill(int cstype, double gamma, double *nc);
 
 // optimize.cpp
 void optimize(iw_context *ctx);

@@ -129,15 +129,19 @@ __device__ __forceinline__ double unassoc_and_bkgd(const Job &J, const DMid &mc,
 
 // Quantise / store every channel of output pixel (i, j) exactly.  Used by the
 // plain form for all pixels and by the fast form for flagged pixels.
+// 'mask' selects the intermediate channels to evaluate (bit m); the alpha
+// channel must be included whenever a colour channel is.
 template<class Interm>
-__device__ void pixel_exact(const Job &J, int i, int j, bool apply_post, Interm interm)
+__device__ void pixel_exact(const Job &J, int i, int j, bool apply_post, Interm interm, unsigned int mask = 0xfu)
 {
 	double a = 0.0;
 	int alpha_code = -1;
 	int codes[dev::kMaxCh];
+	for(int oc = 0; oc < dev::kMaxCh; oc++) codes[oc] = -1;
 	int alt = checker_alt(J, i, j);
 	for(int k = 0; k < J.mid_n; k++) {
 		int m = J.order[k];
+		if(!((mask >> m) & 1u)) continue;
 		const DMid &mc = J.mid[m];
 		bool is_alpha = mc.ctype == IW_CHANNELTYPE_ALPHA;
 		double s = hsum_exact(J, m, i, j, interm);
@@ -309,21 +313,36 @@ __global__ void k_finalize(Job J)
 	}
 }
 
-// Exact re-evaluation of the pixels the fast form flagged.  One warp per
-// pixel: the lanes recompute, in FP64, the intermediate values the pixel's
-// horizontal taps read (each one a vertical sum), then lane 0 finishes the
-// pixel in the reference's order.  Scratch: 'maxt' floats per channel per warp.
+// Position of the r-th set bit of 'mask' (r counts from 0).
+__device__ __forceinline__ int nth_bit(unsigned int mask, int r)
+{
+	for(int k = 0; k < r; k++) mask &= mask - 1u;
+	return __ffs(mask) - 1;
+}
+
+// Exact re-evaluation of the pixels the fast form flagged, one warp per
+// pixel.  FP64 throughput is what limits this kernel, so the work is spread
+// over as many lanes as a pixel offers: first the lanes recompute the
+// intermediate values the pixel's horizontal taps read (one vertical FP64 sum
+// per (channel, tap), for the channels in the pixel's mask), then lane m
+// finishes intermediate channel m -- its horizontal sum, unassociation and
+// quantisation -- with the alpha value and alpha code passed between lanes.
+// The result equals pixel_exact()'s.  Scratch: 'maxt' floats per channel per warp.
 __global__ void k_fix_flagged_warp(Job J, const int *count, const int *list, int maxt)
 {
 	extern __shared__ float fix_cache[];
 	const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, wpb = blockDim.x >> 5;
 	float *my = fix_cache + (size_t)wib * dev::kMaxCh * maxt;
 	const int n = *count;
+	const unsigned int all = (1u << J.mid_n) - 1u;
 	for(int f = blockIdx.x * wpb + wib; f < n; f += gridDim.x * wpb) {
-		const int p = list[f];
+		const int p = list[2 * f];
+		const unsigned int mask = (unsigned int)list[2 * f + 1] & all;
 		const int i = p % J.out_w, j = p / J.out_w;
-		for(int k = lane; k < J.mid_n * maxt; k += 32) {
-			const int m = k / maxt, t = k % maxt;
+		const int ntask = __popc(mask) * maxt;
+		for(int k = lane; k < ntask; k += 32) {
+			const int r = k / maxt, t = k - r * maxt;
+			const int m = nth_bit(mask, r);
 			const DWeights &W = J.wh[J.mid[m].wh];
 			const int t0 = W.kind == 1 ? i : W.off[i];
 			const int nt = W.kind == 1 ? 1 : W.off[i + 1] - t0;
@@ -333,7 +352,38 @@ __global__ void k_fix_flagged_warp(Job J, const int *count, const int *list, int
 			}
 		}
 		__syncwarp();
-		if(lane == 0) pixel_exact(J, i, j, true, [&](int m, int k, int) { return (double)my[m * maxt + k]; });
+		const bool mine = lane < J.mid_n && ((mask >> lane) & 1u);
+		double s = 0.0;
+		if(mine) s = hsum_exact(J, lane, i, j, [&](int m, int k, int) { return (double)my[m * maxt + k]; });
+		const int al = J.mid_alpha >= 0 ? J.mid_alpha : 0;
+		const double a = (double)__double2float_rn(__shfl_sync(0xffffffffu, s, al));
+		int code = -1, oc = -1;
+		bool is_alpha = false;
+		if(mine) {
+			const DMid &mc = J.mid[lane];
+			is_alpha = mc.ctype == IW_CHANNELTYPE_ALPHA;
+			oc = mc.out_ch;
+			if(oc >= 0) {
+				const DOut &o = J.outc[oc];
+				const double v = unassoc_and_bkgd(J, mc, o, s, a, checker_alt(J, i, j), is_alpha);
+				if(J.out_float) {
+					float fv = __double2float_rn(v);
+					if(J.negate && !is_alpha) fv = __fsub_rn(1.0f, fv);
+					store_float(J, oc, i, j, fv);
+				}
+				else if(o.scan) J.scanbuf[((unsigned long long)oc * J.out_h + j) * J.out_w + i] = v;
+				else code = quantize_exact(o.q, v, i, j);
+			}
+		}
+		const int ac = __shfl_sync(0xffffffffu, code, al);
+		const int alpha_code = (J.mid_alpha >= 0 && J.mid[al].out_ch >= 0) ? ac : -1;
+		if(code >= 0) {
+			if(!is_alpha) {
+				if(J.negate) code = J.outc[oc].maxcc - code;
+				if(J.blacken && alpha_code == 0) code = 0;
+			}
+			store_code(J, oc, i, j, (unsigned int)code);
+		}
 		__syncwarp();
 	}
 }
@@ -343,9 +393,10 @@ __global__ void k_fix_flagged_thread(Job J, const int *count, const int *list)
 {
 	const int n = *count;
 	for(int f = blockIdx.x * blockDim.x + threadIdx.x; f < n; f += gridDim.x * blockDim.x) {
-		const int p = list[f];
+		const int p = list[2 * f];
 		const int j = p / J.out_w;
-		pixel_exact(J, p % J.out_w, j, true, [&](int m, int, int x) { return interm_exact<true>(J, m, x, j); });
+		pixel_exact(J, p % J.out_w, j, true, [&](int m, int, int x) { return interm_exact<true>(J, m, x, j); },
+			(unsigned int)list[2 * f + 1]);
 	}
 }
 
@@ -357,8 +408,10 @@ void launch_fix_flagged(cudaStream_t st, const Job &J, const int *count, const i
 	const size_t per_warp = (size_t)dev::kMaxCh * maxt * sizeof(float);
 	int wpb = 4;
 	while(wpb > 1 && per_warp * wpb > 48 * 1024) wpb >>= 1;
-	if(per_warp * wpb <= 48 * 1024) k_fix_flagged_warp<<<2 * 152, 32 * wpb, per_warp * wpb, st>>>(J, count, list, maxt);
-	else k_fix_flagged_thread<<<2 * 152, 64, 0, st>>>(J, count, list);
+	// Flagged pixels are independent and each is a latency-bound FP64 chain:
+	// launch enough warps to take them all at once (idle warps exit at once).
+	if(per_warp * wpb <= 48 * 1024) k_fix_flagged_warp<<<24 * 152, 32 * wpb, per_warp * wpb, st>>>(J, count, list, maxt);
+	else k_fix_flagged_thread<<<24 * 152, 64, 0, st>>>(J, count, list);
 }
 
 // ===========================================================================

@@ -134,51 +134,66 @@ struct QuantTables {
 
 }  // namespace
 
+void quant_fill(int cstype, double gamma, int maxcc, int cc, double *U, double *X, int *code, double *rev)
+{
+	struct iw_csdescr cs{};
+	cs.cstype = cstype;
+	cs.gamma = gamma;
+	const int P = cc ? cc - 1 : maxcc, M = maxcc;
+	GFun g;
+	g.cs = cs;
+	g.P = (double)P;
+	const double inf = std::numeric_limits<double>::infinity();
+	U[0] = -inf;
+	U[P + 1] = inf;
+	for(int k = 1; k <= P; k++) {
+		double guess = to_linear((double)k / P, cs);
+		U[k] = lowest_true([&](double v) { return g(v) >= (double)k; }, guess);
+	}
+	for(int k = 0; k < P; k++) {
+		double guess = U[k + 1];
+		if(k > 0 && guess < U[k]) guess = U[k];
+		X[k] = lowest_true([&](double v) { return g(v) > (double)k; }, guess);
+	}
+	X[P] = inf;
+	// bracket -> code: posterised codes are floor(0.5000000001 + k*(M/P))
+	for(int k = 0; k <= P; k++) {
+		if(cc) code[k] = (int)(unsigned int)floor(0.5000000001 + (double)k * ((double)M / (double)P));
+		else code[k] = k;
+	}
+	code[P + 1] = code[P];
+	for(int c = 0; c <= M; c++) rev[c] = to_linear(((double)c) / (double)M, cs);
+}
+
+// midpoints between adjacent 8-bit codes in linear light (src/imagew-main.c:1197-1236)
+void nc_fill(int cstype, double gamma, double *nc)
+{
+	struct iw_csdescr cs{};
+	cs.cstype = cstype;
+	cs.gamma = gamma;
+	double prev = 0.0;
+	for(int i = 0; i < 255; i++) {
+		double cur = to_linear(((double)(i + 1)) / 255, cs);
+		nc[i] = (prev + cur) / 2.0;
+		prev = cur;
+	}
+}
+
 void build_quant(Quant &q)
 {
 	static std::map<std::tuple<int, uint64_t, int, int>, QuantTables> cache;
 	static std::map<std::tuple<int, uint64_t>, std::shared_ptr<const std::vector<double>>> nc_cache;
 
 	q.P = q.cc ? q.cc - 1 : q.maxcc;
-	struct iw_csdescr cs{};
-	cs.cstype = q.cstype;
-	cs.gamma = q.gamma;
 	auto key = std::make_tuple(q.cstype, dbits(q.gamma), q.maxcc, q.cc);
-
 	std::lock_guard<std::mutex> lk(g_cache_mu);
 	auto it = cache.find(key);
 	if(it == cache.end()) {
-		const int P = q.P, M = q.maxcc;
-		GFun g;
-		g.cs = cs;
-		g.P = (double)P;
-		auto U = std::make_shared<std::vector<double>>(P + 2);
-		auto X = std::make_shared<std::vector<double>>(P + 1);
-		auto code = std::make_shared<std::vector<int>>(P + 2);
-		auto rev = std::make_shared<std::vector<double>>(M + 1);
-		const double inf = std::numeric_limits<double>::infinity();
-		(*U)[0] = -inf;
-		(*U)[P + 1] = inf;
-		for(int k = 1; k <= P; k++) {
-			double guess = to_linear((double)k / P, cs);
-			(*U)[k] = lowest_true([&](double v) { return g(v) >= (double)k; }, guess);
-		}
-		for(int k = 0; k < P; k++) {
-			double guess = (*U)[k + 1];
-			if(k > 0 && guess < (*U)[k]) guess = (*U)[k];
-			(*X)[k] = lowest_true([&](double v) { return g(v) > (double)k; }, guess);
-		}
-		(*X)[P] = inf;
-		// bracket -> code: posterised codes are floor(0.5000000001 + k*(M/P))
-		for(int k = 0; k <= P; k++) {
-			if(q.cc) {
-				double f = floor(0.5000000001 + (double)k * ((double)M / (double)P));
-				(*code)[k] = (int)(unsigned int)f;
-			}
-			else (*code)[k] = k;
-		}
-		(*code)[P + 1] = (*code)[P];
-		for(int c = 0; c <= M; c++) (*rev)[c] = to_linear(((double)c) / (double)M, cs);
+		auto U = std::make_shared<std::vector<double>>(q.P + 2);
+		auto X = std::make_shared<std::vector<double>>(q.P + 1);
+		auto code = std::make_shared<std::vector<int>>(q.P + 2);
+		auto rev = std::make_shared<std::vector<double>>(q.maxcc + 1);
+		quant_fill(q.cstype, q.gamma, q.maxcc, q.cc, U->data(), X->data(), code->data(), rev->data());
 		QuantTables t;
 		t.U = U; t.X = X; t.code = code; t.rev = rev;
 		it = cache.emplace(key, t).first;
@@ -187,19 +202,12 @@ void build_quant(Quant &q)
 	q.X = it->second.X;
 	q.code = it->second.code;
 	q.rev = it->second.rev;
-
 	if(q.use_nc) {
-		// midpoints between adjacent 8-bit codes in linear light (src/imagew-main.c:1197-1236)
 		auto nkey = std::make_tuple(q.cstype, dbits(q.gamma));
 		auto nit = nc_cache.find(nkey);
 		if(nit == nc_cache.end()) {
 			auto nc = std::make_shared<std::vector<double>>(255);
-			double prev = 0.0;
-			for(int i = 0; i < 255; i++) {
-				double cur = to_linear(((double)(i + 1)) / 255, cs);
-				(*nc)[i] = (prev + cur) / 2.0;
-				prev = cur;
-			}
+			nc_fill(q.cstype, q.gamma, nc->data());
 			nit = nc_cache.emplace(nkey, nc).first;
 		}
 		q.nc = nit->second;

@@ -82,19 +82,27 @@ double kernel_at(const Kernel &k, double x)
 
 }  // namespace
 
-std::shared_ptr<const Weights> build_weights(iw_context *ctx, const DimRequest &d, int ctype,
-	int n_in, int n_out, double edge_bkgd_value)
-{
-	auto wt = std::make_shared<Weights>();
-	Kernel k;
-	k.family = d.family;
-	bool standard = true, boxhack = false, sincfam = false;
-	wt->n_in = n_in;
-	wt->n_out = n_out;
+namespace {
 
+// Filter parameters of one dimension (src/imagew-resize.c:412-556).
+struct DimSetup {
+	Kernel k;
+	bool standard = true;
+	double offset = 0.0;
+	double rf = 1.0;
+	double edge_value = 0.0;
+	int max_window = 1;   // upper bound on the taps of one output
+};
+
+// Returns false for an unknown filter family.
+bool setup_dim(const DimRequest &d, int ctype, int n_in, int n_out, double edge_bkgd_value, DimSetup &S)
+{
+	Kernel &k = S.k;
+	k.family = d.family;
+	bool boxhack = false, sincfam = false;
 	switch(d.family) {
-	case IW_RESIZETYPE_NULL: standard = false; break;
-	case IW_RESIZETYPE_NEAREST: standard = false; boxhack = true; break;
+	case IW_RESIZETYPE_NULL: S.standard = false; break;
+	case IW_RESIZETYPE_NEAREST: S.standard = false; boxhack = true; break;
 	case IW_RESIZETYPE_MIX:
 		k.mix = ((double)n_out) / n_in;
 		if(k.mix > 1.0) k.mix = 1.0 / k.mix;
@@ -116,70 +124,72 @@ std::shared_ptr<const Weights> build_weights(iw_context *ctx, const DimRequest &
 		sincfam = true;
 		break;
 	default:
-		iw_set_error(ctx, "Internal: Unknown resize algorithm");
-		return nullptr;
+		return false;
 	}
 	if(sincfam) {   // "lobes", clamped to [2,100]
 		k.radius = floor(d.p1 + 0.5);
 		if(k.radius < 2.0) k.radius = 2.0;
 		if(k.radius > 100.0) k.radius = 100.0;
 	}
-	wt->edge_value = d.edge == IW_EDGE_POLICY_TRANSPARENT ? edge_bkgd_value : 0.0;
+	S.edge_value = d.edge == IW_EDGE_POLICY_TRANSPARENT ? edge_bkgd_value : 0.0;
+	S.offset = d.translate;
+	if(boxhack) S.offset -= 0.00000000001;   // keep pixel centres off box borders
+	if(d.use_offset && ctype >= 0 && ctype <= 2) S.offset += d.chan_offset[ctype];
+	if(S.standard) {
+		double blur = d.blur;
+		if(blur < 0.0001) blur = 0.0001;
+		if(blur > 10000.0) blur = 10000.0;
+		S.rf = (d.true_size < (double)n_in) ? ((double)n_in) / d.true_size : 1.0;
+		S.rf *= blur;
+		S.max_window = (int)floor(2.0 * k.radius * S.rf + 0.0002) + 2;
+	}
+	return true;
+}
 
-	double offset = d.translate;
-	if(boxhack) offset -= 0.00000000001;   // keep pixel centres off box borders
-	if(d.use_offset && ctype >= 0 && ctype <= 2) offset += d.chan_offset[ctype];
+}  // namespace
 
-	wt->off.assign(1, 0);
-	if(!standard) {
+int weights_into(const DimRequest &d, int ctype, int n_in, int n_out, double edge_bkgd_value,
+	int *off, int *src, double *w, int *pos, int cap, int *kind, double *edge_value)
+{
+	DimSetup S;
+	if(!setup_dim(d, ctype, n_in, n_out, edge_bkgd_value, S)) return -2;
+	*edge_value = S.edge_value;
+	off[0] = 0;
+	int n = 0;
+	if(!S.standard) {
 		// NULL: copy, padding with 0 (src/imagew-resize.c:399-410);
 		// NEAREST: nearest source pixel (src/imagew-resize.c:377-393).
-		wt->kind = RowKind::Copy;
+		*kind = (int)RowKind::Copy;
+		if(cap < n_out) return -1;
 		for(int o = 0; o < n_out; o++) {
 			int s;
 			if(d.family == IW_RESIZETYPE_NULL) s = o < n_in ? o : -1;
 			else {
-				double c = (0.5 + (double)o - offset) / (double)n_out;
+				double c = (0.5 + (double)o - S.offset) / (double)n_out;
 				s = (int)floor(c * (double)n_in);
 				if(s < 0) s = 0;
 				if(s > n_in - 1) s = n_in - 1;
 			}
-			wt->src.push_back(s);
-			wt->pos.push_back(s);
-			wt->w.push_back(1.0);
-			wt->off.push_back((int)wt->src.size());
+			src[n] = s;
+			if(pos) pos[n] = s;
+			w[n] = 1.0;
+			n++;
+			off[o + 1] = n;
 		}
-		wt->max_taps = 1;
-		wt->wsum_abs_max = 1.0;
-		return wt;
+		return n;
 	}
-
-	double blur = d.blur;
-	if(blur < 0.0001) blur = 0.0001;
-	if(blur > 10000.0) blur = 10000.0;
-	double rf = (d.true_size < (double)n_in) ? ((double)n_in) / d.true_size : 1.0;
-	rf *= blur;
-
-	// The reference sizes its first allocation from this estimate; an
-	// estimate above the allocation limit is an out-of-memory error there.
-	double est = 2.0 * k.radius * rf * n_out;
-	if(((size_t)(int)est + 32) * 16 > ctx->max_malloc) {
-		iw_set_error(ctx, "Out of memory");
-		return nullptr;
-	}
-	wt->src.reserve((size_t)est + 32);
-
+	*kind = (int)RowKind::Sum;
+	const Kernel &k = S.k;
 	for(int o = 0; o < n_out; o++) {
-		double center = (0.5 + (double)o - offset) / d.true_size;
+		double center = (0.5 + (double)o - S.offset) / d.true_size;
 		double p = center * (double)n_in - 0.5;
-		int first = (int)ceil(p - k.radius * rf - 0.0001);
-		int last = (int)floor(p + k.radius * rf + 0.0001);
-		size_t start = wt->w.size();
-		int count = 0;
+		int first = (int)ceil(p - k.radius * S.rf - 0.0001);
+		int last = (int)floor(p + k.radius * S.rf + 0.0001);
+		int start = n, count = 0;
 		double sum = 0.0;
 		for(int ip = first; ip <= last; ip++) {
 			if(d.edge == IW_EDGE_POLICY_STANDARD && (ip < 0 || ip >= n_in)) continue;
-			double x = (((double)ip) - p) / rf;
+			double x = (((double)ip) - p) / S.rf;
 			double v = kernel_at(k, x < 0 ? -x : x);
 			if(v == 0.0) continue;
 			sum += v;
@@ -189,19 +199,69 @@ std::shared_ptr<const Weights> build_weights(iw_context *ctx, const DimRequest &
 				if(d.edge == IW_EDGE_POLICY_TRANSPARENT) s = -1;
 				else s = ip < 0 ? 0 : n_in - 1;
 			}
-			wt->src.push_back(s);
-			wt->pos.push_back(ip);
-			wt->w.push_back(v);
+			if(n >= cap) return -1;
+			src[n] = s;
+			if(pos) pos[n] = ip;
+			w[n] = v;
+			n++;
 		}
 		if(count > 0)
-			for(size_t i = start; i < wt->w.size(); i++) wt->w[i] = (sum != 0.0) ? wt->w[i] / sum : 0.0;
-		wt->off.push_back((int)wt->w.size());
-		int nt = (int)(wt->w.size() - start);
+			for(int i = start; i < n; i++) w[i] = (sum != 0.0) ? w[i] / sum : 0.0;
+		off[o + 1] = n;
+	}
+	return n;
+}
+
+int weights_max_taps(const DimRequest &d, int n_in, int n_out)
+{
+	DimSetup S;
+	if(!setup_dim(d, 0, n_in, n_out, 0.0, S)) return -1;
+	return S.standard ? S.max_window : 1;
+}
+
+std::shared_ptr<const Weights> build_weights(iw_context *ctx, const DimRequest &d, int ctype,
+	int n_in, int n_out, double edge_bkgd_value)
+{
+	DimSetup S;
+	if(!setup_dim(d, ctype, n_in, n_out, edge_bkgd_value, S)) {
+		iw_set_error(ctx, "Internal: Unknown resize algorithm");
+		return nullptr;
+	}
+	if(S.standard) {
+		// The reference sizes its first allocation from this estimate; an
+		// estimate above the allocation limit is an out-of-memory error there.
+		double est = 2.0 * S.k.radius * S.rf * n_out;
+		if(((size_t)(int)est + 32) * 16 > ctx->max_malloc) {
+			iw_set_error(ctx, "Out of memory");
+			return nullptr;
+		}
+	}
+	auto wt = std::make_shared<Weights>();
+	wt->n_in = n_in;
+	wt->n_out = n_out;
+	size_t cap = (size_t)n_out * (size_t)S.max_window;
+	wt->off.resize(n_out + 1);
+	wt->src.resize(cap);
+	wt->w.resize(cap);
+	wt->pos.resize(cap);
+	int kind = 0;
+	int n = weights_into(d, ctype, n_in, n_out, edge_bkgd_value, wt->off.data(), wt->src.data(), wt->w.data(),
+		wt->pos.data(), (int)cap, &kind, &wt->edge_value);
+	if(n < 0) {
+		iw_set_error(ctx, "Internal: weight list overflow");
+		return nullptr;
+	}
+	wt->kind = (RowKind)kind;
+	wt->src.resize(n);
+	wt->w.resize(n);
+	wt->pos.resize(n);
+	for(int o = 0; o < n_out; o++) {
+		int nt = wt->off[o + 1] - wt->off[o];
 		if(nt > wt->max_taps) wt->max_taps = nt;
 		double sa = 0, sn = 0;
-		for(size_t i = start; i < wt->w.size(); i++) {
-			sa += fabs(wt->w[i]);
-			if(wt->w[i] < 0) sn -= wt->w[i];
+		for(int t = wt->off[o]; t < wt->off[o + 1]; t++) {
+			sa += fabs(wt->w[t]);
+			if(wt->w[t] < 0) sn -= wt->w[t];
 		}
 		if(sa > wt->wsum_abs_max) wt->wsum_abs_max = sa;
 		if(sn > wt->wsum_neg_max) wt->wsum_neg_max = sn;
