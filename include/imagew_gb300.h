@@ -51,6 +51,40 @@ IW_EXPORT(int) iwg_process_image_timed(struct iw_context *ctx, int warmup, int i
  * buf (NUL-terminated, at most buflen bytes).  Returns 0 if no device. */
 IW_EXPORT(int) iwg_device_info(char *buf, int buflen);
 
+/* Resamples one 8-bit image without allocating any memory, host or device.
+ * No counterpart in the reference: it is the iw_process_image() pixel path
+ * (reference arithmetic, FP64 form, bit-identical output) narrowed to what a
+ * caller that cannot allocate needs:
+ *   - imgtype IW_IMGTYPE_GRAY, _GRAYA, _RGB or _RGBA, 8 bits per sample, the
+ *     same type in and out; alpha is premultiplied for resampling and colour
+ *     samples of fully transparent output pixels are set to 0, as
+ *     iw_process_image() does for an output profile that keeps transparency
+ *     (a gray image comes out as iw_process_image() returns it once its
+ *     output post-pass has packed the three equal channels back to gray);
+ *   - one resize algorithm for both dimensions (IW_RESIZETYPE_*, with
+ *     param1/param2 as in iw_set_resize_alg(), blur 1, standard edges);
+ *   - one colour space (IW_CSTYPE_*, gamma for IW_CSTYPE_GAMMA) for input and
+ *     output; no dithering, background, crop, offsets or posterisation.
+ * src and dst must be readable / writable by kernels on the current device:
+ * device or managed memory, mapped pinned memory, or ordinary host memory on a
+ * device with pageable memory access.  The work is queued on 'stream' (a
+ * cudaStream_t; NULL for the default stream) and the call returns without
+ * waiting; dst is complete when the stream is.
+ * Limits: dimensions 1..16384; weight lists of both dimensions within a 4 MiB
+ * staging area; tables + weight lists + the float intermediate image
+ * (4 * channels * dst_h * src_w bytes) within a 32 MiB device scratch array.
+ * A job beyond a limit is rejected with a message and nothing is launched.
+ * All calls share that scratch array and staging area: calls must be ordered
+ * (one stream, or synchronised between streams); overlapping calls on
+ * unsynchronised streams race.  The first call on each device resolves the
+ * scratch array's address (which may load the library's module on that
+ * device); make it before any stream capture.
+ * Returns 1 on success; 0 on error, with a message in errmsg (at most
+ * errmsg_len bytes, NUL-terminated) when errmsg is not NULL. */
+IW_EXPORT(int) iwg_resize_u8_noalloc(const unsigned char *src, int src_w, int src_h, long long src_bpr,
+	unsigned char *dst, int dst_w, int dst_h, long long dst_bpr, int imgtype, int resize_type,
+	double param1, double param2, int cstype, double gamma, void *stream, char *errmsg, int errmsg_len);
+
 #ifdef __cplusplus
 }
 #endif
