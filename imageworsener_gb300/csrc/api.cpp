@@ -11,8 +11,12 @@
 #include <cstdlib>
 #include <cstring>
 #include <strings.h>
+#include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <ctime>
+#include <thread>
+#include <vector>
 
 using iwg::kMsgMax;
 
@@ -912,3 +916,104 @@ extern "C" int iwg_process_image_timed(struct iw_context *ctx, int warmup, int i
 	ctx->stats.ms_total = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
 	return 1;
 }
+
+// ---- batches (include/imagew_gb300.h) ----
+
+namespace {
+
+// Runs fn(i) for i in [0, n) on up to hardware_concurrency threads.
+template<class Fn>
+void parallel_for(int n, Fn fn)
+{
+	int T = (int)std::thread::hardware_concurrency();
+	T = std::max(1, std::min(T, std::min(n, 64)));
+	if(T == 1) {
+		for(int i = 0; i < n; i++) fn(i);
+		return;
+	}
+	std::atomic<int> next(0);
+	std::vector<std::thread> th;
+	for(int t = 0; t < T; t++)
+		th.emplace_back([&]() {
+			for(int i = next++; i < n; i = next++) fn(i);
+		});
+	for(std::thread &x : th) x.join();
+}
+
+// Device bytes one image of a batch holds while it runs (input, float
+// intermediate, output, flag entries).
+size_t batch_bytes(const iwg::Plan &P)
+{
+	const size_t in = P.in_bpr * (size_t)(P.orient >= 4 ? P.img1_w : P.img1_h);
+	const size_t mid = (size_t)P.mid_n * P.crop_w * P.out_h * sizeof(float);
+	const size_t out = P.out_bpr * (size_t)P.out_h;
+	return in + mid + out + (size_t)P.out_w * P.out_h * 16 + 4096;
+}
+
+}  // namespace
+
+extern "C" int iwg_process_batch(struct iw_context **ctxs, int n)
+{
+	if(!ctxs || n <= 0) return 0;
+	auto t0 = std::chrono::steady_clock::now();
+	std::vector<iwg::Plan> plans(n);
+	std::vector<char> planned(n, 0);
+	parallel_for(n, [&](int i) {
+		iw_context *ctx = ctxs[i];
+		if(!ctx) return;
+		if(ctx->use_count > 0) {
+			iw_set_error(ctx, "Internal: Incorrect attempt to reprocess image");
+			return;
+		}
+		ctx->use_count++;
+		planned[i] = iwg::build_plan(ctx, plans[i]) ? 1 : 0;
+	});
+	// chunks of at most kBudget device bytes, in the callers' order
+	const size_t kBudget = (size_t)8 << 30;
+	std::vector<char> done(n, 0);
+	std::vector<int> order;
+	for(int i = 0; i < n; i++) if(planned[i]) order.push_back(i);
+	std::vector<char> batched(n, 0);
+	double dev_total = 0;
+	size_t k = 0;
+	while(k < order.size()) {
+		std::vector<iw_context *> cc;
+		std::vector<iwg::Plan *> pp;
+		std::vector<int> idx;
+		size_t bytes = 0;
+		while(k < order.size()) {
+			const int i = order[k];
+			const size_t b = batch_bytes(plans[i]);
+			if(!idx.empty() && bytes + b > kBudget) break;
+			bytes += b;
+			cc.push_back(ctxs[i]);
+			pp.push_back(&plans[i]);
+			idx.push_back(i);
+			k++;
+		}
+		std::vector<int> status;
+		double dev_ms = 0;
+		iwg::run_batch(cc, pp, status, dev_ms);
+		dev_total += dev_ms;
+		for(size_t j = 0; j < idx.size(); j++) {
+			const int i = idx[j];
+			if(status[j] == 1) done[i] = batched[i] = 1;
+			else if(status[j] == 0) done[i] = iwg::run_pipeline(ctxs[i], plans[i]) ? 1 : 0;   // alone
+		}
+	}
+	parallel_for(n, [&](int i) {
+		if(!done[i]) return;
+		iwg::bkgd_label(ctxs[i], plans[i]);
+		iwg::optimize(ctxs[i]);
+	});
+	const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+	int ok = 0;
+	for(int i = 0; i < n; i++)
+		if(done[i]) {
+			ctxs[i]->stats.ms_total = ms;
+			if(batched[i]) ctxs[i]->stats.ms_device = dev_total;
+			ok++;
+		}
+	return ok;
+}
+

@@ -18,6 +18,7 @@
 // bound is propagated.
 #include "iwg_internal.h"
 #include "device.cuh"
+#include "fastkern.cuh"
 #include "fastpath.cuh"
 
 #include <algorithm>
@@ -35,620 +36,33 @@ void launch_fix_flagged(cudaStream_t st, const Job &J, const int *count, const i
 
 namespace {
 
-constexpr int kVThreads = 128;
-constexpr int kHThreads = 128;
-constexpr int kVPxThreads = 128;
-constexpr int kMaxPlanes = 4;
+using namespace fp;
 
-struct FPlane {
-	int src;          // physical channel, -1: virtual (value 1)
-	int table;        // 1: decode through the shared table; 0: code * inv
-	int premul;       // multiply by the alpha value
-	float inv;        // 1 / maxcc for arithmetic decode
-};
-
-struct FTail {        // quantisation of one output channel, float tables
-	int P, M, cc, use_nc, dfam, dsub;
-	const float *U;   // P+2
-	const float *X;   // P+1
-	const int *code;  // P+2
-	const float *rev; // M+1
-	const float *nc;  // 255
-};
-
-struct FJob {
-	// input
-	const uint8_t *in;
-	unsigned long long in_bpr;
-	int crop_x, crop_y, nphys, depth;
-	int alpha_src;    // physical alpha channel, -1 virtual/none
-	float alpha_inv;
-	int npl;
-	FPlane pl[kMaxPlanes];
-	int vec;                   // 8 / 4: pixels load as one aligned 8- / 4-byte word; 0: bytes
-	const float *dec_tab;      // 8-bit: 256 floats; 16-bit: 4096 (T0, slope) pairs
-	int dec_tab_floats;
-	// vertical pass
-	int mid_w, mid_h;
-	float *interm;
-	unsigned long long plane;
-	// streaming
-	int pmin, npos, ns;
-	const int2 *pinfo;        // per position: (first row finalised, count)
-	const float *sw;          // per position: ns slot weights (padded to 8)
-	const int *srcrow;        // per position: input row, -1 virtual
-	const int *first_pos, *last_pos;
-	int rows_per_band;
-	int in_rows;              // crop height: input rows of the vertical pass
-	// gather (upscale) vertical pass
-	const int *voff, *vsrc;
-	const float *vw;
-	// horizontal pass
-	const int *hoff, *hsrc;
-	const float *hw;
-	int out_w, out_h, out_n, out_depth;
-	uint8_t *out;
-	unsigned long long out_bpr;
-	// per processing slot k (alpha first), so kernels index these statically
-	int mid_n;
-	int k_plane[dev::kMaxCh];   // plane holding the channel's intermediate
-	int k_out[dev::kMaxCh];     // output channel
-	int k_alpha[dev::kMaxCh];   // 1: the alpha channel
-	int k_unassoc[dev::kMaxCh]; // 1: colour channel divided by alpha
-	int k_maxcc[dev::kMaxCh];   // output max code (negation)
-	unsigned int k_bit[dev::kMaxCh];  // bit of the intermediate channel in re-evaluation masks
-	int alpha_plane;
-	const FTail *tail;         // per output channel (device memory)
-	int negate, blacken;
-	// error model
-	float K0[kMaxPlanes], K1[kMaxPlanes];
-	// flags
-	int *flag_count;
-	int *flag_list;
-};
-
-// ---------------------------------------------------------------------------
-// decode
-// ---------------------------------------------------------------------------
-
-template<int DEPTH>
-__device__ __forceinline__ unsigned int fetch_code(const uint8_t *px, int ch)
-{
-	if(DEPTH == 8) return px[ch];
-	return ((unsigned int)px[2 * ch] << 8) | px[2 * ch + 1];
-}
-
-template<int DEPTH>
-__device__ __forceinline__ float dec_table(const float *tab, unsigned int code)
-{
-	if(DEPTH == 8) return tab[code];
-	float2 t = reinterpret_cast<const float2 *>(tab)[code >> 4];
-	return __fmaf_rn((float)(code & 15u), t.y, t.x);
-}
-
-template<int NPL, int DEPTH>
-__device__ __forceinline__ void decode_pixel(const FJob &F, const float *tab, const uint8_t *px, float *val)
-{
-	float a = 1.0f;
-	if(F.alpha_src >= 0) a = __fmul_rn((float)fetch_code<DEPTH>(px, F.alpha_src), F.alpha_inv);
-#pragma unroll
-	for(int c = 0; c < NPL; c++) {
-		const FPlane &P = F.pl[c];
-		float v;
-		if(P.src < 0) v = 1.0f;
-		else {
-			unsigned int code = fetch_code<DEPTH>(px, P.src);
-			v = P.table ? dec_table<DEPTH>(tab, code) : __fmul_rn((float)code, P.inv);
-		}
-		val[c] = P.premul ? __fmul_rn(v, a) : v;
-	}
-}
-
-// ---------------------------------------------------------------------------
-// vertical pass, streaming: each thread owns one column; input rows are read
-// once, in order, and accumulated into NS register slots, one per output row
-// whose window is open (slot = row mod NS).
-// ---------------------------------------------------------------------------
-// Raw bytes of one input pixel (at most 8: four 16-bit channels).
-struct Raw {
-	uint32_t lo, hi;
-};
-
-__device__ __forceinline__ Raw load_raw(const FJob &F, const uint8_t *px, int bpp)
-{
-	Raw r{0u, 0u};
-	if(F.vec == 8) {
-		uint2 v = __ldg(reinterpret_cast<const uint2 *>(px));
-		r.lo = v.x;
-		r.hi = v.y;
-	}
-	else if(F.vec == 4) r.lo = __ldg(reinterpret_cast<const unsigned int *>(px));
-	else {
-		for(int b = 0; b < bpp; b++) {
-			uint32_t byte = __ldg(px + b);
-			if(b < 4) r.lo |= byte << (8 * b);
-			else r.hi |= byte << (8 * (b - 4));
-		}
-	}
-	return r;
-}
-
-__device__ __forceinline__ unsigned int raw_byte(const Raw &r, int b)
-{
-	return ((b < 4 ? (r.lo >> (8 * b)) : (r.hi >> (8 * (b - 4))))) & 0xffu;
-}
-
-template<int DEPTH>
-__device__ __forceinline__ unsigned int raw_code(const Raw &r, int ch)
-{
-	if(DEPTH == 8) return raw_byte(r, ch);
-	return (raw_byte(r, 2 * ch) << 8) | raw_byte(r, 2 * ch + 1);   // big-endian samples
-}
-
-template<int NPL, int DEPTH>
-__device__ __forceinline__ void decode_raw(const FJob &F, const float *tab, const Raw &px, float *val)
-{
-	float a = 1.0f;
-	if(F.alpha_src >= 0) a = __fmul_rn((float)raw_code<DEPTH>(px, F.alpha_src), F.alpha_inv);
-#pragma unroll
-	for(int c = 0; c < NPL; c++) {
-		const FPlane &P = F.pl[c];
-		float v;
-		if(P.src < 0) v = 1.0f;
-		else {
-			unsigned int code = raw_code<DEPTH>(px, P.src);
-			v = P.table ? dec_table<DEPTH>(tab, code) : __fmul_rn((float)code, P.inv);
-		}
-		val[c] = P.premul ? __fmul_rn(v, a) : v;
-	}
-}
-
-// Vertical pass, streaming.  Each thread owns one column and walks the input
-// rows of its band once, in order, keeping PF rows of loads in flight; every
-// row is decoded once and accumulated into NS register slots, one per output
-// row whose window is open (slot = row mod NS).  A slot is stored and cleared
-// when its row's window closes.
 template<int NS, int NPL, int DEPTH>
 __global__ void __launch_bounds__(kVThreads) k_vstream(FJob F)
 {
-	constexpr int PF = 8;
-	extern __shared__ float s_tab[];
-	for(int k = threadIdx.x; k < F.dec_tab_floats; k += blockDim.x) s_tab[k] = F.dec_tab[k];
-	__syncthreads();
-
-	const int x = blockIdx.x * blockDim.x + threadIdx.x;
-	const bool active = x < F.mid_w;
-	const int jb = blockIdx.y * F.rows_per_band;
-	const int je = min(jb + F.rows_per_band, F.mid_h);
-	if(jb >= je) return;
-	const int p0 = F.first_pos[jb], p1 = F.last_pos[je - 1];
-	const int bpp = F.nphys * (DEPTH / 8);
-	const uint8_t *colbase = F.in + (size_t)(F.crop_x + (active ? x : 0)) * bpp +
-		(unsigned long long)F.crop_y * F.in_bpr;
-
-	float acc[NS][NPL];
-#pragma unroll
-	for(int s = 0; s < NS; s++)
-#pragma unroll
-		for(int c = 0; c < NPL; c++) acc[s][c] = 0.0f;
-
-	Raw buf[PF];
-	int rows[PF];
-#pragma unroll
-	for(int u = 0; u < PF; u++) {
-		const int p = p0 + u;
-		const int r = p <= p1 ? __ldg(F.srcrow + (p - F.pmin)) : -1;
-		rows[u] = r;
-		buf[u] = (r >= 0 && active) ? load_raw(F, colbase + (unsigned long long)r * F.in_bpr, bpp) : Raw{0u, 0u};
-	}
-
-	for(int p = p0; p <= p1; p += PF) {
-#pragma unroll
-		for(int u = 0; u < PF; u++) {
-			const int pp = p + u;
-			if(pp > p1) break;
-			const Raw cur = buf[u];
-			const int row = rows[u];
-			{   // refill this slot of the ring with the row PF positions ahead
-				const int pn = pp + PF;
-				const int r = pn <= p1 ? __ldg(F.srcrow + (pn - F.pmin)) : -1;
-				rows[u] = r;
-				buf[u] = (r >= 0 && active) ? load_raw(F, colbase + (unsigned long long)r * F.in_bpr, bpp) : Raw{0u, 0u};
-			}
-			const int q = pp - F.pmin;
-			float val[NPL];
-			if(row >= 0 && active) decode_raw<NPL, DEPTH>(F, s_tab, cur, val);
-			else {
-#pragma unroll
-				for(int c = 0; c < NPL; c++) val[c] = 0.0f;   // transparent edge: value 0
-			}
-			const float4 *w4 = reinterpret_cast<const float4 *>(F.sw + (size_t)q * 8);
-			const float4 wa = __ldg(w4), wb = __ldg(w4 + 1);
-			const float ws[8] = {wa.x, wa.y, wa.z, wa.w, wb.x, wb.y, wb.z, wb.w};
-#pragma unroll
-			for(int s = 0; s < NS; s++)
-#pragma unroll
-				for(int c = 0; c < NPL; c++) acc[s][c] = __fmaf_rn(val[c], ws[s], acc[s][c]);
-			const int2 fin = __ldg(F.pinfo + q);
-			for(int k = 0; k < fin.y; k++) {
-				const int j = fin.x + k;
-				const int sj = j % NS;
-#pragma unroll
-				for(int s = 0; s < NS; s++) {
-					if(s == sj) {
-						if(active && j >= jb && j < je) {
-#pragma unroll
-							for(int c = 0; c < NPL; c++)
-								F.interm[(unsigned long long)c * F.plane + (unsigned long long)j * F.mid_w + x] = acc[s][c];
-						}
-#pragma unroll
-						for(int c = 0; c < NPL; c++) acc[s][c] = 0.0f;
-					}
-				}
-			}
-		}
-	}
+	extern __shared__ __align__(16) float s_tab[];
+	vstream_tile<NS, NPL, DEPTH>(F, s_tab, blockIdx.x, blockIdx.y);
 }
 
-// Exact float of a small unsigned integer (< 2^23) without an I2F: the code
-// is placed in the mantissa of 2^23 and 2^23 is subtracted.
-__device__ __forceinline__ float u2f(unsigned int v)
-{
-	return __fsub_rn(__uint_as_float(0x4b000000u | v), 8388608.0f);
-}
-
-
-// Vertical pass, streaming, PX pixels per thread.  Same scheme as
-// k_vstream, arranged for memory-level parallelism and few instructions
-// per sample:
-//   * each thread reads PX adjacent pixels of a row as one aligned 4/8/16-byte
-//     word group, and keeps PF rows of those loads in flight;
-//   * a row's address is computed from its position (positions map to rows by
-//     clamping, which the host checked for this weight set), so no load waits
-//     on another load;
-//   * the band's schedule (slot weights, rows finished per position) is staged
-//     in shared memory once per block.
 template<int NS, int NCH, bool ALPHA, int DEPTH, int PX>
 __global__ void __launch_bounds__(kVPxThreads) k_vstream_px(FJob F)
 {
-	constexpr int PF = 8;
-	constexpr int BPP = NCH * (DEPTH / 8);
-	constexpr int NW = PX * BPP / 4;              // 32-bit words per thread per row
-	static_assert(PX * BPP % 4 == 0, "thread group must be whole words");
-	extern __shared__ float s_dyn[];
-	float *s_tab = s_dyn;
-	const int jb = blockIdx.y * F.rows_per_band;
-	const int je = min(jb + F.rows_per_band, F.mid_h);
-	if(jb >= je) return;
-	const int p0 = F.first_pos[jb], p1 = F.last_pos[je - 1];
-	const int nq = p1 - p0 + 1;
-	float *s_w = s_dyn + F.dec_tab_floats;         // nq * NS
-	int2 *s_fin = reinterpret_cast<int2 *>(s_w + (size_t)nq * NS);
-	for(int k = threadIdx.x; k < F.dec_tab_floats; k += blockDim.x) s_tab[k] = F.dec_tab[k];
-	for(int k = threadIdx.x; k < nq * NS; k += blockDim.x) {
-		const int q = k / NS, sl = k - q * NS;
-		s_w[k] = F.sw[(size_t)(p0 - F.pmin + q) * 8 + sl];
-	}
-	for(int k = threadIdx.x; k < nq; k += blockDim.x) s_fin[k] = F.pinfo[p0 - F.pmin + k];
-	__syncthreads();
-
-	const int x0 = (blockIdx.x * blockDim.x + threadIdx.x) * PX;
-	if(x0 >= F.mid_w) return;
-	const bool full = x0 + PX <= F.mid_w;
-	const int valid_bytes = (F.mid_w - x0) * BPP;
-	const uint8_t *colbase = F.in + (size_t)(F.crop_x + x0) * BPP + (unsigned long long)F.crop_y * F.in_bpr;
-	const int last_row = F.in_rows - 1;
-	const float ainv = F.alpha_inv;
-
-	float acc[NS][PX][NCH];
-#pragma unroll
-	for(int s = 0; s < NS; s++)
-#pragma unroll
-		for(int px = 0; px < PX; px++)
-#pragma unroll
-			for(int c = 0; c < NCH; c++) acc[s][px][c] = 0.0f;
-
-	auto load_row = [&](int p, uint32_t *w) {
-		const int row = min(max(p, 0), last_row);
-		const uint8_t *a = colbase + (unsigned long long)row * F.in_bpr;
-		if(full) {
-			if(NW % 4 == 0) {
-#pragma unroll
-				for(int k = 0; k < NW; k += 4) {
-					const uint4 v = __ldcs(reinterpret_cast<const uint4 *>(a) + k / 4);
-					w[k] = v.x; w[k + 1] = v.y; w[k + 2] = v.z; w[k + 3] = v.w;
-				}
-			}
-			else if(NW % 2 == 0) {
-#pragma unroll
-				for(int k = 0; k < NW; k += 2) {
-					const uint2 v = __ldcs(reinterpret_cast<const uint2 *>(a) + k / 2);
-					w[k] = v.x; w[k + 1] = v.y;
-				}
-			}
-			else {
-#pragma unroll
-				for(int k = 0; k < NW; k++) w[k] = __ldcs(reinterpret_cast<const unsigned int *>(a) + k);
-			}
-		}
-		else {
-#pragma unroll
-			for(int k = 0; k < NW; k++)
-				w[k] = 4 * k < valid_bytes ? __ldcs(reinterpret_cast<const unsigned int *>(a) + k) : 0u;
-		}
-	};
-
-	uint32_t ring[PF][NW];
-#pragma unroll
-	for(int u = 0; u < PF; u++) {
-		if(p0 + u <= p1) load_row(p0 + u, ring[u]);
-		else {
-#pragma unroll
-			for(int k = 0; k < NW; k++) ring[u][k] = 0u;
-		}
-	}
-
-	for(int p = p0; p <= p1; p += PF) {
-#pragma unroll
-		for(int u = 0; u < PF; u++) {
-			const int pp = p + u;
-			if(pp > p1) break;
-			uint32_t cur[NW];
-#pragma unroll
-			for(int k = 0; k < NW; k++) cur[k] = ring[u][k];
-			if(pp + PF <= p1) load_row(pp + PF, ring[u]);
-			const int q = pp - p0;
-			float val[PX][NCH];
-#pragma unroll
-			for(int px = 0; px < PX; px++) {
-				float a = 1.0f;
-#pragma unroll
-				for(int c = 0; c < NCH; c++) {
-					const int sidx = px * NCH + c;      // sample index within the group
-					unsigned int code;
-					if(DEPTH == 8) code = __byte_perm(cur[sidx >> 2], 0u, 0x4440u + (sidx & 3));
-					else code = __byte_perm(cur[sidx >> 1], 0u, (sidx & 1) ? 0x4423u : 0x4401u);
-					if(ALPHA && c == NCH - 1) {
-						a = __fmul_rn(u2f(code), ainv);
-						val[px][c] = a;
-					}
-					else val[px][c] = dec_table<DEPTH>(s_tab, code);
-				}
-				if(ALPHA) {
-#pragma unroll
-					for(int c = 0; c < NCH - 1; c++) val[px][c] = __fmul_rn(val[px][c], a);
-				}
-			}
-			float ws[NS];
-			if(NS == 4) {
-				const float4 w4 = reinterpret_cast<const float4 *>(s_w)[q];
-				ws[0] = w4.x; ws[1] = w4.y; ws[2] = w4.z; ws[3] = w4.w;
-			}
-			else {
-#pragma unroll
-				for(int s = 0; s < NS; s += 2) {
-					const float2 w2 = reinterpret_cast<const float2 *>(s_w)[(q * NS + s) / 2];
-					ws[s] = w2.x; ws[s + 1] = w2.y;
-				}
-			}
-#pragma unroll
-			for(int s = 0; s < NS; s++)
-#pragma unroll
-				for(int px = 0; px < PX; px++)
-#pragma unroll
-					for(int c = 0; c < NCH; c++) acc[s][px][c] = __fmaf_rn(val[px][c], ws[s], acc[s][px][c]);
-			const int2 fin = s_fin[q];
-			for(int k = 0; k < fin.y; k++) {
-				const int j = fin.x + k;
-				const int sj = j % NS;
-				const bool keep = j >= jb && j < je;
-#pragma unroll
-				for(int s = 0; s < NS; s++) {
-					if(s == sj) {
-						if(keep) {
-							float *o = F.interm + (unsigned long long)j * F.mid_w + x0;
-#pragma unroll
-							for(int px = 0; px < PX; px++) {
-								if(full || x0 + px < F.mid_w) {
-#pragma unroll
-									for(int c = 0; c < NCH; c++) o[(unsigned long long)c * F.plane + px] = acc[s][px][c];
-								}
-							}
-						}
-#pragma unroll
-						for(int px = 0; px < PX; px++)
-#pragma unroll
-							for(int c = 0; c < NCH; c++) acc[s][px][c] = 0.0f;
-					}
-				}
-			}
-		}
-	}
+	extern __shared__ __align__(16) float s_dyn[];
+	vstream_px_tile<NS, NCH, ALPHA, DEPTH, PX>(F, s_dyn, blockIdx.x, blockIdx.y);
 }
 
-// vertical pass, gather (upsampling or wide windows): one thread per (x, j).
 template<int NPL, int DEPTH>
 __global__ void __launch_bounds__(kVThreads) k_vgather(FJob F)
 {
-	extern __shared__ float s_tab[];
-	for(int k = threadIdx.x; k < F.dec_tab_floats; k += blockDim.x) s_tab[k] = F.dec_tab[k];
-	__syncthreads();
-	const int x = blockIdx.x * blockDim.x + threadIdx.x;
-	const int j = blockIdx.y;
-	if(x >= F.mid_w || j >= F.mid_h) return;
-	const int bpp = F.nphys * (DEPTH / 8);
-	const uint8_t *colbase = F.in + (size_t)(F.crop_x + x) * bpp;
-	float acc[NPL];
-#pragma unroll
-	for(int c = 0; c < NPL; c++) acc[c] = 0.0f;
-	for(int t = F.voff[j]; t < F.voff[j + 1]; t++) {
-		int row = F.vsrc[t];
-		if(row < 0) continue;   // transparent edge contributes 0
-		float val[NPL];
-		decode_pixel<NPL, DEPTH>(F, s_tab, colbase + (unsigned long long)(F.crop_y + row) * F.in_bpr, val);
-		float w = F.vw[t];
-#pragma unroll
-		for(int c = 0; c < NPL; c++) acc[c] = __fmaf_rn(val[c], w, acc[c]);
-	}
-#pragma unroll
-	for(int c = 0; c < NPL; c++) F.interm[(unsigned long long)c * F.plane + (unsigned long long)j * F.mid_w + x] = acc[c];
-}
-
-// ---------------------------------------------------------------------------
-// horizontal pass + guarded quantisation
-// ---------------------------------------------------------------------------
-
-__device__ __forceinline__ int count_le_f(const float *t, int n, float v)
-{
-	int lo = 0, hi = n;
-	while(lo < hi) {
-		int mid = (lo + hi) >> 1;
-		if(t[mid] <= v) lo = mid + 1; else hi = mid;
-	}
-	return lo;
-}
-
-// Decides the output code for every value in [v - E, v + E]; returns -1 if
-// the interval straddles a decision of the reference.
-__device__ __forceinline__ int quantize_guarded(const FTail &T, float v, float E, int x, int y)
-{
-	v = fminf(fmaxf(v, 0.0f), 1.0f);
-	// slack for float rounding of the tables and of this arithmetic
-	const float Ep = __fmaf_rn(E, 1.0000001f, __fmaf_rn(fabsf(v), 2.4e-7f, 1e-37f));
-	const float lo_v = __fsub_rn(v, Ep), hi_v = __fadd_rn(v, Ep);
-	if(T.use_nc) {
-		int c = count_le_f(T.nc, 255, v);
-		if(c > 0 && !(T.nc[c - 1] < lo_v)) return -1;
-		if(c < 255 && !(T.nc[c] > hi_v)) return -1;
-		return c;
-	}
-	int k = count_le_f(T.U + 1, T.P, v);
-	bool near_lo = k > 0 && !(T.U[k] < lo_v);          // v within E of the bracket's lower edge
-	bool near_hi = k < T.P && !(T.U[k + 1] > hi_v);    // ... or of the next bracket
-	if(near_lo || near_hi) {
-		// With all codes available, the code at a bracket edge U[k] is k from
-		// both sides (the fraction is ~0 above it and ~1 below it), provided
-		// the uncertainty is far smaller than the distance to the thresholds.
-		if(T.cc != 0 || (near_lo && near_hi)) return -1;
-		int kk = near_lo ? k : k + 1;
-		// distance to the neighbouring codes on both sides of code kk
-		float step = fminf(__fsub_rn(T.rev[kk], T.rev[kk - 1]), kk < T.M ? __fsub_rn(T.rev[kk + 1], T.rev[kk]) : 1.0f);
-		if(!(__fmul_rn(Ep, 512.0f) < step)) return -1;
-		return T.code[kk];
-	}
-	const int lo = T.code[k], hi = T.code[k + 1];
-	if(k == T.P) return lo;
-	const float a = T.rev[lo], b = T.rev[hi];
-	const float den = __fsub_rn(b, a);
-	const float f = __fdiv_rn(__fsub_rn(v, a), den);
-	const float mf = __fdiv_rn(__fmaf_rn(fabsf(a) + fabsf(b), 1.2e-7f, Ep), den) + 1e-6f;
-	float thr = 0.5f;
-	if(T.dfam == IW_DITHERFAMILY_ORDERED) thr = ((float)dither_rank(T.dsub, x, y) + 0.5f) * 0.015625f;
-	int decided;
-	if(f >= thr + mf) decided = hi;
-	else if(f < thr - mf) decided = lo;
-	else return -1;
-	// inside the exactly-representable region the reference always picks lo
-	if(decided != lo && !(T.X[k] <= lo_v)) return -1;
-	return decided;
-}
-
-__device__ __forceinline__ void store_code_f(const FJob &F, int ch, int x, int y, unsigned int code)
-{
-	uint8_t *row = F.out + (unsigned long long)y * F.out_bpr;
-	if(F.out_depth == 8) row[F.out_n * x + ch] = (uint8_t)code;
-	else {
-		uint8_t *p = row + (size_t)(F.out_n * x + ch) * 2;
-		p[0] = (uint8_t)(code >> 8);
-		p[1] = (uint8_t)(code & 0xff);
-	}
+	extern __shared__ __align__(16) float s_tab[];
+	vgather_tile<NPL, DEPTH>(F, s_tab, blockIdx.x, blockIdx.y);
 }
 
 template<int NPL>
 __global__ void __launch_bounds__(kHThreads) k_hpass_fast(FJob F)
 {
-	const int i = blockIdx.x * blockDim.x + threadIdx.x;
-	const int j = blockIdx.y;
-	if(i >= F.out_w || j >= F.out_h) return;
-	float v[NPL], T[NPL];
-#pragma unroll
-	for(int c = 0; c < NPL; c++) { v[c] = 0.0f; T[c] = 0.0f; }
-	const int t0 = F.hoff[i], t1 = F.hoff[i + 1];
-	for(int t = t0; t < t1; t++) {
-		const int src = __ldg(F.hsrc + t);
-		if(src < 0) continue;   // transparent edge: value 0
-		const float w = __ldg(F.hw + t), aw = fabsf(w);
-#pragma unroll
-		for(int c = 0; c < NPL; c++) {
-			const float I = __ldg(F.interm + (unsigned long long)c * F.plane + (unsigned long long)j * F.mid_w + src);
-			v[c] = __fmaf_rn(I, w, v[c]);
-			T[c] = __fmaf_rn(fabsf(I), aw, T[c]);
-		}
-	}
-	float E[NPL];
-#pragma unroll
-	for(int c = 0; c < NPL; c++) E[c] = __fmaf_rn(F.K1[c], T[c], F.K0[c]);
-
-	// Decide every sample; 'redo' collects the intermediate channels that
-	// must be re-evaluated exactly.  An undecided colour sample needs its own
-	// channel and the exact alpha (the reference divides by the float alpha);
-	// an undecided alpha makes blackening undecided, so the whole pixel is redone.
-	// codes are kept per processing slot k (registers); out_of maps k to the channel
-	int codes[dev::kMaxCh];
-	int alpha_code = -1;
-	unsigned int redo = 0;
-	const unsigned int all = (1u << F.mid_n) - 1u;
-	float A = 0.0f, EA = 0.0f;
-#pragma unroll
-	for(int k = 0; k < dev::kMaxCh; k++) {
-		codes[k] = -1;
-		if(k >= F.mid_n || redo == all) continue;
-		const int pl = F.k_plane[k];
-		float val = 0.0f, err = 0.0f;
-#pragma unroll
-		for(int c = 0; c < NPL; c++) if(c == pl) { val = v[c]; err = E[c]; }
-		const int oc = F.k_out[k];
-		const bool is_alpha = F.k_alpha[k];
-		if(is_alpha) {
-			A = val;
-			// the reference divides by the float-rounded alpha: widen by one rounding
-			EA = __fmaf_rn(fabsf(val) + err, 6.0e-8f, err);
-		}
-		else if(F.k_unassoc[k]) {
-			if(alpha_code == 0 && F.blacken) { codes[k] = 0; continue; }
-			const float den = __fsub_rn(A, EA);
-			if(!(den > 0.0f)) { redo |= F.k_bit[k] | F.k_bit[0]; continue; }
-			const float q = __fdiv_rn(val, A);
-			err = __fdiv_rn(__fmaf_rn(fabsf(q), EA, err), den);
-			err = __fmaf_rn(fabsf(q), 1.2e-7f, err);
-			val = q;
-		}
-		const int c = quantize_guarded(F.tail[oc], val, err, i, j);
-		if(c < 0) {
-			if(is_alpha) redo = all;
-			else redo |= F.k_bit[k] | (F.k_unassoc[k] ? F.k_bit[0] : 0u);
-			continue;
-		}
-		if(is_alpha) alpha_code = c;
-		codes[k] = c;
-	}
-	if(redo) {
-		const int slot = atomicAdd(F.flag_count, 1);
-		F.flag_list[2 * slot] = j * F.out_w + i;
-		F.flag_list[2 * slot + 1] = (int)redo;
-		if(redo == all) return;
-	}
-#pragma unroll
-	for(int k = 0; k < dev::kMaxCh; k++) {
-		if(k >= F.mid_n) continue;
-		if(redo & F.k_bit[k]) continue;
-		int c = codes[k];
-		if(!F.k_alpha[k]) {
-			if(F.negate) c = F.k_maxcc[k] - c;
-			if(F.blacken && alpha_code == 0) c = 0;
-		}
-		store_code_f(F, F.k_out[k], i, j, (unsigned int)c);
-	}
+	hpass_pixel<NPL>(F, blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y);
 }
 
 // ---------------------------------------------------------------------------
@@ -840,14 +254,7 @@ bool fast_eligible(const Plan &P, const Job &J, FastInfo &fi)
 	return true;
 }
 
-struct FastState {
-	FJob F;
-	Job J;
-	const void *vkernel = nullptr, *hkernel = nullptr;
-	dim3 vgrid, hgrid;
-	int vthreads = kVThreads;
-	size_t vsmem = 0;
-};
+
 
 void fast_launch_impl(cudaStream_t st, void *state, void (*mark)(void *), void *markarg)
 {
@@ -869,10 +276,11 @@ void fast_release(FastInfo &fi)
 	fi.state = nullptr;
 }
 
-bool fast_prepare(cudaStream_t st, const Plan &P, Job &J, FastInfo &fi, std::string &err)
+// Host preparation of one image: job layout, error model, per-image arrays
+// (in FastState::blob, placed later) and kernel choice.  'batch' picks
+// taller vertical tiles (many images fill the GPU).  Caller holds the cache lock.
+static FastState *fast_build(const Plan &P, const Job &J, bool batch, std::string &err)
 {
-	Cache &C = cache();
-	std::lock_guard<std::mutex> lk(C.mu);
 	FJob F;
 	memset(&F, 0, sizeof(F));
 	const Weights &WV = *P.wsets[1][0], &WH = *P.wsets[0][0];
@@ -924,7 +332,7 @@ bool fast_prepare(cudaStream_t st, const Plan &P, Job &J, FastInfo &fi, std::str
 		});
 		e_dec = dec_err[std::make_pair((const void *)coltab.get(), P.in_depth)];
 		dec_floats = P.in_depth == 8 ? 256 : 8192;
-		if(!dec_tab) { err = "Out of GPU memory (fast tables)"; return false; }
+		if(!dec_tab) { err = "Out of GPU memory (fast tables)"; return nullptr; }
 	}
 	e_dec = std::max(e_dec, 2.0 * u);   // code*inv: 1/maxcc rounded, product rounded
 	F.dec_tab = dec_tab;
@@ -1002,32 +410,7 @@ bool fast_prepare(cudaStream_t st, const Plan &P, Job &J, FastInfo &fi, std::str
 		o_pi = add(S.pinfo.data(), S.pinfo.size() * 4);
 		o_sw = add(S.sw.data(), S.sw.size() * 4);
 	}
-	const size_t flag_bytes = 256 + (size_t)J.out_w * J.out_h * 8;
-	size_t need = blob.size() + 256 + flag_bytes + 256 + sizeof(FTail) * dev::kMaxCh;
-	if(need > C.scratch_cap) {
-		if(C.scratch) cudaFree(C.scratch);
-		C.scratch = nullptr;
-		C.scratch_cap = 0;
-		if(cudaMalloc(&C.scratch, need + need / 8) != cudaSuccess) { err = "Out of GPU memory (fast form)"; return false; }
-		C.scratch_cap = need + need / 8;
-	}
-	uint8_t *base = (uint8_t *)C.scratch;
-	cudaMemcpyAsync(base, blob.data(), blob.size(), cudaMemcpyHostToDevice, st);
-	size_t flag_off = (blob.size() + 255) & ~(size_t)255;
-	F.flag_count = (int *)(base + flag_off);
-	F.flag_list = (int *)(base + flag_off + 256);
-	F.hoff = (const int *)(base + o_hoff);
-	F.hsrc = (const int *)(base + o_hsrc);
-	F.hw = (const float *)(base + o_hw);
-	F.voff = (const int *)(base + o_voff);
-	F.vsrc = (const int *)(base + o_vsrc);
-	F.vw = (const float *)(base + o_vw);
 	if(S.ok) {
-		F.first_pos = (const int *)(base + o_fp);
-		F.last_pos = (const int *)(base + o_lp);
-		F.srcrow = (const int *)(base + o_src);
-		F.pinfo = (const int2 *)(base + o_pi);
-		F.sw = (const float *)(base + o_sw);
 		F.pmin = S.pmin;
 		F.npos = S.npos;
 		F.ns = S.ns;
@@ -1045,13 +428,9 @@ bool fast_prepare(cudaStream_t st, const Plan &P, Job &J, FastInfo &fi, std::str
 		T.code = dev_table(q.code);
 		T.rev = dev_derived(q.rev, 1, as_float);
 		T.nc = q.use_nc ? dev_derived(q.nc, 1, as_float) : nullptr;
-		if(!T.U || !T.X || !T.code || !T.rev || (q.use_nc && !T.nc)) { err = "Out of GPU memory (fast tables)"; return false; }
+		if(!T.U || !T.X || !T.code || !T.rev || (q.use_nc && !T.nc)) { err = "Out of GPU memory (fast tables)"; return nullptr; }
 	}
-	{
-		const size_t tail_off = (flag_off + 256 + flag_bytes + 255) & ~(size_t)255;
-		cudaMemcpyAsync(base + tail_off, tails, sizeof(tails), cudaMemcpyHostToDevice, st);
-		F.tail = (const FTail *)(base + tail_off);
-	}
+	for(int k = 0; k < P.mid_n; k++) F.k_tail[k] = tails[F.k_out[k] >= 0 ? F.k_out[k] : 0];
 
 	// ---- kernel selection
 	auto *FS = new FastState();
@@ -1060,14 +439,18 @@ bool fast_prepare(cudaStream_t st, const Plan &P, Job &J, FastInfo &fi, std::str
 	FS->vgrid = dim3(gx, F.mid_h);
 #define IWG_VSTREAM(NS_, NPL_, D_) \
 	if(!FS->vkernel && S.ns == NS_ && nplanes == NPL_ && P.in_depth == D_) { \
-		int bands = std::max(1, std::min(F.mid_h, (4 * 152 + gx - 1) / gx)); \
+		int bands = std::max(1, std::min(F.mid_h, batch ? (F.mid_h + 47) / 48 : (4 * 152 + gx - 1) / gx)); \
 		F.rows_per_band = (F.mid_h + bands - 1) / bands; \
 		bands = (F.mid_h + F.rows_per_band - 1) / F.rows_per_band; \
 		FS->vkernel = (const void *)k_vstream<NS_, NPL_, D_>; \
 		FS->vgrid = dim3(gx, bands); \
+		FS->vv.kind = 2; FS->vv.ns = NS_; FS->vv.nch = NPL_; FS->vv.depth = D_; \
 	}
 #define IWG_VGATHER(NPL_, D_) \
-	if(!FS->vkernel && nplanes == NPL_ && P.in_depth == D_) FS->vkernel = (const void *)k_vgather<NPL_, D_>;
+	if(!FS->vkernel && nplanes == NPL_ && P.in_depth == D_) { \
+		FS->vkernel = (const void *)k_vgather<NPL_, D_>; \
+		FS->vv.kind = 3; FS->vv.nch = NPL_; FS->vv.depth = D_; \
+	}
 	// identity layout: plane c reads input channel c, the last one alpha when present
 	bool ident = S.ok && nplanes == P.in_nphys && dec_tab != nullptr;
 	for(int q = 0; q < nplanes && ident; q++) {
@@ -1088,7 +471,7 @@ bool fast_prepare(cudaStream_t st, const Plan &P, Job &J, FastInfo &fi, std::str
 		if(v_base % va_ == 0 && P.in_bpr % va_ == 0) { \
 			const int threads_ = (F.mid_w + PX_ - 1) / PX_; \
 			const int gxp_ = (threads_ + kVPxThreads - 1) / kVPxThreads; \
-			int bands = std::max(1, std::min(F.mid_h, (5 * 152 + gxp_ / 2) / gxp_)); \
+			int bands = std::max(1, std::min(F.mid_h, batch ? (F.mid_h + 47) / 48 : (5 * 152 + gxp_ / 2) / gxp_)); \
 			F.rows_per_band = (F.mid_h + bands - 1) / bands; \
 			bands = (F.mid_h + F.rows_per_band - 1) / F.rows_per_band; \
 			int nq_max = 0; \
@@ -1104,33 +487,19 @@ bool fast_prepare(cudaStream_t st, const Plan &P, Job &J, FastInfo &fi, std::str
 				FS->vgrid = dim3(gxp_, bands); \
 				FS->vthreads = kVPxThreads; \
 				FS->vsmem = sm_; \
+				FS->vv.kind = 1; FS->vv.ns = NS_; FS->vv.nch = NCH_; FS->vv.alpha = A_; FS->vv.depth = D_; FS->vv.px = PX_; \
 			} \
 		} \
 	}
-	{
-		IWG_VPX(4, 4, true, 16, 2) IWG_VPX(6, 4, true, 16, 2) IWG_VPX(8, 4, true, 16, 2)
-		IWG_VPX(4, 3, false, 16, 2) IWG_VPX(6, 3, false, 16, 2) IWG_VPX(8, 3, false, 16, 2)
-		IWG_VPX(4, 2, true, 16, 4) IWG_VPX(6, 2, true, 16, 4) IWG_VPX(8, 2, true, 16, 4)
-		IWG_VPX(4, 1, false, 16, 8) IWG_VPX(6, 1, false, 16, 8) IWG_VPX(8, 1, false, 16, 8)
-		IWG_VPX(4, 4, true, 8, 2) IWG_VPX(6, 4, true, 8, 2) IWG_VPX(8, 4, true, 8, 2)
-		IWG_VPX(4, 3, false, 8, 4)
-		IWG_VPX(4, 2, true, 8, 4) IWG_VPX(6, 2, true, 8, 4) IWG_VPX(8, 2, true, 8, 4)
-		IWG_VPX(4, 1, false, 8, 8) IWG_VPX(6, 1, false, 8, 8) IWG_VPX(8, 1, false, 8, 8)
-	}
+	IWG_VPX_VARIANTS(IWG_VPX)
 #undef IWG_VPX
 	if(S.ok) {
-		IWG_VSTREAM(4, 1, 8) IWG_VSTREAM(4, 2, 8) IWG_VSTREAM(4, 3, 8) IWG_VSTREAM(4, 4, 8)
-		IWG_VSTREAM(6, 1, 8) IWG_VSTREAM(6, 2, 8) IWG_VSTREAM(6, 3, 8) IWG_VSTREAM(6, 4, 8)
-		IWG_VSTREAM(8, 1, 8) IWG_VSTREAM(8, 2, 8) IWG_VSTREAM(8, 3, 8) IWG_VSTREAM(8, 4, 8)
-		IWG_VSTREAM(4, 1, 16) IWG_VSTREAM(4, 2, 16) IWG_VSTREAM(4, 3, 16) IWG_VSTREAM(4, 4, 16)
-		IWG_VSTREAM(6, 1, 16) IWG_VSTREAM(6, 2, 16) IWG_VSTREAM(6, 3, 16) IWG_VSTREAM(6, 4, 16)
-		IWG_VSTREAM(8, 1, 16) IWG_VSTREAM(8, 2, 16) IWG_VSTREAM(8, 3, 16) IWG_VSTREAM(8, 4, 16)
+		IWG_VSTREAM_VARIANTS(IWG_VSTREAM)
 	}
-	IWG_VGATHER(1, 8) IWG_VGATHER(2, 8) IWG_VGATHER(3, 8) IWG_VGATHER(4, 8)
-	IWG_VGATHER(1, 16) IWG_VGATHER(2, 16) IWG_VGATHER(3, 16) IWG_VGATHER(4, 16)
+	IWG_VGATHER_VARIANTS(IWG_VGATHER)
 #undef IWG_VSTREAM
 #undef IWG_VGATHER
-	if(!FS->vkernel) { delete FS; err = "fast form: no kernel for this layout"; return false; }
+	if(!FS->vkernel) { delete FS; err = "fast form: no kernel for this layout"; return nullptr; }
 	switch(nplanes) {
 	case 1: FS->hkernel = (const void *)k_hpass_fast<1>; break;
 	case 2: FS->hkernel = (const void *)k_hpass_fast<2>; break;
@@ -1138,15 +507,93 @@ bool fast_prepare(cudaStream_t st, const Plan &P, Job &J, FastInfo &fi, std::str
 	default: FS->hkernel = (const void *)k_hpass_fast<4>; break;
 	}
 	FS->hgrid = dim3((F.out_w + kHThreads - 1) / kHThreads, F.out_h);
+	F.vgx = (int)FS->vgrid.x;
+	F.vgy = (int)FS->vgrid.y;
+	F.hgx = (int)FS->hgrid.x;
 	FS->F = F;
 	FS->J = J;
+	FS->blob = std::move(blob);
+	FS->o_hoff = o_hoff; FS->o_hsrc = o_hsrc; FS->o_hw = o_hw;
+	FS->o_voff = o_voff; FS->o_vsrc = o_vsrc; FS->o_vw = o_vw;
+	FS->o_fp = o_fp; FS->o_lp = o_lp; FS->o_src = o_src; FS->o_pi = o_pi; FS->o_sw = o_sw;
+	FS->streaming = S.ok;
+	FS->flag_entries = (size_t)F.out_w * F.out_h;
+	return FS;
+}
+
+// Points the image's per-image arrays at 'base' (a device copy of its blob)
+// and its flags at the given counter and list.
+static void fast_place(FastState *FS, const uint8_t *base, int *flag_count, int *flag_list, int img)
+{
+	FJob &F = FS->F;
+	F.flag_count = flag_count;
+	F.flag_list = flag_list;
+	F.img = img;
+	F.hoff = (const int *)(base + FS->o_hoff);
+	F.hsrc = (const int *)(base + FS->o_hsrc);
+	F.hw = (const float *)(base + FS->o_hw);
+	F.voff = (const int *)(base + FS->o_voff);
+	F.vsrc = (const int *)(base + FS->o_vsrc);
+	F.vw = (const float *)(base + FS->o_vw);
+	if(FS->streaming) {
+		F.first_pos = (const int *)(base + FS->o_fp);
+		F.last_pos = (const int *)(base + FS->o_lp);
+		F.srcrow = (const int *)(base + FS->o_src);
+		F.pinfo = (const int2 *)(base + FS->o_pi);
+		F.sw = (const float *)(base + FS->o_sw);
+	}
+}
+
+bool fast_prepare(cudaStream_t st, const Plan &P, Job &J, FastInfo &fi, std::string &err)
+{
+	Cache &C = cache();
+	std::lock_guard<std::mutex> lk(C.mu);
+	FastState *FS = fast_build(P, J, false, err);
+	if(!FS) return false;
+	const size_t flag_off = (FS->blob.size() + 255) & ~(size_t)255;
+	const size_t need = flag_off + 256 + FS->flag_entries * 16;
+	if(need > C.scratch_cap) {
+		if(C.scratch) cudaFree(C.scratch);
+		C.scratch = nullptr;
+		C.scratch_cap = 0;
+		if(cudaMalloc(&C.scratch, need + need / 8) != cudaSuccess) {
+			delete FS;
+			err = "Out of GPU memory (fast form)";
+			return false;
+		}
+		C.scratch_cap = need + need / 8;
+	}
+	uint8_t *base = (uint8_t *)C.scratch;
+	cudaMemcpyAsync(base, FS->blob.data(), FS->blob.size(), cudaMemcpyHostToDevice, st);
+	fast_place(FS, base, (int *)(base + flag_off), (int *)(base + flag_off + 256), 0);
 	fi.state = FS;
 	fi.launches = 3;
 	fi.launch_fn = fast_launch_impl;
-	fi.streaming = S.ok;
-	fi.slots = S.ns;
-	fi.flag_count_dev = F.flag_count;
+	fi.streaming = FS->streaming;
+	fi.slots = FS->F.ns;
+	fi.flag_count_dev = FS->F.flag_count;
 	return true;
 }
+
+// ---- batch support (see fastpath.cuh) ----
+
+void *fast_batch_item(const Plan &P, const Job &J, std::string &err)
+{
+	Cache &C = cache();
+	std::lock_guard<std::mutex> lk(C.mu);
+	return fast_build(P, J, true, err);
+}
+
+size_t fast_item_blob_bytes(const void *item) { return static_cast<const FastState *>(item)->blob.size(); }
+const void *fast_item_blob(const void *item) { return static_cast<const FastState *>(item)->blob.data(); }
+size_t fast_item_flag_entries(const void *item) { return static_cast<const FastState *>(item)->flag_entries; }
+int fast_item_htaps(const void *item) { return static_cast<const FastState *>(item)->J.wh[0].max_taps; }
+
+void fast_item_place(void *item, const uint8_t *dev_blob, int *flag_count, int *flag_list, int img)
+{
+	fast_place(static_cast<FastState *>(item), dev_blob, flag_count, flag_list, img);
+}
+
+void fast_item_free(void *item) { delete static_cast<FastState *>(item); }
 
 }  // namespace iwg

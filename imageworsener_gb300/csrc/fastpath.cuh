@@ -38,4 +38,20 @@ int fast_launch(cudaStream_t st, FastInfo &fi, Mark mark)
 // Frees the prepared state.
 void fast_release(FastInfo &fi);
 
+// ---- batch: many images in a few launches ----
+// Host preparation of one image (no device work); null with 'err' if the
+// image cannot run in the fast form.  J's device pointers (input, output,
+// intermediate) must already be final.
+void *fast_batch_item(const Plan &P, const dev::Job &J, std::string &err);
+size_t fast_item_blob_bytes(const void *item);     // per-image arrays, to copy to the device as one block
+const void *fast_item_blob(const void *item);
+size_t fast_item_flag_entries(const void *item);   // flag list capacity the image needs
+int fast_item_htaps(const void *item);             // widest horizontal window
+// Points the image at its device copy of the blob and the shared flag list.
+void fast_item_place(void *item, const uint8_t *dev_blob, int *flag_count, int *flag_list, int img);
+// Launches the vertical and horizontal passes of n placed images, one launch
+// per kernel variant (fastbatch.cu).  Returns the number of launches, -1 on error.
+int fast_launch_batch(cudaStream_t st, void *const *items, int n, std::string &err);
+void fast_item_free(void *item);
+
 }  // namespace iwg

@@ -267,6 +267,9 @@ void optimize(iw_context *ctx);
 
 // pipeline.cu
 bool run_pipeline(iw_context *ctx, Plan &P, int warmup = 0, int iters = 1);
+// Runs the fast-form images of a batch together (pipeline.cu); see there.
+bool run_batch(const std::vector<iw_context *> &ctxs, const std::vector<Plan *> &plans, std::vector<int> &status,
+	double &dev_ms);
 
 // api.cpp
 const char *get_option(iw_context *ctx, const char *name);

@@ -190,8 +190,11 @@ __global__ void k_hpass_exact(Job J)
 
 // Serial scan for error-diffusion and random dither of one output channel
 // (src/imagew-main.c:487-567, :1072-1136).  The reference visits samples in a
-// fixed order (serpentine rows for error diffusion) and each decision depends
-// on the previous ones, so one thread walks the whole channel.
+// fixed order and each decision depends on the previous ones.  Error
+// diffusion runs serpentine: a right-to-left row starts where the row above
+// ended, so it needs that whole row's errors and rows cannot overlap in a
+// wavefront.  One thread walks the whole channel; channels are independent
+// and run in separate warps of one launch.
 __device__ unsigned int prng_next(unsigned int &mult, unsigned int &carry)
 {
 	unsigned long long x = 0xfff0bf23ULL * mult + carry;
@@ -200,9 +203,8 @@ __device__ unsigned int prng_next(unsigned int &mult, unsigned int &carry)
 	return mult;
 }
 
-__global__ void k_scan(Job J, int oc)
+__device__ void scan_channel(const Job &J, int oc)
 {
-	if(threadIdx.x != 0) return;
 	const DOut &o = J.outc[oc];
 	const DQuant &q = o.q;
 	const int W = J.out_w;
@@ -294,6 +296,15 @@ __global__ void k_scan(Job J, int oc)
 	}
 }
 
+// One warp per output channel; lane 0 of the warp of each scanned channel
+// walks it.
+__global__ void k_scan(Job J)
+{
+	const int oc = threadIdx.x >> 5;
+	if((threadIdx.x & 31) != 0 || oc >= J.out_n || !J.outc[oc].scan) return;
+	scan_channel(J, oc);
+}
+
 // Negation and blackening of fully transparent pixels, for outputs whose
 // channels were (partly) quantised by the serial scan.
 __global__ void k_finalize(Job J)
@@ -328,16 +339,18 @@ __device__ __forceinline__ int nth_bit(unsigned int mask, int r)
 // finishes intermediate channel m -- its horizontal sum, unassociation and
 // quantisation -- with the alpha value and alpha code passed between lanes.
 // The result equals pixel_exact()'s.  Scratch: 'maxt' floats per channel per warp.
-__global__ void k_fix_flagged_warp(Job J, const int *count, const int *list, int maxt)
+template<bool BATCH>
+__global__ void k_fix_flagged_warp(Job J1, const Job *jobs, const int *count, const int *list, int maxt)
 {
 	extern __shared__ float fix_cache[];
 	const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, wpb = blockDim.x >> 5;
 	float *my = fix_cache + (size_t)wib * dev::kMaxCh * maxt;
 	const int n = *count;
-	const unsigned int all = (1u << J.mid_n) - 1u;
 	for(int f = blockIdx.x * wpb + wib; f < n; f += gridDim.x * wpb) {
-		const int p = list[2 * f];
-		const unsigned int mask = (unsigned int)list[2 * f + 1] & all;
+		const int4 e = reinterpret_cast<const int4 *>(list)[f];
+		const Job &J = BATCH ? jobs[e.z] : J1;
+		const int p = e.x;
+		const unsigned int mask = (unsigned int)e.y & ((1u << J.mid_n) - 1u);
 		const int i = p % J.out_w, j = p / J.out_w;
 		const int ntask = __popc(mask) * maxt;
 		for(int k = lane; k < ntask; k += 32) {
@@ -389,14 +402,17 @@ __global__ void k_fix_flagged_warp(Job J, const int *count, const int *list, int
 }
 
 // Fallback for very wide horizontal windows: one thread per flagged pixel.
-__global__ void k_fix_flagged_thread(Job J, const int *count, const int *list)
+template<bool BATCH>
+__global__ void k_fix_flagged_thread(Job J1, const Job *jobs, const int *count, const int *list)
 {
 	const int n = *count;
 	for(int f = blockIdx.x * blockDim.x + threadIdx.x; f < n; f += gridDim.x * blockDim.x) {
-		const int p = list[2 * f];
+		const int4 e = reinterpret_cast<const int4 *>(list)[f];
+		const Job &J = BATCH ? jobs[e.z] : J1;
+		const int p = e.x;
 		const int j = p / J.out_w;
 		pixel_exact(J, p % J.out_w, j, true, [&](int m, int, int x) { return interm_exact<true>(J, m, x, j); },
-			(unsigned int)list[2 * f + 1]);
+			(unsigned int)e.y);
 	}
 }
 
@@ -410,8 +426,21 @@ void launch_fix_flagged(cudaStream_t st, const Job &J, const int *count, const i
 	while(wpb > 1 && per_warp * wpb > 48 * 1024) wpb >>= 1;
 	// Flagged pixels are independent and each is a latency-bound FP64 chain:
 	// launch enough warps to take them all at once (idle warps exit at once).
-	if(per_warp * wpb <= 48 * 1024) k_fix_flagged_warp<<<24 * 152, 32 * wpb, per_warp * wpb, st>>>(J, count, list, maxt);
-	else k_fix_flagged_thread<<<24 * 152, 64, 0, st>>>(J, count, list);
+	if(per_warp * wpb <= 48 * 1024) k_fix_flagged_warp<false><<<24 * 152, 32 * wpb, per_warp * wpb, st>>>(J, nullptr, count, list, maxt);
+	else k_fix_flagged_thread<false><<<24 * 152, 64, 0, st>>>(J, nullptr, count, list);
+}
+
+// The same for a batch: flag entries name their image in 'jobs' (device
+// memory); maxt is the widest horizontal window of any image.
+void launch_fix_flagged_batch(cudaStream_t st, const Job *jobs, int maxt, const int *count, const int *list)
+{
+	const size_t per_warp = (size_t)dev::kMaxCh * maxt * sizeof(float);
+	int wpb = 4;
+	while(wpb > 1 && per_warp * wpb > 48 * 1024) wpb >>= 1;
+	Job none;
+	memset(&none, 0, sizeof(none));
+	if(per_warp * wpb <= 48 * 1024) k_fix_flagged_warp<true><<<24 * 152, 32 * wpb, per_warp * wpb, st>>>(none, jobs, count, list, maxt);
+	else k_fix_flagged_thread<true><<<24 * 152, 64, 0, st>>>(none, jobs, count, list);
 }
 
 // ===========================================================================
@@ -446,6 +475,7 @@ struct DeviceState {
 	int pageable = 0;          // kernels may access pageable host memory (Grace: NVLink-C2C + ATS)
 	cudaStream_t stream = nullptr;
 	DevBuf in, interm, out, scan, err, params, flags;
+	DevBuf batch_io, batch_tab;   // batches: buffers + tables of all images
 	std::map<const void *, std::pair<std::shared_ptr<const void>, void *>> table_cache;
 	std::vector<uint8_t> staging;
 };
@@ -510,25 +540,13 @@ struct Fixup { size_t off; const void **slot; };
 template<class Mark>
 int plain_launch(cudaStream_t st, const Plan &P, const Job &J, Mark mark);
 
-bool run_pipeline(iw_context *ctx, Plan &P, int warmup, int iters)
+// Fills the device job description of a planned image: geometry, flags and
+// the tables (weights packed into 'pk' with fix-ups for their device
+// addresses; decode and quantisation tables from the device table cache).
+// Buffers (input, intermediate, output, dither scratch) are left to the caller.
+static bool make_job(iw_context *ctx, const Plan &P, DeviceState &S, Packer &pk, std::vector<Fixup> &fix, Job &J)
 {
-	DeviceState &S = state();
-	std::lock_guard<std::mutex> lk(S.mu);
-	std::string err;
-	if(!ensure_init(S, err)) {
-		iw_set_error(ctx, err.c_str());
-		return false;
-	}
-
-	// host output image, owned by the context
-	ctx->img2.bpr = P.out_bpr;
-	ctx->img2.pixels = (iw_byte *)iw_malloc_large(ctx, P.out_bpr, P.out_h);
-	if(!ctx->img2.pixels) return false;
-
-	Job J;
 	memset(&J, 0, sizeof(J));
-	const int phys_h = P.orient >= 4 ? P.img1_w : P.img1_h;
-	const size_t in_bytes = P.in_bpr * (size_t)phys_h;
 	J.in_bpr = P.in_bpr;
 	J.in_depth = P.in_depth;
 	J.in_float = P.in_sampletype == IW_SAMPLETYPE_FLOATINGPOINT;
@@ -569,8 +587,6 @@ bool run_pipeline(iw_context *ctx, Plan &P, int warmup, int iters)
 	}
 
 	// ---- tables ----
-	Packer pk(S.staging);
-	std::vector<Fixup> fix;
 	auto put = [&](const void **slot, size_t off) { fix.push_back({off, slot}); };
 	std::vector<std::vector<float>> wf_store;
 	for(int d = 0; d < 2; d++) {
@@ -643,6 +659,32 @@ bool run_pipeline(iw_context *ctx, Plan &P, int warmup, int iters)
 		if(D.scan) any_scan = true;
 	}
 	J.any_scan = any_scan;
+
+	return true;
+}
+
+bool run_pipeline(iw_context *ctx, Plan &P, int warmup, int iters)
+{
+	DeviceState &S = state();
+	std::lock_guard<std::mutex> lk(S.mu);
+	std::string err;
+	if(!ensure_init(S, err)) {
+		iw_set_error(ctx, err.c_str());
+		return false;
+	}
+
+	// host output image, owned by the context
+	ctx->img2.bpr = P.out_bpr;
+	ctx->img2.pixels = (iw_byte *)iw_malloc_large(ctx, P.out_bpr, P.out_h);
+	if(!ctx->img2.pixels) return false;
+
+	Job J;
+	Packer pk(S.staging);
+	std::vector<Fixup> fix;
+	if(!make_job(ctx, P, S, pk, fix, J)) return false;
+	const int phys_h = P.orient >= 4 ? P.img1_w : P.img1_h;
+	const size_t in_bytes = P.in_bpr * (size_t)phys_h;
+	const bool any_scan = J.any_scan != 0;
 
 	// ---- buffers ----
 	// Zero copy: where the GPU can access pageable host memory coherently
@@ -744,6 +786,179 @@ bool run_pipeline(iw_context *ctx, Plan &P, int warmup, int iters)
 	return true;
 }
 
+// A batch of planned images.  The images the fast form takes run together:
+// one launch per kernel variant for the vertical and horizontal passes, one
+// exact re-evaluation launch for the flagged pixels of all of them.  Each
+// image keeps its own tables and buffers, so its bytes equal a lone run's.
+// status[i]: 1 done here, 0 left for the caller (run it alone), -1 failed
+// (error set on the context).  'dev_ms' receives the batch's device time.
+bool run_batch(const std::vector<iw_context *> &ctxs, const std::vector<Plan *> &plans, std::vector<int> &status,
+	double &dev_ms)
+{
+	DeviceState &S = state();
+	std::lock_guard<std::mutex> lk(S.mu);
+	const int n = (int)ctxs.size();
+	status.assign(n, 0);
+	dev_ms = 0;
+	std::string err;
+	if(!ensure_init(S, err)) {
+		for(int i = 0; i < n; i++) { iw_set_error(ctxs[i], err.c_str()); status[i] = -1; }
+		return false;
+	}
+	std::vector<Job> jobs(n);                 // sized once: fix-ups point into it
+	std::vector<std::vector<Fixup>> fixes(n);
+	Packer pk(S.staging);
+	std::vector<int> sel;
+	for(int i = 0; i < n; i++) {
+		iw_context *ctx = ctxs[i];
+		const Plan &P = *plans[i];
+		const char *prec = get_option(ctx, "gpu:precision");
+		if(prec && !strcmp(prec, "fp64")) continue;
+		if(!make_job(ctx, P, S, pk, fixes[i], jobs[i])) { status[i] = -1; continue; }
+		FastInfo fi;
+		if(jobs[i].any_scan || !fast_eligible(P, jobs[i], fi)) continue;
+		sel.push_back(i);
+	}
+	if(sel.empty()) return true;
+
+	// zero copy where the device reads pageable host memory (as run_pipeline)
+	bool zc = S.pageable != 0;
+	for(int i : sel) {
+		const char *upl = get_option(ctxs[i], "gpu:upload");
+		if(upl && !strcmp(upl, "copy")) zc = false;
+	}
+	// buffers of every image, the packed weight lists and the flag list in one block
+	size_t top = 0;
+	auto take = [&](size_t bytes) { size_t at = (top + 255) & ~(size_t)255; top = at + bytes; return at; };
+	const size_t o_par = take(S.staging.size());
+	const size_t o_cnt = take(256);
+	size_t nflag = 0;
+	for(int i : sel) nflag += (size_t)plans[i]->out_w * plans[i]->out_h;
+	const size_t o_flags = take(nflag * 16);
+	std::vector<size_t> o_in(n, 0), o_mid(n, 0), o_out(n, 0), in_bytes(n, 0), out_bytes(n, 0);
+	for(int i : sel) {
+		const Plan &P = *plans[i];
+		in_bytes[i] = P.in_bpr * (size_t)(P.orient >= 4 ? P.img1_w : P.img1_h);
+		out_bytes[i] = P.out_bpr * (size_t)P.out_h;
+		if(!zc) o_in[i] = take(in_bytes[i] ? in_bytes[i] : 16);
+		o_mid[i] = take((size_t)P.mid_n * jobs[i].interm_plane * sizeof(float));
+		if(!zc) o_out[i] = take(out_bytes[i]);
+	}
+	if(!S.batch_io.ensure(top)) {
+		for(int i : sel) { iw_set_error(ctxs[i], "Out of GPU memory (batch)"); status[i] = -1; }
+		return false;
+	}
+	uint8_t *base = (uint8_t *)S.batch_io.p;
+	int *flag_count = (int *)(base + o_cnt);
+	int *flag_list = (int *)(base + o_flags);
+
+	// final device addresses, then the fast form's host preparation
+	std::vector<void *> items;
+	std::vector<int> item_img;
+	for(int i : sel) {
+		iw_context *ctx = ctxs[i];
+		const Plan &P = *plans[i];
+		Job &J = jobs[i];
+		for(const Fixup &f : fixes[i]) *f.slot = base + o_par + f.off;
+		ctx->img2.bpr = P.out_bpr;
+		ctx->img2.pixels = (iw_byte *)iw_malloc_large(ctx, P.out_bpr, P.out_h);
+		if(!ctx->img2.pixels) { status[i] = -1; continue; }
+		J.in = zc ? (const uint8_t *)ctx->img1.pixels : base + o_in[i];
+		J.interm = (float *)(base + o_mid[i]);
+		J.out = zc ? (uint8_t *)ctx->img2.pixels : base + o_out[i];
+		std::string e2;
+		void *it = fast_batch_item(P, J, e2);
+		if(!it) {   // leave it to the caller's lone run
+			iw_free(ctx, ctx->img2.pixels);
+			ctx->img2.pixels = nullptr;
+			continue;
+		}
+		items.push_back(it);
+		item_img.push_back(i);
+	}
+	if(items.empty()) return true;
+	const int m = (int)items.size();
+
+	// per-image arrays of the fast form and the exact form's job array
+	std::vector<uint8_t> tab;
+	auto add = [&](const void *p, size_t bytes) {
+		size_t at = (tab.size() + 255) & ~(size_t)255;
+		tab.resize(at + bytes);
+		if(bytes) memcpy(tab.data() + at, p, bytes);
+		return at;
+	};
+	std::vector<size_t> o_blob(m);
+	for(int k = 0; k < m; k++) o_blob[k] = add(fast_item_blob(items[k]), fast_item_blob_bytes(items[k]));
+	std::vector<Job> djobs(m);
+	for(int k = 0; k < m; k++) djobs[k] = jobs[item_img[k]];
+	const size_t o_jobs = add(djobs.data(), djobs.size() * sizeof(Job));
+	auto fail_all = [&](const char *msg) {
+		for(int k = 0; k < m; k++) {
+			iw_set_error(ctxs[item_img[k]], msg);
+			status[item_img[k]] = -1;
+			fast_item_free(items[k]);
+		}
+		return false;
+	};
+	if(!S.batch_tab.ensure(tab.size())) return fail_all("Out of GPU memory (batch tables)");
+	uint8_t *tbase = (uint8_t *)S.batch_tab.p;
+	int maxt = 1;
+	for(int k = 0; k < m; k++) {
+		fast_item_place(items[k], tbase + o_blob[k], flag_count, flag_list, k);
+		maxt = std::max(maxt, fast_item_htaps(items[k]));
+	}
+
+	cudaStream_t st = S.stream;
+	cudaEvent_t e0, e1;
+	cudaEventCreate(&e0);
+	cudaEventCreate(&e1);
+	cudaMemcpyAsync(base + o_par, S.staging.data(), S.staging.size(), cudaMemcpyHostToDevice, st);
+	cudaMemcpyAsync(tbase, tab.data(), tab.size(), cudaMemcpyHostToDevice, st);
+	if(!zc)
+		for(int k = 0; k < m; k++) {
+			const int i = item_img[k];
+			cudaMemcpyAsync(base + o_in[i], ctxs[i]->img1.pixels, in_bytes[i], cudaMemcpyHostToDevice, st);
+		}
+	cudaMemsetAsync(flag_count, 0, sizeof(int), st);
+	cudaEventRecord(e0, st);
+	int launches = fast_launch_batch(st, items.data(), m, err);
+	if(launches >= 0) {
+		launch_fix_flagged_batch(st, (const Job *)(tbase + o_jobs), maxt, flag_count, flag_list);
+		launches++;
+	}
+	cudaEventRecord(e1, st);
+	if(!zc)
+		for(int k = 0; k < m; k++) {
+			const int i = item_img[k];
+			cudaMemcpyAsync(ctxs[i]->img2.pixels, base + o_out[i], out_bytes[i], cudaMemcpyDeviceToHost, st);
+		}
+	cudaError_t ce = cudaStreamSynchronize(st);
+	if(ce == cudaSuccess) ce = cudaGetLastError();
+	int nflagged = 0;
+	float ms = 0;
+	if(ce == cudaSuccess) ce = cudaMemcpy(&nflagged, flag_count, sizeof(int), cudaMemcpyDeviceToHost);
+	if(ce == cudaSuccess) cudaEventElapsedTime(&ms, e0, e1);
+	cudaEventDestroy(e0);
+	cudaEventDestroy(e1);
+	if(launches < 0) return fail_all(err.c_str());
+	if(ce != cudaSuccess) {
+		std::string msg = std::string("CUDA error: ") + cudaGetErrorString(ce);
+		return fail_all(msg.c_str());
+	}
+	dev_ms = ms;
+	for(int k = 0; k < m; k++) {
+		iw_context *ctx = ctxs[item_img[k]];
+		ctx->stats.form = 1;
+		ctx->stats.zero_copy = zc;
+		ctx->stats.kernels = launches;
+		ctx->stats.ms_device = ms;
+		ctx->stats.flagged = nflagged;
+		status[item_img[k]] = 1;
+		fast_item_free(items[k]);
+	}
+	return true;
+}
+
 // The plain form's launches; 'mark' is called after each launch group.
 template<class Mark>
 int plain_launch(cudaStream_t st, const Plan &P, const Job &J, Mark mark)
@@ -757,8 +972,8 @@ int plain_launch(cudaStream_t st, const Plan &P, const Job &J, Mark mark)
 	mark();
 	launches += 2;
 	if(J.any_scan) {
-		for(int oc = 0; oc < P.out_n; oc++)
-			if(J.outc[oc].scan) { k_scan<<<1, 32, 0, st>>>(J, oc); launches++; }
+		k_scan<<<1, 32 * P.out_n, 0, st>>>(J);
+		launches++;
 		if(J.negate || J.blacken) { k_finalize<<<gh, bh, 0, st>>>(J); launches++; }
 		mark();
 	}

@@ -219,6 +219,46 @@ def _convert_arg(a):
     return a
 
 
+def _setup(lib: IWLib, ctx, job: Job) -> None:
+    # a transposing orientation (4..7) stores the image 'height' pixels wide
+    nbytes = job.bpr * (job.width if job.orient >= 4 else job.height)
+    buf = _libc.malloc(max(nbytes, 1))
+    if not buf:
+        raise MemoryError("malloc failed")
+    C.memmove(buf, job.pixels, nbytes)
+    img = Image()
+    img.imgtype, img.bit_depth, img.sampletype = job.imgtype, job.bit_depth, job.sampletype
+    img.width, img.height, img.pixels, img.bpr = job.width, job.height, buf, job.bpr
+    img.orient_transform = job.orient
+    lib.iw_set_input_image(ctx, C.byref(img))  # the library now owns buf
+    for call in job.calls:
+        name, args = call[0], [_convert_arg(a) for a in call[1:]]
+        getattr(lib, name)(ctx, *args)
+
+
+def _collect(lib: IWLib, ctx, ok: bool, warnings: list[str]) -> Result:
+    err = None
+    if lib.iw_get_errorflag(ctx):
+        mb = C.create_string_buffer(256)
+        err = lib.iw_get_errormsg(ctx, mb, 256).decode("utf-8", "replace")
+    if not ok:
+        return Result(False, err, warnings=warnings)
+    out = Image()
+    lib.iw_get_output_image(ctx, C.byref(out))
+    n = out.bpr * out.height
+    pix = C.string_at(out.pixels, n) if (out.pixels and n) else b""
+    pal = None
+    p = lib.iw_get_output_palette(ctx)
+    if p:
+        pal = [(p.contents.entry[i].r, p.contents.entry[i].g, p.contents.entry[i].b, p.contents.entry[i].a)
+               for i in range(p.contents.num_entries)]
+    ck = tuple(out.colorkey) if out.has_colorkey_trns else None
+    lbl = tuple(out.bkgdlabel.c) if out.has_bkgdlabel else None
+    rm = tuple(out.maxcolorcode) if out.reduced_maxcolors else None
+    return Result(True, err, out.imgtype, out.bit_depth, out.sampletype, out.width, out.height, out.bpr,
+                  pix, pal, ck, lbl, rm, warnings)
+
+
 def run_job(lib: IWLib, job: Job, keep_warnings: bool = False) -> Result:
     """Run one job through ``lib`` and collect the output image."""
     ctx = lib.iw_create_context(None)
@@ -230,41 +270,30 @@ def run_job(lib: IWLib, job: Job, keep_warnings: bool = False) -> Result:
         if keep_warnings:
             cb = WARNFN(lambda _c, msg: warnings.append(msg.decode("utf-8", "replace")))
             lib.iw_set_warning_fn(ctx, cb)
-        # a transposing orientation (4..7) stores the image 'height' pixels wide
-        nbytes = job.bpr * (job.width if job.orient >= 4 else job.height)
-        buf = _libc.malloc(max(nbytes, 1))
-        if not buf:
-            raise MemoryError("malloc failed")
-        C.memmove(buf, job.pixels, nbytes)
-        img = Image()
-        img.imgtype, img.bit_depth, img.sampletype = job.imgtype, job.bit_depth, job.sampletype
-        img.width, img.height, img.pixels, img.bpr = job.width, job.height, buf, job.bpr
-        img.orient_transform = job.orient
-        lib.iw_set_input_image(ctx, C.byref(img))  # the library now owns buf
-        for call in job.calls:
-            name, args = call[0], [_convert_arg(a) for a in call[1:]]
-            getattr(lib, name)(ctx, *args)
+        _setup(lib, ctx, job)
         ok = bool(lib.iw_process_image(ctx))
-        err = None
-        if lib.iw_get_errorflag(ctx):
-            mb = C.create_string_buffer(256)
-            err = lib.iw_get_errormsg(ctx, mb, 256).decode("utf-8", "replace")
-        if not ok:
-            return Result(False, err, warnings=warnings)
-        out = Image()
-        lib.iw_get_output_image(ctx, C.byref(out))
-        n = out.bpr * out.height
-        pix = C.string_at(out.pixels, n) if (out.pixels and n) else b""
-        pal = None
-        p = lib.iw_get_output_palette(ctx)
-        if p:
-            pal = [(p.contents.entry[i].r, p.contents.entry[i].g, p.contents.entry[i].b, p.contents.entry[i].a)
-                   for i in range(p.contents.num_entries)]
-        ck = tuple(out.colorkey) if out.has_colorkey_trns else None
-        lbl = tuple(out.bkgdlabel.c) if out.has_bkgdlabel else None
-        rm = tuple(out.maxcolorcode) if out.reduced_maxcolors else None
-        return Result(True, err, out.imgtype, out.bit_depth, out.sampletype, out.width, out.height, out.bpr,
-                      pix, pal, ck, lbl, rm, warnings)
+        return _collect(lib, ctx, ok, warnings)
     finally:
         lib.iw_destroy_context(ctx)
         del cb
+
+
+def run_batch(lib: IWLib, jobs: Sequence[Job]) -> list[Result]:
+    """Run jobs as one ``iwg_process_batch`` call (libimagew_gb300 only)."""
+    ctxs = []
+    try:
+        for job in jobs:
+            ctx = lib.iw_create_context(None)
+            if not ctx:
+                raise MemoryError("iw_create_context failed")
+            ctxs.append(ctx)
+            _setup(lib, ctx, job)
+        f = lib.dll.iwg_process_batch
+        f.restype = C.c_int
+        f.argtypes = [C.POINTER(C.c_void_p), C.c_int]
+        arr = (C.c_void_p * len(ctxs))(*ctxs)
+        f(arr, len(ctxs))
+        return [_collect(lib, ctx, not lib.iw_get_errorflag(ctx), []) for ctx in ctxs]
+    finally:
+        for ctx in ctxs:
+            lib.iw_destroy_context(ctx)

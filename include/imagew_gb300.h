@@ -51,6 +51,20 @@ IW_EXPORT(int) iwg_process_image_timed(struct iw_context *ctx, int warmup, int i
  * buf (NUL-terminated, at most buflen bytes).  Returns 0 if no device. */
 IW_EXPORT(int) iwg_device_info(char *buf, int buflen);
 
+/* Processes n contexts as one batch.  Each context must be set up as for
+ * iw_process_image() and not yet processed; afterwards each holds exactly the
+ * output iw_process_image() would have given it alone (and counts as
+ * processed).  The images the FP32 form takes run together, one kernel launch
+ * per kernel variant and pass for the whole batch, in chunks of at most 8 GiB
+ * of device memory; the others run one after another.  Planning and the
+ * output post-pass run on several host threads, so warning callbacks may be
+ * called from them.  Returns the number of contexts processed successfully; a
+ * context that failed has its error set as with iw_process_image().
+ * iwg_get_stats() of a context processed with the others reports the whole
+ * call's wall time (ms_total) and the device time of all its batched passes
+ * (ms_device). */
+IW_EXPORT(int) iwg_process_batch(struct iw_context **ctxs, int n);
+
 /* Resamples one 8-bit image without allocating any memory, host or device.
  * No counterpart in the reference: it is the iw_process_image() pixel path
  * (reference arithmetic, FP64 form, bit-identical output) narrowed to what a
