@@ -66,6 +66,15 @@ class Stats(C.Structure):
                 ("flagged", C.c_longlong), ("form", C.c_int), ("kernels", C.c_int), ("zero_copy", C.c_int)]
 
 
+_T0 = time.perf_counter()
+
+
+def progress(msg: str) -> None:
+    """One line per bench phase on stderr (the JSON line stays alone on stdout)."""
+    sys.stderr.write(f"[bench {time.perf_counter() - _T0:7.1f}s] {msg}\n")
+    sys.stderr.flush()
+
+
 def dist_env():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
@@ -174,7 +183,7 @@ def device_timed(lib: IWLib, job, warmup: int, steps: int, form: str):
         lib.iw_destroy_context(ctx)
 
 
-def e2e_timed(lib: IWLib, job, warmup: int, steps: int):
+def e2e_timed(lib: IWLib, job, warmup: int, steps: int, extra_calls=()):
     """Per step, wall clock: the C-ABI call sequence a caller makes with its
     image already in a malloc'd host buffer -- iw_create_context,
     iw_set_input_image (ownership passes to the library), the settings,
@@ -193,7 +202,7 @@ def e2e_timed(lib: IWLib, job, warmup: int, steps: int):
         t0 = time.perf_counter()
         ctx = lib.iw_create_context(None)
         lib.iw_set_input_image(ctx, C.byref(img))
-        for call in job.calls:
+        for call in list(job.calls) + list(extra_calls):
             getattr(lib, call[0])(ctx, *[_convert_arg(a) for a in call[1:]])
         ok = lib.iw_process_image(ctx)
         out = Image()
@@ -285,7 +294,8 @@ def run_reference_arm(args, rank, world):
     return 0
 
 
-def batch_leg(lib: IWLib, n_images: int, pool_size: int, cpu_threads: int, cpu_images: int):
+def batch_leg(lib: IWLib, n_images: int, pool_size: int, cpu_threads: int, cpu_images: int,
+              modes=("copy", "stage", "zero")):
     """The batched configuration: n_images contexts (image content drawn from a
     pool of pool_size generated images, sizes log-uniform 64..2048, gray/RGB/RGBA,
     8/16-bit, five filters, each fitted to a 256x256 box) through one
@@ -298,8 +308,8 @@ def batch_leg(lib: IWLib, n_images: int, pool_size: int, cpu_threads: int, cpu_i
     f.restype = C.c_int
     f.argtypes = [C.POINTER(C.c_void_p), C.c_int]
 
-    def run(js):
-        ctxs = [make_ctx(lib, j) for j in js]
+    def run(js, mode):
+        ctxs = [make_ctx(lib, j, [("iw_set_option", b"gpu:upload", mode.encode())]) for j in js]
         arr = (C.c_void_p * len(ctxs))(*ctxs)
         t0 = time.perf_counter()
         ok = f(arr, len(ctxs))
@@ -312,11 +322,16 @@ def batch_leg(lib: IWLib, n_images: int, pool_size: int, cpu_threads: int, cpu_i
         for c in ctxs:
             lib.iw_destroy_context(c)
 
-    ctxs, _, _, _ = run(jobs[:64])     # warm-up: device tables, kernel modules
+    ctxs, _, _, _ = run(jobs[:64], modes[0])     # warm-up: device tables, kernel modules
     free(ctxs)
-    ctxs, ok, wall, st = run(jobs)
-    digests = [output_digest(lib, ctxs[k]) for k in range(min(pool_size, n_images))]
-    free(ctxs)
+    per_mode = {}
+    for mode in modes:
+        ctxs, ok_m, wall_m, st_m = run(jobs, mode)
+        dig_m = [output_digest(lib, ctxs[k]) for k in range(min(pool_size, n_images))]
+        free(ctxs)
+        per_mode[mode] = {"wall_ms": 1000 * wall_m, "e2e_mpix_s": out_px / 1e6 / wall_m, "device_ms": st_m.ms_device}
+        if mode == modes[0]:
+            ok, wall, st, digests = ok_m, wall_m, st_m, dig_m
     # the same images one by one through iw_process_image, for the batching gain and identity
     t0 = time.perf_counter()
     lone = []
@@ -331,7 +346,7 @@ def batch_leg(lib: IWLib, n_images: int, pool_size: int, cpu_threads: int, cpu_i
            "e2e_mpix_s": out_px / 1e6 / wall, "wall_ms": 1000 * wall,
            "device_ms": st.ms_device, "device_mpix_s": out_px / 1e6 / (st.ms_device / 1000.0) if st.ms_device else None,
            "lone_mpix_s": pool_px / 1e6 / lone_dt,
-           "identical_to_lone": digests == lone[:len(digests)]}
+           "identical_to_lone": digests == lone[:len(digests)], "transfer": modes[0], "by_transfer_mode": per_mode}
     if cpu_images > 0:
         import concurrent.futures as cf
         oracle = IWLib(os.path.join(ROOT, "oracle", "_build", "liboracle_iw.so"))
@@ -347,6 +362,89 @@ def batch_leg(lib: IWLib, n_images: int, pool_size: int, cpu_threads: int, cpu_i
     return res
 
 
+def serving_leg(lib: IWLib, rate: float, seconds: float, thumbs, ups):
+    """The serving configuration: Poisson arrivals at 'rate' requests/s for
+    'seconds'; 70 % thumbnails (the batched config's images), 30 % 2-4x
+    upscales (4:3 inputs 160x120..1024x768, Catmull-Rom), 10 % of all with
+    Floyd-Steinberg error diffusion; an 8 GiB device budget per batch.
+    Latency = submit -> completion as the server measures it."""
+    import queue
+    from imageworsener_gb300.iwapi import Completion, ServerStats, server_api, CT_ALL, DITHER_ERRDIFF
+    d = server_api(lib)
+    sched = W.serving_schedule(rate, seconds)
+    ed = [("iw_set_dither_type", CT_ALL, DITHER_ERRDIFF, 0)]
+    srv = d.iwg_server_create(8 << 30, 0, 0)
+    ready = queue.Queue(maxsize=512)
+    lat = {}
+    out_px = {}
+    stop = threading.Event()
+
+    def producer():
+        for k, (t, kind, errdiff) in enumerate(sched):
+            job = thumbs[k % len(thumbs)] if kind == "thumb" else ups[k % len(ups)]
+            ctx = make_ctx(lib, job, ed if errdiff else [])
+            ready.put((k, t, ctx, W.out_pixels(job)))
+
+    ctxs = {}
+
+    def poller():
+        buf = (Completion * 256)()
+        while not stop.is_set() or len(lat) < len(sched):
+            n = d.iwg_server_poll(srv, buf, 256, 50)
+            for i in range(n):
+                k = buf[i].tag
+                lat[k] = (buf[i].latency_ms, buf[i].ok)
+                lib.iw_destroy_context(ctxs.pop(k))
+            if stop.is_set() and len(lat) >= len(sched):
+                break
+
+    pt = threading.Thread(target=producer, daemon=True)
+    pt.start()
+    po = threading.Thread(target=poller, daemon=True)
+    po.start()
+    t0 = time.perf_counter()
+    late = 0
+    for _ in range(len(sched)):
+        k, t, ctx, px = ready.get(timeout=120)
+        now = time.perf_counter() - t0
+        if t > now:
+            time.sleep(t - now)
+        elif now - t > 0.005:
+            late += 1
+        ctxs[k] = ctx
+        out_px[k] = px
+        d.iwg_server_submit(srv, ctx, k)
+    t_sub = time.perf_counter() - t0
+    stop.set()
+    po.join(timeout=max(60.0, 6 * seconds))
+    wall = time.perf_counter() - t0
+    drained = len(lat) == len(sched)
+    info = ServerStats()
+    d.iwg_server_info(srv, C.byref(info))
+    if drained:
+        d.iwg_server_destroy(srv)   # (left running otherwise: the backlog did not drain in time)
+    ls = sorted(v[0] for v in lat.values())
+    pct = lambda q: ls[min(len(ls) - 1, int(q * len(ls)))] if ls else None
+    done_px = sum(out_px[k] for k in lat)
+
+    def cls(sel):
+        v = sorted(lat[k][0] for k in lat if sel(sched[k]))
+        return {"n": len(v), "p50_ms": v[len(v) // 2] if v else None,
+                "p99_ms": v[min(len(v) - 1, int(0.99 * len(v)))] if v else None}
+    return {"rate_req_s": rate, "seconds": seconds, "requests": len(sched), "completed": len(lat),
+            "failed": sum(1 for v in lat.values() if not v[1]),
+            "errdiff_requests": sum(1 for x in sched if x[2]), "upscale_requests": sum(1 for x in sched if x[1] == "up"),
+            "p50_ms": pct(0.50), "p90_ms": pct(0.90), "p99_ms": pct(0.99), "max_ms": ls[-1] if ls else None,
+            "throughput_mpix_s": done_px / 1e6 / wall, "wall_s": wall, "submit_s": t_sub,
+            "late_submits": late, "device_budget_gib": 8, "drained": drained,
+            "by_class": {"thumb": cls(lambda x: x[1] == "thumb" and not x[2]), "up": cls(lambda x: x[1] == "up" and not x[2]),
+                         "errdiff_thumb": cls(lambda x: x[1] == "thumb" and x[2]),
+                         "errdiff_up": cls(lambda x: x[1] == "up" and x[2])},
+            "lanes": {"batches": info.batches, "batched_requests": info.batched_requests,
+                      "device_ms": info.device_ms, "scan_lane_batches": info.slow_batches,
+                      "scan_lane_requests": info.slow_requests, "scan_lane_device_ms": info.slow_device_ms}}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -357,6 +455,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--batch-images", type=int, default=4096, help="batched leg: contexts per call (0: skip)")
     ap.add_argument("--batch-pool", type=int, default=256, help="batched leg: distinct generated images")
+    ap.add_argument("--serve-seconds", type=float, default=10.0, help="serving leg: length of the arrival stream (0: skip)")
+    ap.add_argument("--serve-rate", type=float, default=2000.0, help="serving leg: requests per second")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     rank, world, local = dist_env()
@@ -385,16 +485,40 @@ def main():
 
     with ClockSampler(local) as clk:
         barrier()
+        progress("device-timed fp32")
         st, dig_fast = device_timed(lib, job, args.warmup, args.steps, "fp32")
         barrier()
+        progress("device-timed fp64")
         st64, dig_plain = device_timed(lib, job, 1, max(2, min(args.steps, 5)), "fp64")
         barrier()
+        progress("end to end")
         e2e_times, dig_e2e, e2e_zc = e2e_timed(lib, job, 2, max(3, min(args.steps, 10)))
+        e2e_modes = {}
+        for mode in ("zero", "stage", "copy"):
+            progress(f"end to end, transfer {mode}")
+            tm, dg, info = e2e_timed(lib, job, 2, 5, [("iw_set_option", b"gpu:upload", mode.encode())])
+            e2e_modes[mode] = {"ms_per_step": 1000.0 * statistics.mean(tm), "bit_exact": dg == gold,
+                               "device_ms": info.get("device_ms")}
         barrier()
         batched = None
         if args.batch_images > 0:
+            progress("batched configuration")
             batched = batch_leg(lib, args.batch_images, min(args.batch_pool, args.batch_images),
                                 os.cpu_count() or 1, 0 if args.no_cpu_baseline else 64)
+        progress("large downscale")
+        large = {}
+        for name in ("downscale", "downscale_fs4"):
+            ljob = WORKLOADS[name]()
+            lst, ldig = device_timed(lib, ljob, 1, 3, "fp32")
+            large[name] = {"ms": lst.ms_device, "mpix_s": W.out_pixels(ljob) / 1e6 / (lst.ms_device / 1000.0),
+                           "input_gb_s": len(ljob.pixels) / 1e9 / (lst.ms_device / 1000.0), "form": lst.form,
+                           "flagged": lst.flagged, "kernel_ms": list(lst.ms_part)[:3],
+                           "bit_exact": ldig == golden_digest(name)}
+        serving = None
+        if args.serve_seconds > 0:
+            progress("serving configuration")
+            serving = serving_leg(lib, args.serve_rate, args.serve_seconds, W.batch(128, seed=4),
+                                  W.upscale_pool(64))
         barrier()
 
     ms = st.ms_device
@@ -434,8 +558,8 @@ def main():
         "e2e": {"value": world * out_px / 1e6 / (e2e_ms / 1000.0), "unit": "Mpix/s", "h2d_bytes_per_step": in_bytes,
                 "d2h_bytes_per_step": out_bytes, "ms_per_step": e2e_ms, "p50_ms": 1000 * statistics.median(e2e_times),
                 "host_buffers": "pageable (caller-malloc'd, as the libimagew ownership model requires)",
-                "transfer": "zero-copy (GPU reads/writes host memory over NVLink-C2C)" if e2e_zc.get("zero_copy") else "cudaMemcpy",
-                "last_call": e2e_zc},
+                "transfer": "zero-copy (GPU reads/writes host memory over NVLink-C2C)" if e2e_zc.get("zero_copy") else "pinned staging (host copy threads + DMA)",
+                "last_call": e2e_zc, "by_transfer_mode": e2e_modes},
         "roofline": {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None, "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)",
                      "traffic": None, "algorithmic_bytes_per_launch": comp[dom],
@@ -448,6 +572,8 @@ def main():
         "bit_exact": {"fp32": dig_fast == gold, "fp64": dig_plain == gold, "e2e": dig_e2e == gold,
                       "golden": gold is not None},
         "batched": batched,
+        "serving": serving,
+        "large_downscale": large,
         "gpu_launches": st.kernels * args.steps,
         "clocks": clk.summary(),
         "cpu_baseline": cpu,

@@ -940,17 +940,30 @@ void parallel_for(int n, Fn fn)
 	for(std::thread &x : th) x.join();
 }
 
+}  // namespace
+
+// Output channels quantised by a serial scan (error-diffusion / random dither).
+bool iwg::plan_needs_scan(const iwg::Plan &P)
+{
+	if(P.out_sampletype != IW_SAMPLETYPE_UINT) return false;
+	for(int oc = 0; oc < P.out_n; oc++) {
+		const int f = P.out[oc].q.dfam;
+		if(f == IW_DITHERFAMILY_ERRDIFF || f == IW_DITHERFAMILY_RANDOM) return true;
+	}
+	return false;
+}
+
 // Device bytes one image of a batch holds while it runs (input, float
-// intermediate, output, flag entries).
-size_t batch_bytes(const iwg::Plan &P)
+// intermediate, output, flag entries; scan buffers for serial dither).
+size_t iwg::batch_device_bytes(const iwg::Plan &P)
 {
 	const size_t in = P.in_bpr * (size_t)(P.orient >= 4 ? P.img1_w : P.img1_h);
 	const size_t mid = (size_t)P.mid_n * P.crop_w * P.out_h * sizeof(float);
 	const size_t out = P.out_bpr * (size_t)P.out_h;
-	return in + mid + out + (size_t)P.out_w * P.out_h * 16 + 4096;
+	size_t scan = 0;
+	if(plan_needs_scan(P)) scan = (size_t)P.out_n * P.out_w * ((size_t)P.out_h + 4) * sizeof(double);
+	return in + mid + out + scan + (size_t)P.out_w * P.out_h * 16 + 4096;
 }
-
-}  // namespace
 
 extern "C" int iwg_process_batch(struct iw_context **ctxs, int n)
 {
@@ -983,7 +996,7 @@ extern "C" int iwg_process_batch(struct iw_context **ctxs, int n)
 		size_t bytes = 0;
 		while(k < order.size()) {
 			const int i = order[k];
-			const size_t b = batch_bytes(plans[i]);
+			const size_t b = iwg::batch_device_bytes(plans[i]);
 			if(!idx.empty() && bytes + b > kBudget) break;
 			bytes += b;
 			cc.push_back(ctxs[i]);
@@ -995,10 +1008,28 @@ extern "C" int iwg_process_batch(struct iw_context **ctxs, int n)
 		double dev_ms = 0;
 		iwg::run_batch(cc, pp, status, dev_ms);
 		dev_total += dev_ms;
+		// what the fast form did not take: one batch in the plain form
+		std::vector<iw_context *> cc2;
+		std::vector<iwg::Plan *> pp2;
+		std::vector<int> idx2;
 		for(size_t j = 0; j < idx.size(); j++) {
 			const int i = idx[j];
 			if(status[j] == 1) done[i] = batched[i] = 1;
-			else if(status[j] == 0) done[i] = iwg::run_pipeline(ctxs[i], plans[i]) ? 1 : 0;   // alone
+			else if(status[j] == 0) {
+				cc2.push_back(ctxs[i]);
+				pp2.push_back(&plans[i]);
+				idx2.push_back(i);
+			}
+		}
+		if(!cc2.empty()) {
+			std::vector<int> status2;
+			iwg::run_batch_plain(cc2, pp2, status2, dev_ms);
+			dev_total += dev_ms;
+			for(size_t j = 0; j < idx2.size(); j++) {
+				const int i = idx2[j];
+				if(status2[j] == 1) done[i] = batched[i] = 1;
+				else if(status2[j] == 0) done[i] = iwg::run_pipeline(ctxs[i], plans[i]) ? 1 : 0;   // alone
+			}
 		}
 	}
 	parallel_for(n, [&](int i) {

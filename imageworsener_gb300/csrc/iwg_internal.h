@@ -266,10 +266,17 @@ void nc_fill(int cstype, double gamma, double *nc);
 void optimize(iw_context *ctx);
 
 // pipeline.cu
-bool run_pipeline(iw_context *ctx, Plan &P, int warmup = 0, int iters = 1);
+bool run_pipeline(iw_context *ctx, Plan &P, int warmup = 0, int iters = 1, int lane = 0);
+// Whether an output channel is quantised by a serial scan (api.cpp).
+bool plan_needs_scan(const Plan &P);
+// Device bytes an image holds while it runs in a batch (api.cpp).
+size_t batch_device_bytes(const Plan &P);
 // Runs the fast-form images of a batch together (pipeline.cu); see there.
 bool run_batch(const std::vector<iw_context *> &ctxs, const std::vector<Plan *> &plans, std::vector<int> &status,
-	double &dev_ms);
+	double &dev_ms, int lane = 0);
+// The same in the plain (FP64) form for any image, scans in parallel (pipeline.cu).
+bool run_batch_plain(const std::vector<iw_context *> &ctxs, const std::vector<Plan *> &plans, std::vector<int> &status,
+	double &dev_ms, int lane = 0);
 
 // api.cpp
 const char *get_option(iw_context *ctx, const char *name);

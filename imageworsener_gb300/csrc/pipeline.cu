@@ -17,7 +17,11 @@
 #include "fastpath.cuh"
 #include "imagew_gb300.h"
 
+#include <algorithm>
 #include <chrono>
+#include <condition_variable>
+#include <functional>
+#include <thread>
 #include <cmath>
 #include <cstring>
 #include <map>
@@ -34,10 +38,8 @@ using namespace dev;
 // ===========================================================================
 
 // Vertical pass: one thread per (column x, intermediate row j), all channels.
-__global__ void k_vpass_exact(Job J)
+__device__ __forceinline__ void vpass_exact_at(const Job &J, int x, int j)
 {
-	int x = blockIdx.x * blockDim.x + threadIdx.x;
-	int j = blockIdx.y;
 	if(x >= J.mid_w || j >= J.mid_h) return;
 	for(int m = 0; m < J.mid_n; m++) {
 		const DMid &mc = J.mid[m];
@@ -57,6 +59,11 @@ __global__ void k_vpass_exact(Job J)
 		if(J.intclamp) s = s < 0.0 ? 0.0 : (s > 1.0 ? 1.0 : s);
 		J.interm[(unsigned long long)m * J.interm_plane + (unsigned long long)j * J.mid_w + x] = __double2float_rn(s);
 	}
+}
+
+__global__ void k_vpass_exact(Job J)
+{
+	vpass_exact_at(J, blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y);
 }
 
 // Exact intermediate value of channel m at (column x, row j): read from the
@@ -180,21 +187,180 @@ __device__ void pixel_exact(const Job &J, int i, int j, bool apply_post, Interm 
 	}
 }
 
-__global__ void k_hpass_exact(Job J)
+__device__ __forceinline__ void hpass_exact_at(const Job &J, int i, int j)
 {
-	int i = blockIdx.x * blockDim.x + threadIdx.x;
-	int j = blockIdx.y;
 	if(i >= J.out_w || j >= J.out_h) return;
 	pixel_exact(J, i, j, !J.any_scan, [&](int m, int, int x) { return interm_exact<false>(J, m, x, j); });
 }
 
-// Serial scan for error-diffusion and random dither of one output channel
+__global__ void k_hpass_exact(Job J)
+{
+	hpass_exact_at(J, blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y);
+}
+
+// Serial scans for error-diffusion and random dither of one output channel
 // (src/imagew-main.c:487-567, :1072-1136).  The reference visits samples in a
 // fixed order and each decision depends on the previous ones.  Error
 // diffusion runs serpentine: a right-to-left row starts where the row above
 // ended, so it needs that whole row's errors and rows cannot overlap in a
-// wavefront.  One thread walks the whole channel; channels are independent
-// and run in separate warps of one launch.
+// wavefront.  Channels are independent and run in separate warps.
+
+// Bracket of v in [0, 1] with integer comparisons: for non-negative doubles
+// the order of the bit patterns is the order of the values (the tables' -inf
+// and +inf ends compare correctly as signed integers), which keeps the FP64
+// pipe free for the arithmetic.
+__device__ __forceinline__ Bracket bracket_bits(const DQuant &q, double v)
+{
+	const long long vb = __double_as_longlong(v);
+	const long long *U = reinterpret_cast<const long long *>(q.U) + 1;
+	int lo = 0, hi = q.P;
+	while(lo < hi) {
+		const int mid = (lo + hi) >> 1;
+		if(__ldg(U + mid) <= vb) lo = mid + 1; else hi = mid;
+	}
+	Bracket b;
+	const int k = lo;
+	b.exact = (k == q.P) || (vb < __ldg(reinterpret_cast<const long long *>(q.X) + k));
+	b.lo = q.code[k];
+	b.hi = q.code[k + 1];
+	b.d_lo = b.d_hi = 0.0;
+	if(!b.exact) {
+		b.d_lo = dsub(v, q.rev[b.lo]);
+		b.d_hi = dsub(q.rev[b.hi], v);
+	}
+	return b;
+}
+
+// The twelve error-diffusion weights of subtype 'dsub': numerators over a
+// denominator (positions x+1 x+2 / x-2 x-1 x x+1 x+2 / the same on the row
+// after next), as separately rounded quotients like the reference's.
+__device__ __forceinline__ void errdiff_weights(int dsub, double *c)
+{
+	const signed char num[8][12] = {
+		{7,0, 0,3,5,1,0, 0,0,0,0,0}, {7,5, 3,5,7,5,3, 1,3,5,3,1}, {8,4, 2,4,8,4,2, 1,2,4,2,1},
+		{8,4, 2,4,8,4,2, 0,0,0,0,0}, {5,3, 2,4,5,4,2, 0,2,3,2,0}, {4,3, 1,2,3,2,1, 0,0,0,0,0},
+		{2,0, 0,1,1,0,0, 0,0,0,0,0}, {1,1, 0,1,1,1,0, 0,0,1,0,0}};
+	const double den[8] = {16.0, 48.0, 42.0, 32.0, 32.0, 16.0, 4.0, 8.0};
+	const int sub = (dsub >= 0 && dsub <= 7) ? dsub : 0;
+	for(int k = 0; k < 12; k++) c[k] = ddiv((double)num[sub][k], den[sub]);
+}
+
+// Bracket index k (U[k] <= v < U[k+1]) of v >= +0, by binary search.
+__device__ __forceinline__ int bracket_index(const DQuant &q, long long vb)
+{
+	const long long *U = reinterpret_cast<const long long *>(q.U) + 1;
+	int lo = 0, hi = q.P;
+	while(lo < hi) {
+		const int mid = (lo + hi) >> 1;
+		if(__ldg(U + mid) <= vb) lo = mid + 1; else hi = mid;
+	}
+	return lo;
+}
+
+// Error diffusion of one channel by one warp.  Per row:
+//   1. all lanes clamp the row's values and find their brackets (the value
+//      before its error is added; the error moves it by about one code);
+//   2. lane 0 walks the samples in the reference's order doing only what
+//      the next sample depends on -- the value plus its accumulated error
+//      (the error carried from the previous rows plus the two in-row
+//      contributions, kept in registers and added in the reference's order),
+//      the decision from the nearby bracket, and the sample's error;
+//   3. all lanes send the row's errors to the next two rows (e1, e2), each
+//      lane owning target positions and adding the contributions in the order
+//      the reference adds them (sample x-2f, x-f, x, x+f, x+2f); rows shift.
+// Error buffer of a channel: e0, e1, e2, the row's errors and the row's
+// brackets, out_w doubles each.
+__device__ void errdiff_warp(const Job &J, int oc)
+{
+	const int lane = threadIdx.x & 31;
+	const DOut &o = J.outc[oc];
+	const DQuant &q = o.q;
+	const int W = J.out_w;
+	double *e0 = J.errbuf + (unsigned long long)oc * 5 * W, *e1 = e0 + W, *e2 = e1 + W, *er = e2 + W;
+	int *kb = reinterpret_cast<int *>(er + W);
+	const long long *U = reinterpret_cast<const long long *>(q.U);
+	const long long *X = reinterpret_cast<const long long *>(q.X);
+	double c[12];
+	errdiff_weights(q.dsub, c);
+	for(int x = lane; x < 3 * W; x += 32) e0[x] = 0.0;
+	__syncwarp();
+	const double skip = __longlong_as_double(0x7ff8dead0000beefLL);   // a NaN: the sample sent no error
+	for(int y = 0; y < J.out_h; y++) {
+		const int f = (y % 2) ? -1 : 1;
+		const double *row = J.scanbuf + ((unsigned long long)oc * J.out_h + y) * W;
+		for(int t = lane; t < W; t += 32) {
+			double v = row[t];
+			if(v < 0.0) v = 0.0;
+			if(v > 1.0) v = 1.0;
+			kb[t] = v == v ? bracket_index(q, __double_as_longlong(dadd(v, 0.0))) : 0;
+		}
+		__syncwarp();
+		if(lane == 0) {
+			double err1 = 0.0, err2 = 0.0;     // errors of the previous two samples
+			bool has1 = false, has2 = false;
+			for(int z = 0; z < W; z++) {
+				const int x = (y % 2) ? W - 1 - z : z;
+				double v = row[x];
+				if(v < 0.0) v = 0.0;
+				if(v > 1.0) v = 1.0;
+				// e0[x] as the reference has it when it reaches x: the carried
+				// error, then x-2f's contribution, then x-f's
+				double e = e0[x];
+				if(has2) e = dadd(e, dmul(err2, c[1]));
+				if(has1) e = dadd(e, dmul(err1, c[0]));
+				v = dadd(v, e);
+				if(v > 1.0) v = 1.0;
+				else if(v < 0.0) v = 0.0;
+				int code;
+				double err = skip;
+				if(v != v) code = 0;
+				else {
+					const long long vb = __double_as_longlong(dadd(v, 0.0));   // -0 becomes +0 (same value)
+					int k = kb[x];
+					while(k < q.P && __ldg(U + k + 1) <= vb) k++;
+					while(k > 0 && __ldg(U + k) > vb) k--;
+					const int lo = q.code[k], hi = q.code[k + 1];
+					if(k == q.P || vb < __ldg(X + k)) code = lo;
+					else {
+						const double d_lo = dsub(v, q.rev[lo]), d_hi = dsub(q.rev[hi], v);
+						if(d_hi <= d_lo) { err = -d_hi; code = hi; }
+						else { err = d_lo; code = lo; }
+					}
+				}
+				er[x] = err;
+				// this sample's contributions reach x+f (c0) and x+2f (c1) when those exist
+				const bool sent = err == err;
+				err2 = err1; has2 = has1 && (x + f >= 0 && x + f < W);
+				err1 = err; has1 = sent;
+				store_code(J, oc, x, y, (unsigned int)code);
+			}
+		}
+		__syncwarp();
+		for(int t = lane; t < W; t += 32) {
+			double a1 = e1[t], a2 = e2[t];
+#pragma unroll
+			for(int k = -2; k <= 2; k++) {          // source sample t + k*f, in processing order
+				const int qx = t + k * f;
+				if(qx < 0 || qx >= W) continue;
+				const double err = er[qx];
+				if(err != err) continue;
+				a1 = dadd(a1, dmul(err, c[4 - k]));
+				a2 = dadd(a2, dmul(err, c[9 - k]));
+			}
+			e1[t] = a1;
+			e2[t] = a2;
+		}
+		__syncwarp();
+		for(int t = lane; t < W; t += 32) {
+			e0[t] = e1[t];
+			e1[t] = e2[t];
+			e2[t] = 0.0;
+		}
+		__syncwarp();
+	}
+}
+
+// Multiply-with-carry generator of the reference (src/imagew-util.c:202-233).
 __device__ unsigned int prng_next(unsigned int &mult, unsigned int &carry)
 {
 	unsigned long long x = 0xfff0bf23ULL * mult + carry;
@@ -203,80 +369,86 @@ __device__ unsigned int prng_next(unsigned int &mult, unsigned int &carry)
 	return mult;
 }
 
-__device__ void scan_channel(const Job &J, int oc)
+// ---- random dither: the generator jumped ahead per row ----
+//
+// The generator's state (mult m, carry c) packs into w = a*m + c (a =
+// 0xfff0bf23, c < a, m < 2^32), and one draw maps w to -a*w + a*(2^32-1)
+// modulo the prime q = a*2^32 + 1 (a complementary multiply-with-carry is
+// an affine map on w).  The state after n draws is that map composed n
+// times, found by squaring, so each row of samples starts from its own state
+// and rows run in parallel while every sample still gets the draw the
+// reference gives it (one draw per sample in row-major order).
+constexpr unsigned long long kMwcA = 0xfff0bf23ULL;
+constexpr unsigned long long kMwcQ = 0xfff0bf2300000001ULL;   // a * 2^32 + 1
+constexpr unsigned long long kMwcD = 0x000f40dcffffffffULL;   // 2^64 - q = 2^64 mod q
+
+__device__ __forceinline__ unsigned long long mwc_mod(unsigned long long hi, unsigned long long lo)
 {
+	while(hi) {   // hi * 2^64 + lo == hi * D + lo (mod q); D < 2^52, so hi shrinks each round
+		const unsigned long long ph = __umul64hi(hi, kMwcD), pl = hi * kMwcD;
+		const unsigned long long nl = pl + lo;
+		hi = ph + (nl < pl ? 1ULL : 0ULL);
+		lo = nl;
+	}
+	return lo >= kMwcQ ? lo - kMwcQ : lo;
+}
+
+__device__ __forceinline__ unsigned long long mwc_mul(unsigned long long x, unsigned long long y)
+{
+	return mwc_mod(__umul64hi(x, y), x * y);
+}
+
+__device__ __forceinline__ unsigned long long mwc_add(unsigned long long x, unsigned long long y)
+{
+	const unsigned long long s = x + y;
+	return mwc_mod(s < x ? 1ULL : 0ULL, s);
+}
+
+// Generator state after n draws from (mult, carry).
+__device__ void mwc_jump(unsigned int &mult, unsigned int &carry, unsigned long long n)
+{
+	unsigned long long A = 1, B = 0;                                  // identity map
+	unsigned long long pa = kMwcQ - kMwcA, pb = kMwcQ - 1 - kMwcA;    // one draw: w -> -a*w + a*(2^32-1)
+	while(n) {
+		if(n & 1) {
+			B = mwc_add(mwc_mul(pa, B), pb);
+			A = mwc_mul(pa, A);
+		}
+		pb = mwc_add(mwc_mul(pa, pb), pb);
+		pa = mwc_mul(pa, pa);
+		n >>= 1;
+	}
+	const unsigned long long w = mwc_add(mwc_mul(A, kMwcA * mult + carry), B);
+	mult = (unsigned int)(w / kMwcA);
+	carry = (unsigned int)(w % kMwcA);
+}
+
+// Random dither of one channel by one warp: lane l takes rows l, l+32, ...
+__device__ void random_warp(const Job &J, int oc)
+{
+	const int lane = threadIdx.x & 31;
 	const DOut &o = J.outc[oc];
 	const DQuant &q = o.q;
 	const int W = J.out_w;
-	const bool errdiff = q.dfam == IW_DITHERFAMILY_ERRDIFF;
-	double *e0 = J.errbuf + (unsigned long long)oc * 3 * W, *e1 = e0 + W, *e2 = e1 + W;
-	unsigned int mult = 0, carry = 0;
-	if(q.dfam == IW_DITHERFAMILY_RANDOM) {
-		int s = (q.dsub == IW_DITHERSUBTYPE_SAMEPATTERN && o.ctype != IW_CHANNELTYPE_ALPHA) ? J.seed : J.seed + o.ctype;
-		mult = 0x03333333U + (unsigned int)s;
-		carry = 0x05555555U + (unsigned int)s;
-	}
-	// error-diffusion kernels: numerators over a denominator
-	// (positions: x+1 x+2 / x-2 x-1 x x+1 x+2 / same on the row after)
-	const signed char num[8][12] = {
-		{7,0, 0,3,5,1,0, 0,0,0,0,0}, {7,5, 3,5,7,5,3, 1,3,5,3,1}, {8,4, 2,4,8,4,2, 1,2,4,2,1},
-		{8,4, 2,4,8,4,2, 0,0,0,0,0}, {5,3, 2,4,5,4,2, 0,2,3,2,0}, {4,3, 1,2,3,2,1, 0,0,0,0,0},
-		{2,0, 0,1,1,0,0, 0,0,0,0,0}, {1,1, 0,1,1,1,0, 0,0,1,0,0}};
-	const double den[8] = {16.0, 48.0, 42.0, 32.0, 32.0, 16.0, 4.0, 8.0};
-	int sub = (q.dsub >= 0 && q.dsub <= 7) ? q.dsub : 0;
-	double c[12];
-	for(int k = 0; k < 12; k++) c[k] = ddiv((double)num[sub][k], den[sub]);
-	if(errdiff)
-		for(int x = 0; x < 3 * W; x++) e0[x] = 0.0;
-
-	for(int y = 0; y < J.out_h; y++) {
-		const int f = (y % 2) ? -1 : 1;
-		for(int z = 0; z < W; z++) {
-			int x = (errdiff && (y % 2)) ? W - 1 - z : z;
-			double v = J.scanbuf[((unsigned long long)oc * J.out_h + y) * W + x];
+	const int s = (q.dsub == IW_DITHERSUBTYPE_SAMEPATTERN && o.ctype != IW_CHANNELTYPE_ALPHA) ? J.seed : J.seed + o.ctype;
+	for(int y = lane; y < J.out_h; y += 32) {
+		unsigned int mult = 0x03333333U + (unsigned int)s, carry = 0x05555555U + (unsigned int)s;
+		mwc_jump(mult, carry, (unsigned long long)y * W);
+		const double *row = J.scanbuf + ((unsigned long long)oc * J.out_h + y) * W;
+		for(int x = 0; x < W; x++) {
+			double v = row[x];
 			if(v < 0.0) v = 0.0;
 			if(v > 1.0) v = 1.0;
 			int code;
-			if(errdiff) {
-				v = dadd(v, e0[x]);
-				if(v > 1.0) v = 1.0;
-				else if(v < 0.0) v = 0.0;
-			}
 			if(v != v) {
 				code = 0;
-				if(!errdiff) (void)prng_next(mult, carry);
+				(void)prng_next(mult, carry);
 			}
 			else {
-				Bracket b = bracket_exact(q, v);
+				Bracket b = bracket_bits(q, dadd(v, 0.0));
 				if(b.exact) {
 					code = b.lo;
-					if(!errdiff) (void)prng_next(mult, carry);   // one draw per sample
-				}
-				else if(errdiff) {
-					double err;
-					if(b.d_hi <= b.d_lo) { err = -b.d_hi; code = b.hi; }
-					else { err = b.d_lo; code = b.lo; }
-					// scatter the error (src/imagew-main.c:545-566)
-					if(x - f >= 0 && x - f < W) {
-						if(x - 2 * f >= 0 && x - 2 * f < W) {
-							e1[x - 2 * f] = dadd(e1[x - 2 * f], dmul(err, c[2]));
-							e2[x - 2 * f] = dadd(e2[x - 2 * f], dmul(err, c[7]));
-						}
-						e1[x - f] = dadd(e1[x - f], dmul(err, c[3]));
-						e2[x - f] = dadd(e2[x - f], dmul(err, c[8]));
-					}
-					e1[x] = dadd(e1[x], dmul(err, c[4]));
-					e2[x] = dadd(e2[x], dmul(err, c[9]));
-					if(x + f >= 0 && x + f < W) {
-						e0[x + f] = dadd(e0[x + f], dmul(err, c[0]));
-						e1[x + f] = dadd(e1[x + f], dmul(err, c[5]));
-						e2[x + f] = dadd(e2[x + f], dmul(err, c[10]));
-						if(x + 2 * f >= 0 && x + 2 * f < W) {
-							e0[x + 2 * f] = dadd(e0[x + 2 * f], dmul(err, c[1]));
-							e1[x + 2 * f] = dadd(e1[x + 2 * f], dmul(err, c[6]));
-							e2[x + 2 * f] = dadd(e2[x + 2 * f], dmul(err, c[11]));
-						}
-					}
+					(void)prng_next(mult, carry);   // one draw per sample
 				}
 				else {
 					double fr = ddiv(b.d_lo, dadd(b.d_lo, b.d_hi));
@@ -286,31 +458,26 @@ __device__ void scan_channel(const Job &J, int oc)
 			}
 			store_code(J, oc, x, y, (unsigned int)code);
 		}
-		if(errdiff) {
-			for(int x = 0; x < W; x++) {
-				e0[x] = e1[x];
-				e1[x] = e2[x];
-				e2[x] = 0.0;
-			}
-		}
 	}
 }
 
-// One warp per output channel; lane 0 of the warp of each scanned channel
-// walks it.
+// One warp per output channel of the image.
+__device__ __forceinline__ void scan_warp(const Job &J, int oc)
+{
+	if(oc >= J.out_n || !J.outc[oc].scan) return;
+	if(J.outc[oc].q.dfam == IW_DITHERFAMILY_ERRDIFF) errdiff_warp(J, oc);
+	else random_warp(J, oc);
+}
+
 __global__ void k_scan(Job J)
 {
-	const int oc = threadIdx.x >> 5;
-	if((threadIdx.x & 31) != 0 || oc >= J.out_n || !J.outc[oc].scan) return;
-	scan_channel(J, oc);
+	scan_warp(J, threadIdx.x >> 5);
 }
 
 // Negation and blackening of fully transparent pixels, for outputs whose
 // channels were (partly) quantised by the serial scan.
-__global__ void k_finalize(Job J)
+__device__ __forceinline__ void finalize_at(const Job &J, int i, int j)
 {
-	int i = blockIdx.x * blockDim.x + threadIdx.x;
-	int j = blockIdx.y;
 	if(i >= J.out_w || j >= J.out_h) return;
 	int alpha_oc = -1;
 	for(int oc = 0; oc < J.out_n; oc++) if(J.outc[oc].ctype == IW_CHANNELTYPE_ALPHA) alpha_oc = oc;
@@ -322,6 +489,56 @@ __global__ void k_finalize(Job J)
 		if(clear) c = 0;
 		store_code(J, oc, i, j, c);
 	}
+}
+
+__global__ void k_finalize(Job J)
+{
+	finalize_at(J, blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y);
+}
+
+// ---- the plain form for a batch: jobs in device memory, block -> image by a
+// prefix table of per-image block counts ----
+
+__device__ __forceinline__ int find_job(const int *start, int n, int b)
+{
+	int lo = 0, hi = n - 1;
+	while(lo < hi) {
+		const int mid = (lo + hi + 1) >> 1;
+		if(__ldg(start + mid) <= b) lo = mid; else hi = mid - 1;
+	}
+	return lo;
+}
+
+__global__ void kb_vpass_exact(const Job *jobs, const int *start, int n)
+{
+	const int g = find_job(start, n, blockIdx.x);
+	const Job &J = jobs[g];
+	const int local = blockIdx.x - start[g], gx = (J.mid_w + blockDim.x - 1) / blockDim.x;
+	vpass_exact_at(J, (local % gx) * blockDim.x + threadIdx.x, local / gx);
+}
+
+__global__ void kb_hpass_exact(const Job *jobs, const int *start, int n)
+{
+	const int g = find_job(start, n, blockIdx.x);
+	const Job &J = jobs[g];
+	const int local = blockIdx.x - start[g], gx = (J.out_w + blockDim.x - 1) / blockDim.x;
+	hpass_exact_at(J, (local % gx) * blockDim.x + threadIdx.x, local / gx);
+}
+
+// one block per image, one warp per output channel
+__global__ void kb_scan(const Job *jobs)
+{
+	const Job &J = jobs[blockIdx.x];
+	if(J.any_scan) scan_warp(J, threadIdx.x >> 5);
+}
+
+__global__ void kb_finalize(const Job *jobs, const int *start, int n)
+{
+	const int g = find_job(start, n, blockIdx.x);
+	const Job &J = jobs[g];
+	if(!J.any_scan || !(J.negate || J.blacken)) return;
+	const int local = blockIdx.x - start[g], gx = (J.out_w + blockDim.x - 1) / blockDim.x;
+	finalize_at(J, (local % gx) * blockDim.x + threadIdx.x, local / gx);
 }
 
 // Position of the r-th set bit of 'mask' (r counts from 0).
@@ -465,6 +682,188 @@ struct DevBuf {
 	}
 };
 
+// ---- host <-> device transfers through pinned staging ----
+//
+// A kernel reading the caller's pageable buffer directly (zero copy) is fast
+// once the device has touched those pages, but the first touch of fresh pages
+// costs a translation per page.  Staging copies instead: host threads copy the
+// caller's bytes into one half of a pinned buffer while the copy engine moves
+// the other half, so neither waits for page pinning or page faults.
+
+// A fixed set of host threads for parallel memcpy.
+struct HostPool {
+	std::mutex run_mu;   // one run at a time (callers on different lanes take turns)
+	std::mutex mu;
+	std::condition_variable cv, cv_done;
+	std::vector<std::thread> th;
+	std::function<void(int)> task;
+	int ntask = 0, next = 0, pending = 0;
+	unsigned gen = 0;
+	bool stop = false;
+	HostPool()
+	{
+		int n = (int)std::thread::hardware_concurrency();
+		n = std::max(1, std::min(n, 32)) - 1;
+		for(int k = 0; k < n; k++) th.emplace_back([this] { loop(); });
+	}
+	void loop()
+	{
+		unsigned seen = 0;
+		for(;;) {
+			std::unique_lock<std::mutex> lk(mu);
+			cv.wait(lk, [&] { return stop || gen != seen; });
+			if(stop) return;
+			seen = gen;
+			while(next < ntask) {
+				const int t = next++;
+				lk.unlock();
+				task(t);
+				lk.lock();
+				if(--pending == 0) cv_done.notify_all();
+			}
+		}
+	}
+	// Runs fn(0..n-1) on the pool and the calling thread; returns when all are done.
+	void run(int n, const std::function<void(int)> &fn)
+	{
+		if(n <= 0) return;
+		std::lock_guard<std::mutex> one(run_mu);
+		std::unique_lock<std::mutex> lk(mu);
+		task = fn;
+		ntask = n;
+		next = 0;
+		pending = n;
+		gen++;
+		cv.notify_all();
+		while(next < ntask) {
+			const int t = next++;
+			lk.unlock();
+			fn(t);
+			lk.lock();
+			if(--pending == 0) cv_done.notify_all();
+		}
+		cv_done.wait(lk, [&] { return pending == 0; });
+	}
+};
+
+HostPool &host_pool()
+{
+	static HostPool *p = new HostPool();   // never destroyed
+	return *p;
+}
+
+struct Piece { uint8_t *dst; const uint8_t *src; size_t n; };
+
+// memcpy of many pieces, split in 1 MiB parts over the host pool.
+void copy_pieces(const std::vector<Piece> &pieces)
+{
+	constexpr size_t kPart = (size_t)1 << 20;
+	std::vector<Piece> parts;
+	size_t total = 0;
+	for(const Piece &p : pieces)
+		for(size_t o = 0; o < p.n; o += kPart) {
+			parts.push_back({p.dst + o, p.src + o, std::min(kPart, p.n - o)});
+			total += std::min(kPart, p.n - o);
+		}
+	if(total < ((size_t)2 << 20)) {
+		for(const Piece &p : parts) memcpy(p.dst, p.src, p.n);
+		return;
+	}
+	host_pool().run((int)parts.size(), [&](int k) { memcpy(parts[k].dst, parts[k].src, parts[k].n); });
+}
+
+struct Xfer { uint8_t *dev; uint8_t *host; size_t n; };
+
+struct Stager {
+	uint8_t *pin[2] = {nullptr, nullptr};
+	size_t half = 0;
+	cudaEvent_t ev[2] = {nullptr, nullptr};
+	bool ensure()
+	{
+		if(pin[0]) return true;
+		const size_t want = (size_t)64 << 20;
+		if(cudaMallocHost((void **)&pin[0], 2 * want) != cudaSuccess) { pin[0] = nullptr; return false; }
+		pin[1] = pin[0] + want;
+		half = want;
+		cudaEventCreateWithFlags(&ev[0], cudaEventDisableTiming);
+		cudaEventCreateWithFlags(&ev[1], cudaEventDisableTiming);
+		return true;
+	}
+};
+
+// Host -> device for every item, on 'st'.  Returns once the host side is
+// done; the last copies may still be in flight on the stream.
+bool stage_h2d(Stager &G, cudaStream_t st, const std::vector<Xfer> &items)
+{
+	if(!G.ensure()) return false;
+	int slot = 0;
+	size_t fill = 0;
+	std::vector<Piece> host_side;
+	std::vector<Xfer> dma;
+	auto flush = [&]() {
+		if(!fill) return;
+		copy_pieces(host_side);
+		for(const Xfer &x : dma) cudaMemcpyAsync(x.dev, x.host, x.n, cudaMemcpyHostToDevice, st);
+		cudaEventRecord(G.ev[slot], st);
+		host_side.clear();
+		dma.clear();
+		fill = 0;
+		slot ^= 1;
+		cudaEventSynchronize(G.ev[slot]);   // the other half is free again
+	};
+	cudaEventSynchronize(G.ev[0]);
+	for(const Xfer &x : items) {
+		size_t off = 0;
+		while(off < x.n) {
+			const size_t take = std::min(G.half - fill, x.n - off);
+			host_side.push_back({G.pin[slot] + fill, x.host + off, take});
+			dma.push_back({x.dev + off, G.pin[slot] + fill, take});
+			fill += take;
+			off += take;
+			if(fill == G.half) flush();
+		}
+	}
+	flush();
+	return true;
+}
+
+// Device -> host for every item after the work queued on 'st'; returns when
+// the bytes are in the callers' buffers.
+bool stage_d2h(Stager &G, cudaStream_t st, const std::vector<Xfer> &items)
+{
+	if(!G.ensure()) return false;
+	struct Group { std::vector<Piece> out; std::vector<Xfer> dma; };
+	std::vector<Group> groups(1);
+	size_t fill = 0;
+	for(const Xfer &x : items) {
+		size_t off = 0;
+		while(off < x.n) {
+			if(fill == G.half) { groups.emplace_back(); fill = 0; }
+			const size_t take = std::min(G.half - fill, x.n - off);
+			// pin offsets are relative; the half is chosen when the group is issued
+			groups.back().dma.push_back({x.dev + off, (uint8_t *)(uintptr_t)fill, take});
+			groups.back().out.push_back({x.host + off, (const uint8_t *)(uintptr_t)fill, take});
+			fill += take;
+			off += take;
+		}
+	}
+	auto issue = [&](size_t g) {
+		uint8_t *pin = G.pin[g & 1];
+		for(const Xfer &x : groups[g].dma)
+			cudaMemcpyAsync(pin + (uintptr_t)x.host, x.dev, x.n, cudaMemcpyDeviceToHost, st);
+		cudaEventRecord(G.ev[g & 1], st);
+	};
+	for(size_t g = 0; g < groups.size() && g < 2; g++) issue(g);
+	for(size_t g = 0; g < groups.size(); g++) {
+		if(cudaEventSynchronize(G.ev[g & 1]) != cudaSuccess) return false;
+		std::vector<Piece> out = groups[g].out;
+		for(Piece &p : out) p.src = G.pin[g & 1] + (uintptr_t)p.src;
+		copy_pieces(out);
+		if(g + 2 < groups.size()) issue(g + 2);
+	}
+	return true;
+}
+
 // Per-process device state: one stream, grow-only buffers and a cache of
 // device copies of the shared host tables.  Calls are serialised on it.
 struct DeviceState {
@@ -478,12 +877,16 @@ struct DeviceState {
 	DevBuf batch_io, batch_tab;   // batches: buffers + tables of all images
 	std::map<const void *, std::pair<std::shared_ptr<const void>, void *>> table_cache;
 	std::vector<uint8_t> staging;
+	Stager stager;
 };
 
-DeviceState &state()
+// Lanes: independent device states (stream, buffers, table cache), so that a
+// request server can keep a lane of long serial work (dither scans) apart
+// from its batches.  Lane 0 serves the public entry points.
+DeviceState &state(int lane = 0)
 {
-	static DeviceState *s = new DeviceState();   // never destroyed: outlives other statics
-	return *s;
+	static DeviceState *s[2] = {new DeviceState(), new DeviceState()};   // never destroyed: outlive other statics
+	return *s[lane & 1];
 }
 
 bool ensure_init(DeviceState &S, std::string &err)
@@ -539,6 +942,23 @@ struct Fixup { size_t off; const void **slot; };
 
 template<class Mark>
 int plain_launch(cudaStream_t st, const Plan &P, const Job &J, Mark mark);
+
+// Transfer mode of a context: "gpu:upload" = "copy" (cudaMemcpy from / to the
+// caller's pageable buffers, the default: fastest measured on Grace), "stage"
+// (pinned staging with host copy threads) or "zero" (kernels read and write
+// the caller's host buffers in place; needs pageable memory access, and is
+// slow on the first touch of fresh pages).  'resident' runs need the input
+// on the device.
+enum { UP_ZERO = 0, UP_COPY = 1, UP_STAGE = 2 };
+static int upload_mode(iw_context *ctx, const DeviceState &S, bool resident)
+{
+	const char *u = get_option(ctx, "gpu:upload");
+	int m = UP_COPY;
+	if(u && !strcmp(u, "stage")) m = UP_STAGE;
+	else if(u && !strcmp(u, "zero")) m = UP_ZERO;
+	if(m == UP_ZERO && (!S.pageable || resident)) m = UP_COPY;
+	return m;
+}
 
 // Fills the device job description of a planned image: geometry, flags and
 // the tables (weights packed into 'pk' with fix-ups for their device
@@ -663,9 +1083,9 @@ static bool make_job(iw_context *ctx, const Plan &P, DeviceState &S, Packer &pk,
 	return true;
 }
 
-bool run_pipeline(iw_context *ctx, Plan &P, int warmup, int iters)
+bool run_pipeline(iw_context *ctx, Plan &P, int warmup, int iters, int lane)
 {
-	DeviceState &S = state();
+	DeviceState &S = state(lane);
 	std::lock_guard<std::mutex> lk(S.mu);
 	std::string err;
 	if(!ensure_init(S, err)) {
@@ -691,8 +1111,8 @@ bool run_pipeline(iw_context *ctx, Plan &P, int warmup, int iters)
 	// (cudaDevAttrPageableMemoryAccess), the kernels read the caller's input
 	// image and write the output image in place, over the CPU-GPU link, instead
 	// of staging copies.  Timed runs keep the input resident in device memory.
-	const char *upl = get_option(ctx, "gpu:upload");
-	const bool zero_copy = S.pageable && !(upl && !strcmp(upl, "copy")) && warmup == 0 && iters <= 1;
+	const int upmode = upload_mode(ctx, S, warmup > 0 || iters > 1);
+	const bool zero_copy = upmode == UP_ZERO;
 	const size_t interm_bytes = (size_t)P.mid_n * J.interm_plane * sizeof(float);
 	const size_t out_bytes = P.out_bpr * (size_t)P.out_h;
 	if((!zero_copy && (!S.in.ensure(in_bytes ? in_bytes : 16) || !S.out.ensure(out_bytes))) ||
@@ -702,7 +1122,7 @@ bool run_pipeline(iw_context *ctx, Plan &P, int warmup, int iters)
 	}
 	if(any_scan) {
 		if(!S.scan.ensure((size_t)P.out_n * P.out_w * P.out_h * sizeof(double)) ||
-			!S.err.ensure((size_t)P.out_n * 3 * P.out_w * sizeof(double))) {
+			!S.err.ensure((size_t)P.out_n * 5 * P.out_w * sizeof(double))) {
 			iw_set_error(ctx, "Out of GPU memory");
 			return false;
 		}
@@ -717,7 +1137,12 @@ bool run_pipeline(iw_context *ctx, Plan &P, int warmup, int iters)
 
 	cudaStream_t st = S.stream;
 	cudaMemcpyAsync(S.params.p, S.staging.data(), S.staging.size(), cudaMemcpyHostToDevice, st);
-	if(!zero_copy) cudaMemcpyAsync(S.in.p, ctx->img1.pixels, in_bytes, cudaMemcpyHostToDevice, st);
+	if(upmode == UP_COPY) cudaMemcpyAsync(S.in.p, ctx->img1.pixels, in_bytes, cudaMemcpyHostToDevice, st);
+	if(upmode == UP_STAGE &&
+		!stage_h2d(S.stager, st, {Xfer{(uint8_t *)S.in.p, (uint8_t *)ctx->img1.pixels, in_bytes}})) {
+		iw_set_error(ctx, "Out of pinned host memory");
+		return false;
+	}
 
 	const char *prec = get_option(ctx, "gpu:precision");
 	bool want_plain = prec && !strcmp(prec, "fp64");
@@ -752,7 +1177,8 @@ bool run_pipeline(iw_context *ctx, Plan &P, int warmup, int iters)
 		if(timed) marks_per_it = (int)(ev.size() - before);
 		launches = l;
 	}
-	if(!zero_copy) cudaMemcpyAsync(ctx->img2.pixels, S.out.p, out_bytes, cudaMemcpyDeviceToHost, st);
+	if(upmode == UP_COPY) cudaMemcpyAsync(ctx->img2.pixels, S.out.p, out_bytes, cudaMemcpyDeviceToHost, st);
+	if(upmode == UP_STAGE) stage_d2h(S.stager, st, {Xfer{(uint8_t *)S.out.p, (uint8_t *)ctx->img2.pixels, out_bytes}});
 	cudaError_t ce = cudaStreamSynchronize(st);
 	if(ce == cudaSuccess) ce = cudaGetLastError();
 	ctx->stats.flagged = 0;
@@ -793,9 +1219,9 @@ bool run_pipeline(iw_context *ctx, Plan &P, int warmup, int iters)
 // status[i]: 1 done here, 0 left for the caller (run it alone), -1 failed
 // (error set on the context).  'dev_ms' receives the batch's device time.
 bool run_batch(const std::vector<iw_context *> &ctxs, const std::vector<Plan *> &plans, std::vector<int> &status,
-	double &dev_ms)
+	double &dev_ms, int lane)
 {
-	DeviceState &S = state();
+	DeviceState &S = state(lane);
 	std::lock_guard<std::mutex> lk(S.mu);
 	const int n = (int)ctxs.size();
 	status.assign(n, 0);
@@ -821,12 +1247,9 @@ bool run_batch(const std::vector<iw_context *> &ctxs, const std::vector<Plan *> 
 	}
 	if(sel.empty()) return true;
 
-	// zero copy where the device reads pageable host memory (as run_pipeline)
-	bool zc = S.pageable != 0;
-	for(int i : sel) {
-		const char *upl = get_option(ctxs[i], "gpu:upload");
-		if(upl && !strcmp(upl, "copy")) zc = false;
-	}
+	// one transfer mode for the batch: the first image's (as run_pipeline)
+	const int upmode = upload_mode(ctxs[sel[0]], S, false);
+	const bool zc = upmode == UP_ZERO;
 	// buffers of every image, the packed weight lists and the flag list in one block
 	size_t top = 0;
 	auto take = [&](size_t bytes) { size_t at = (top + 255) & ~(size_t)255; top = at + bytes; return at; };
@@ -914,11 +1337,19 @@ bool run_batch(const std::vector<iw_context *> &ctxs, const std::vector<Plan *> 
 	cudaEventCreate(&e1);
 	cudaMemcpyAsync(base + o_par, S.staging.data(), S.staging.size(), cudaMemcpyHostToDevice, st);
 	cudaMemcpyAsync(tbase, tab.data(), tab.size(), cudaMemcpyHostToDevice, st);
-	if(!zc)
+	if(upmode == UP_COPY)
 		for(int k = 0; k < m; k++) {
 			const int i = item_img[k];
 			cudaMemcpyAsync(base + o_in[i], ctxs[i]->img1.pixels, in_bytes[i], cudaMemcpyHostToDevice, st);
 		}
+	if(upmode == UP_STAGE) {
+		std::vector<Xfer> xs;
+		for(int k = 0; k < m; k++) {
+			const int i = item_img[k];
+			xs.push_back({base + o_in[i], (uint8_t *)ctxs[i]->img1.pixels, in_bytes[i]});
+		}
+		if(!stage_h2d(S.stager, st, xs)) return fail_all("Out of pinned host memory");
+	}
 	cudaMemsetAsync(flag_count, 0, sizeof(int), st);
 	cudaEventRecord(e0, st);
 	int launches = fast_launch_batch(st, items.data(), m, err);
@@ -927,11 +1358,19 @@ bool run_batch(const std::vector<iw_context *> &ctxs, const std::vector<Plan *> 
 		launches++;
 	}
 	cudaEventRecord(e1, st);
-	if(!zc)
+	if(upmode == UP_COPY)
 		for(int k = 0; k < m; k++) {
 			const int i = item_img[k];
 			cudaMemcpyAsync(ctxs[i]->img2.pixels, base + o_out[i], out_bytes[i], cudaMemcpyDeviceToHost, st);
 		}
+	if(upmode == UP_STAGE) {
+		std::vector<Xfer> xs;
+		for(int k = 0; k < m; k++) {
+			const int i = item_img[k];
+			xs.push_back({base + o_out[i], (uint8_t *)ctxs[i]->img2.pixels, out_bytes[i]});
+		}
+		stage_d2h(S.stager, st, xs);
+	}
 	cudaError_t ce = cudaStreamSynchronize(st);
 	if(ce == cudaSuccess) ce = cudaGetLastError();
 	int nflagged = 0;
@@ -955,6 +1394,155 @@ bool run_batch(const std::vector<iw_context *> &ctxs, const std::vector<Plan *> 
 		ctx->stats.flagged = nflagged;
 		status[item_img[k]] = 1;
 		fast_item_free(items[k]);
+	}
+	return true;
+}
+
+// A batch in the plain (FP64) form: every image runs the reference's
+// arithmetic through batched launches of the plain kernels, and the serial
+// dither scans of all images run at once, one warp per channel.  For images
+// the fast form does not take (error-diffusion / random dither, fp64
+// requests, ...).  status / dev_ms as run_batch.
+bool run_batch_plain(const std::vector<iw_context *> &ctxs, const std::vector<Plan *> &plans, std::vector<int> &status,
+	double &dev_ms, int lane)
+{
+	DeviceState &S = state(lane);
+	std::lock_guard<std::mutex> lk(S.mu);
+	const int n = (int)ctxs.size();
+	status.assign(n, 0);
+	dev_ms = 0;
+	std::string err;
+	if(!ensure_init(S, err)) {
+		for(int i = 0; i < n; i++) { iw_set_error(ctxs[i], err.c_str()); status[i] = -1; }
+		return false;
+	}
+	std::vector<Job> jobs(n);
+	std::vector<std::vector<Fixup>> fixes(n);
+	Packer pk(S.staging);
+	std::vector<int> sel;
+	for(int i = 0; i < n; i++) {
+		if(!make_job(ctxs[i], *plans[i], S, pk, fixes[i], jobs[i])) { status[i] = -1; continue; }
+		sel.push_back(i);
+	}
+	if(sel.empty()) return true;
+	const int upmode = upload_mode(ctxs[sel[0]], S, false);
+	const bool zc = upmode == UP_ZERO;
+	size_t top = 0;
+	auto take = [&](size_t bytes) { size_t at = (top + 255) & ~(size_t)255; top = at + bytes; return at; };
+	const size_t o_par = take(S.staging.size());
+	std::vector<size_t> o_in(n, 0), o_mid(n, 0), o_out(n, 0), o_scan(n, 0), o_err(n, 0), in_bytes(n, 0), out_bytes(n, 0);
+	for(int i : sel) {
+		const Plan &P = *plans[i];
+		in_bytes[i] = P.in_bpr * (size_t)(P.orient >= 4 ? P.img1_w : P.img1_h);
+		out_bytes[i] = P.out_bpr * (size_t)P.out_h;
+		if(!zc) o_in[i] = take(in_bytes[i] ? in_bytes[i] : 16);
+		o_mid[i] = take((size_t)P.mid_n * jobs[i].interm_plane * sizeof(float));
+		if(!zc) o_out[i] = take(out_bytes[i]);
+		if(jobs[i].any_scan) {
+			o_scan[i] = take((size_t)P.out_n * P.out_w * P.out_h * sizeof(double));
+			o_err[i] = take((size_t)P.out_n * 5 * P.out_w * sizeof(double));
+		}
+	}
+	if(!S.batch_io.ensure(top)) {
+		for(int i : sel) { iw_set_error(ctxs[i], "Out of GPU memory (batch)"); status[i] = -1; }
+		return false;
+	}
+	uint8_t *base = (uint8_t *)S.batch_io.p;
+	std::vector<int> run;
+	for(int i : sel) {
+		iw_context *ctx = ctxs[i];
+		const Plan &P = *plans[i];
+		Job &J = jobs[i];
+		for(const Fixup &f : fixes[i]) *f.slot = base + o_par + f.off;
+		ctx->img2.bpr = P.out_bpr;
+		ctx->img2.pixels = (iw_byte *)iw_malloc_large(ctx, P.out_bpr, P.out_h);
+		if(!ctx->img2.pixels) { status[i] = -1; continue; }
+		J.in = zc ? (const uint8_t *)ctx->img1.pixels : base + o_in[i];
+		J.interm = (float *)(base + o_mid[i]);
+		J.out = zc ? (uint8_t *)ctx->img2.pixels : base + o_out[i];
+		if(J.any_scan) {
+			J.scanbuf = (double *)(base + o_scan[i]);
+			J.errbuf = (double *)(base + o_err[i]);
+		}
+		run.push_back(i);
+	}
+	if(run.empty()) return true;
+	const int m = (int)run.size();
+	// job array and block tables
+	std::vector<Job> djobs(m);
+	std::vector<int> sv(m), sh(m);
+	long long bv = 0, bh = 0;
+	int maxch = 1;
+	for(int k = 0; k < m; k++) {
+		const Job &J = jobs[run[k]];
+		djobs[k] = J;
+		sv[k] = (int)bv;
+		sh[k] = (int)bh;
+		bv += (long long)((J.mid_w + 127) / 128) * J.mid_h;
+		bh += (long long)((J.out_w + 127) / 128) * J.out_h;
+		maxch = std::max(maxch, J.out_n);
+	}
+	auto fail_all = [&](const char *msg) {
+		for(int i : run) { iw_set_error(ctxs[i], msg); status[i] = -1; }
+		return false;
+	};
+	if(bv > 0x7fffffffLL || bh > 0x7fffffffLL) return fail_all("batch: too many blocks in one launch");
+	std::vector<uint8_t> tab;
+	auto add = [&](const void *p, size_t bytes) {
+		size_t at = (tab.size() + 255) & ~(size_t)255;
+		tab.resize(at + bytes);
+		if(bytes) memcpy(tab.data() + at, p, bytes);
+		return at;
+	};
+	const size_t o_jobs = add(djobs.data(), djobs.size() * sizeof(Job));
+	const size_t o_sv = add(sv.data(), sv.size() * sizeof(int)), o_sh = add(sh.data(), sh.size() * sizeof(int));
+	if(!S.batch_tab.ensure(tab.size())) return fail_all("Out of GPU memory (batch tables)");
+	uint8_t *tbase = (uint8_t *)S.batch_tab.p;
+	const Job *dj = (const Job *)(tbase + o_jobs);
+	const int *dsv = (const int *)(tbase + o_sv), *dsh = (const int *)(tbase + o_sh);
+
+	cudaStream_t st = S.stream;
+	cudaEvent_t e0, e1;
+	cudaEventCreate(&e0);
+	cudaEventCreate(&e1);
+	cudaMemcpyAsync(base + o_par, S.staging.data(), S.staging.size(), cudaMemcpyHostToDevice, st);
+	cudaMemcpyAsync(tbase, tab.data(), tab.size(), cudaMemcpyHostToDevice, st);
+	std::vector<Xfer> xin, xout;
+	for(int i : run) {
+		xin.push_back({base + o_in[i], (uint8_t *)ctxs[i]->img1.pixels, in_bytes[i]});
+		xout.push_back({base + o_out[i], (uint8_t *)ctxs[i]->img2.pixels, out_bytes[i]});
+	}
+	if(upmode == UP_COPY)
+		for(const Xfer &x : xin) cudaMemcpyAsync(x.dev, x.host, x.n, cudaMemcpyHostToDevice, st);
+	if(upmode == UP_STAGE && !stage_h2d(S.stager, st, xin)) return fail_all("Out of pinned host memory");
+	cudaEventRecord(e0, st);
+	kb_vpass_exact<<<(unsigned)bv, 128, 0, st>>>(dj, dsv, m);
+	kb_hpass_exact<<<(unsigned)bh, 128, 0, st>>>(dj, dsh, m);
+	kb_scan<<<m, 32 * maxch, 0, st>>>(dj);
+	kb_finalize<<<(unsigned)bh, 128, 0, st>>>(dj, dsh, m);
+	cudaEventRecord(e1, st);
+	if(upmode == UP_COPY)
+		for(const Xfer &x : xout) cudaMemcpyAsync(x.host, x.dev, x.n, cudaMemcpyDeviceToHost, st);
+	if(upmode == UP_STAGE) stage_d2h(S.stager, st, xout);
+	cudaError_t ce = cudaStreamSynchronize(st);
+	if(ce == cudaSuccess) ce = cudaGetLastError();
+	float ms = 0;
+	if(ce == cudaSuccess) cudaEventElapsedTime(&ms, e0, e1);
+	cudaEventDestroy(e0);
+	cudaEventDestroy(e1);
+	if(ce != cudaSuccess) {
+		std::string msg = std::string("CUDA error: ") + cudaGetErrorString(ce);
+		return fail_all(msg.c_str());
+	}
+	dev_ms = ms;
+	for(int i : run) {
+		iw_context *ctx = ctxs[i];
+		ctx->stats.form = 0;
+		ctx->stats.zero_copy = zc;
+		ctx->stats.kernels = 4;
+		ctx->stats.ms_device = ms;
+		ctx->stats.flagged = 0;
+		status[i] = 1;
 	}
 	return true;
 }

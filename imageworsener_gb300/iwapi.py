@@ -297,3 +297,56 @@ def run_batch(lib: IWLib, jobs: Sequence[Job]) -> list[Result]:
     finally:
         for ctx in ctxs:
             lib.iw_destroy_context(ctx)
+
+
+class Completion(C.Structure):
+    _fields_ = [("tag", C.c_ulonglong), ("ok", C.c_int), ("latency_ms", C.c_double)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("in_flight", C.c_int), ("queued", C.c_int), ("batches", C.c_longlong),
+                ("batched_requests", C.c_longlong), ("device_ms", C.c_double), ("slow_batches", C.c_longlong),
+                ("slow_requests", C.c_longlong), ("slow_device_ms", C.c_double)]
+
+
+def server_api(lib: IWLib):
+    """ctypes signatures of the iwg_server_* entry points."""
+    d = lib.dll
+    d.iwg_server_create.restype = C.c_void_p
+    d.iwg_server_create.argtypes = [C.c_size_t, C.c_int, C.c_int]
+    d.iwg_server_submit.restype = C.c_int
+    d.iwg_server_submit.argtypes = [C.c_void_p, C.c_void_p, C.c_ulonglong]
+    d.iwg_server_poll.restype = C.c_int
+    d.iwg_server_poll.argtypes = [C.c_void_p, C.POINTER(Completion), C.c_int, C.c_int]
+    d.iwg_server_destroy.restype = None
+    d.iwg_server_destroy.argtypes = [C.c_void_p]
+    d.iwg_server_info.restype = C.c_int
+    d.iwg_server_info.argtypes = [C.c_void_p, C.POINTER(ServerStats)]
+    return d
+
+
+def run_served(lib: IWLib, jobs: Sequence[Job], budget: int = 0, max_batch: int = 0) -> list[Result]:
+    """Submit every job to one iwg_server, collect the completions."""
+    d = server_api(lib)
+    srv = d.iwg_server_create(budget, max_batch, 0)
+    ctxs = []
+    try:
+        for k, job in enumerate(jobs):
+            ctx = lib.iw_create_context(None)
+            ctxs.append(ctx)
+            _setup(lib, ctx, job)
+            d.iwg_server_submit(srv, ctx, k)
+        got = {}
+        buf = (Completion * 64)()
+        while len(got) < len(jobs):
+            n = d.iwg_server_poll(srv, buf, 64, 10000)
+            if n == 0:
+                raise TimeoutError("server returned no completion within 10 s")
+            for i in range(n):
+                got[buf[i].tag] = buf[i].ok
+        return [_collect(lib, ctxs[k], bool(got[k]), []) for k in range(len(jobs))]
+    finally:
+        d.iwg_server_destroy(srv)
+        for ctx in ctxs:
+            lib.iw_destroy_context(ctx)
+

@@ -189,6 +189,45 @@ def batch(count: int, seed: int = 4, box: int = 256, max_side: int = 2048) -> li
     return jobs
 
 
+# 4:3 input sizes 160x120 .. 1024x768 (log-spaced widths)
+_UPWIDTHS = [int(round(160 * 2 ** (k / 16))) // 4 * 4 for k in range(43)]
+
+
+def upscale_pool(count: int, seed: int = 6) -> list[Job]:
+    """Serving-mix upscales: 4:3 inputs 160x120..1024x768, RGB or RGBA 8-bit,
+    enlarged 2-4x with Catmull-Rom (cubic B=0, C=0.5)."""
+    jobs = []
+    u = uniform(seed, 80, (count, 4))
+    widths = [w for w in _UPWIDTHS if w <= 1024]
+    for k in range(count):
+        w = widths[int(u[k, 0] * len(widths))]
+        h = w * 3 // 4
+        imgtype = (IMGTYPE_RGB, IMGTYPE_RGBA)[int(u[k, 1] * 2)]
+        factor = 2.0 + 2.0 * u[k, 2]
+        ow, oh = int(w * factor), int(h * factor)
+        nch = 3 if imgtype == IMGTYPE_RGB else 4
+        yy, xx = np.mgrid[0:h, 0:w].astype(np.float64)
+        base = (xx / max(w - 1, 1))[..., None] * np.linspace(0.3, 0.9, nch)[None, None, :] + \
+            (yy / max(h - 1, 1))[..., None] * np.linspace(0.7, 0.2, nch)[None, None, :]
+        noise = uniform(seed, 2000 + k, (h, w, nch)) * 0.1
+        px = np.clip(np.floor((0.5 * base + noise) * 255.0 + 0.5), 0, 255).astype(np.uint8).tobytes()
+        calls = [("iw_set_output_profile", PNG_PROFILE), ("iw_set_output_canvas_size", ow, oh)] + _resize("cubic", 0.0, 0.5)
+        jobs.append(Job(imgtype, 8, w, h, px, calls=calls))
+    return jobs
+
+
+def serving_schedule(rate: float, seconds: float, seed: int = 7) -> list[tuple[float, str, bool]]:
+    """Poisson arrivals: (time s, "thumb" | "up", error diffusion?) -- 70 %
+    thumbnails, 30 % upscales, 10 % of all requests with error diffusion."""
+    rng = np.random.default_rng(seed)
+    t, out = 0.0, []
+    while True:
+        t += rng.exponential(1.0 / rate)
+        if t >= seconds:
+            return out
+        out.append((t, "thumb" if rng.random() < 0.7 else "up", bool(rng.random() < 0.1)))
+
+
 def out_pixels(job: Job) -> int:
     """Output pixel count of a job (its canvas size)."""
     for c in job.calls:

@@ -65,6 +65,41 @@ IW_EXPORT(int) iwg_device_info(char *buf, int buflen);
  * (ms_device). */
 IW_EXPORT(int) iwg_process_batch(struct iw_context **ctxs, int n);
 
+/* ---- request server: continuous batching under a device-memory budget ----
+ * A server owns host threads that plan submitted contexts as they arrive, a
+ * dispatcher that runs every planned request fitting the budget as one batch
+ * (as iwg_process_batch) while the next requests are being planned, and
+ * threads that run the output post-pass.  Each request's output is exactly
+ * what iw_process_image() gives it alone.  The caller keeps ownership of the
+ * contexts: a context may be read or destroyed once its completion was polled. */
+struct iwg_server;
+struct iwg_completion {
+	unsigned long long tag;  /* as given to iwg_server_submit */
+	int ok;                  /* 1: processed; 0: failed (error set on the context) */
+	double latency_ms;       /* submit -> completion */
+};
+struct iwg_server_stats {
+	int in_flight;               /* submitted, completion not yet polled */
+	int queued;                  /* waiting for planning or for the GPU */
+	long long batches;           /* device batches run */
+	long long batched_requests;  /* requests in them */
+	double device_ms;            /* device time of the batched passes */
+	long long slow_batches;      /* of them on the lane for serial dither scans */
+	long long slow_requests;
+	double slow_device_ms;
+};
+/* device_budget: bytes of device memory one batch may hold (0: 8 GiB);
+ * max_batch: requests per batch (0: 4096); host_threads (0: all cores). */
+IW_EXPORT(struct iwg_server *) iwg_server_create(size_t device_budget, int max_batch, int host_threads);
+/* Queues a configured, unprocessed context.  Returns 1, or 0 if refused. */
+IW_EXPORT(int) iwg_server_submit(struct iwg_server *s, struct iw_context *ctx, unsigned long long tag);
+/* Moves up to max completions into out; waits up to wait_ms for the first
+ * (0: no wait, negative: until one completes).  Returns the number moved. */
+IW_EXPORT(int) iwg_server_poll(struct iwg_server *s, struct iwg_completion *out, int max, int wait_ms);
+IW_EXPORT(int) iwg_server_info(struct iwg_server *s, struct iwg_server_stats *out);
+/* Finishes every submitted request, then stops the server's threads. */
+IW_EXPORT(void) iwg_server_destroy(struct iwg_server *s);
+
 /* Resamples one 8-bit image without allocating any memory, host or device.
  * No counterpart in the reference: it is the iw_process_image() pixel path
  * (reference arithmetic, FP64 form, bit-identical output) narrowed to what a

@@ -9,7 +9,7 @@ the call) and contexts that fail.
 import pytest
 
 from conftest import load_workload_digests
-from imageworsener_gb300.iwapi import run_batch, run_job, Job, IMGTYPE_RGB, RT
+from imageworsener_gb300.iwapi import run_batch, run_job, run_served, Job, IMGTYPE_RGB, RT
 from imageworsener_gb300 import workloads as W
 import iwcases
 
@@ -63,3 +63,39 @@ def test_batch_repeat_is_stable(gpulib):
     a = run_batch(gpulib, jobs)
     b = run_batch(gpulib, jobs)
     assert [r.key() for r in a] == [r.key() for r in b]
+
+
+@pytest.mark.parametrize("mode", ["zero", "copy", "stage"])
+def test_transfer_modes_identical(gpulib, mode):
+    """Zero copy, cudaMemcpy and pinned staging give the same bytes, alone and batched."""
+    jobs = W.batch(12, seed=41, max_side=600)
+    opt = [("iw_set_option", b"gpu:upload", mode.encode())]
+    ref = [run_job(gpulib, j) for j in jobs]
+    for j in jobs:
+        j.calls = list(j.calls) + opt
+    lone = [run_job(gpulib, j) for j in jobs]
+    batched = run_batch(gpulib, jobs)
+    for a, b, c in zip(ref, lone, batched):
+        assert a.key() == b.key() == c.key()
+
+
+def test_server_mix_same_as_alone(gpulib):
+    """Requests served together (continuous batching, error diffusion on the
+    second lane) come out exactly as each does alone."""
+    jobs = W.batch(40, seed=51, max_side=800)
+    jobs += [iwcases.random_case(7000 + k) for k in range(30)]
+    for k in range(0, 40, 7):   # error diffusion on some thumbnails
+        jobs[k].calls = list(jobs[k].calls) + [("iw_set_dither_type", 10, 2, 0)]
+    lone = [run_job(gpulib, j) for j in jobs]
+    served = run_served(gpulib, jobs)
+    for k, (a, b) in enumerate(zip(lone, served)):
+        assert a.key() == b.key(), f"request {k}"
+
+
+def test_server_small_budget(gpulib):
+    """A budget smaller than one image still admits one request at a time."""
+    jobs = W.batch(10, seed=61, max_side=500)
+    lone = [run_job(gpulib, j) for j in jobs]
+    served = run_served(gpulib, jobs, budget=1 << 20, max_batch=3)
+    assert [r.key() for r in lone] == [r.key() for r in served]
+
