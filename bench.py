@@ -63,10 +63,15 @@ WORKLOADS = {
 
 class Stats(C.Structure):
     _fields_ = [("ms_total", C.c_double), ("ms_device", C.c_double), ("ms_part", C.c_double * 4),
-                ("flagged", C.c_longlong), ("form", C.c_int), ("kernels", C.c_int), ("zero_copy", C.c_int)]
+                ("flagged", C.c_longlong), ("form", C.c_int), ("kernels", C.c_int), ("zero_copy", C.c_int),
+                ("flagged_exact", C.c_longlong)]
 
 
 _T0 = time.perf_counter()
+
+# DRAM bytes (read + write) per launch of the vertical pass from one ncu
+# capture of this workload (profiles/ holds the capture summaries).
+ROOFLINE_TRAFFIC = {"precision": 182.4e6}
 
 
 def progress(msg: str) -> None:
@@ -295,7 +300,7 @@ def run_reference_arm(args, rank, world):
 
 
 def batch_leg(lib: IWLib, n_images: int, pool_size: int, cpu_threads: int, cpu_images: int,
-              modes=("copy", "stage", "zero")):
+              modes=("stage", "copy", "zero")):
     """The batched configuration: n_images contexts (image content drawn from a
     pool of pool_size generated images, sizes log-uniform 64..2048, gray/RGB/RGBA,
     8/16-bit, five filters, each fitted to a 256x256 box) through one
@@ -345,6 +350,8 @@ def batch_leg(lib: IWLib, n_images: int, pool_size: int, cpu_threads: int, cpu_i
     res = {"images": n_images, "pool": pool_size, "ok": ok, "output_px": out_px, "input_bytes": in_bytes,
            "e2e_mpix_s": out_px / 1e6 / wall, "wall_ms": 1000 * wall,
            "device_ms": st.ms_device, "device_mpix_s": out_px / 1e6 / (st.ms_device / 1000.0) if st.ms_device else None,
+           "last_chunk_ms": {"vertical": st.ms_part[0], "horizontal": st.ms_part[1], "fixup": st.ms_part[2]},
+           "last_chunk_flagged": st.flagged, "last_chunk_left_to_fp64": st.flagged_exact,
            "lone_mpix_s": pool_px / 1e6 / lone_dt,
            "identical_to_lone": digests == lone[:len(digests)], "transfer": modes[0], "by_transfer_mode": per_mode}
     if cpu_images > 0:
@@ -423,16 +430,17 @@ def serving_leg(lib: IWLib, rate: float, seconds: float, thumbs, ups):
     d.iwg_server_info(srv, C.byref(info))
     if drained:
         d.iwg_server_destroy(srv)   # (left running otherwise: the backlog did not drain in time)
-    ls = sorted(v[0] for v in lat.values())
+    snap = dict(lat)   # a snapshot: the poller may still be collecting if the backlog did not drain
+    ls = sorted(v[0] for v in snap.values())
     pct = lambda q: ls[min(len(ls) - 1, int(q * len(ls)))] if ls else None
-    done_px = sum(out_px[k] for k in lat)
+    done_px = sum(out_px[k] for k in snap)
 
     def cls(sel):
-        v = sorted(lat[k][0] for k in lat if sel(sched[k]))
+        v = sorted(snap[k][0] for k in snap if sel(sched[k]))
         return {"n": len(v), "p50_ms": v[len(v) // 2] if v else None,
                 "p99_ms": v[min(len(v) - 1, int(0.99 * len(v)))] if v else None}
-    return {"rate_req_s": rate, "seconds": seconds, "requests": len(sched), "completed": len(lat),
-            "failed": sum(1 for v in lat.values() if not v[1]),
+    return {"rate_req_s": rate, "seconds": seconds, "requests": len(sched), "completed": len(snap),
+            "failed": sum(1 for v in snap.values() if not v[1]),
             "errdiff_requests": sum(1 for x in sched if x[2]), "upscale_requests": sum(1 for x in sched if x[1] == "up"),
             "p50_ms": pct(0.50), "p90_ms": pct(0.90), "p99_ms": pct(0.99), "max_ms": ls[-1] if ls else None,
             "throughput_mpix_s": done_px / 1e6 / wall, "wall_s": wall, "submit_s": t_sub,
@@ -457,6 +465,7 @@ def main():
     ap.add_argument("--batch-pool", type=int, default=256, help="batched leg: distinct generated images")
     ap.add_argument("--serve-seconds", type=float, default=10.0, help="serving leg: length of the arrival stream (0: skip)")
     ap.add_argument("--serve-rate", type=float, default=2000.0, help="serving leg: requests per second")
+    ap.add_argument("--no-large", action="store_true", help="skip the large-downscale leg")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     rank, world, local = dist_env()
@@ -505,14 +514,14 @@ def main():
             progress("batched configuration")
             batched = batch_leg(lib, args.batch_images, min(args.batch_pool, args.batch_images),
                                 os.cpu_count() or 1, 0 if args.no_cpu_baseline else 64)
-        progress("large downscale")
         large = {}
-        for name in ("downscale", "downscale_fs4"):
+        for name in (() if args.no_large else ("downscale", "downscale_fs4")):
+            progress(f"large downscale: {name}")
             ljob = WORKLOADS[name]()
             lst, ldig = device_timed(lib, ljob, 1, 3, "fp32")
             large[name] = {"ms": lst.ms_device, "mpix_s": W.out_pixels(ljob) / 1e6 / (lst.ms_device / 1000.0),
                            "input_gb_s": len(ljob.pixels) / 1e9 / (lst.ms_device / 1000.0), "form": lst.form,
-                           "flagged": lst.flagged, "kernel_ms": list(lst.ms_part)[:3],
+                           "flagged": lst.flagged, "left_to_fp64": lst.flagged_exact, "kernel_ms": list(lst.ms_part)[:3],
                            "bit_exact": ldig == golden_digest(name)}
         serving = None
         if args.serve_seconds > 0:
@@ -536,9 +545,13 @@ def main():
     value = world * out_px / 1e6 / (ms / 1000.0)
     peak, peak_src = peaks()
     parts = list(st.ms_part)
-    dom = max(range(3), key=lambda k: parts[k])
-    names = ["vertical pass (k_vstream/k_vgather)", "horizontal pass + guarded quantisation (k_hpass_fast)",
-             "exact FP64 re-evaluation (k_fix_flagged_warp)"]
+    names = ["vertical pass (k_vbulk / k_vstream_px)", "horizontal pass + guarded quantisation (k_hpass_fast)",
+             "re-evaluation of flagged pixels, double-float then FP64 (k_fix_flagged_warp)"]
+    slowest = max(range(3), key=lambda k: parts[k])
+    # The roofline is reported for the vertical pass: it moves the compulsory
+    # bytes (the input image) and is the HBM-bound kernel of the pipeline.
+    # The re-evaluation has no compulsory traffic (FP64 / latency bound).
+    dom = 0
     # compulsory bytes of each launch group: vertical reads the input image;
     # horizontal writes the output image; the fix-up has no compulsory traffic.
     comp = [in_bytes, out_bytes, 0]
@@ -562,10 +575,12 @@ def main():
                 "last_call": e2e_zc, "by_transfer_mode": e2e_modes},
         "roofline": {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None, "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)",
-                     "traffic": None, "algorithmic_bytes_per_launch": comp[dom],
-                     "pipeline_GBps": (in_bytes + out_bytes) / (ms / 1000.0) / 1e9},
+                     "traffic": ROOFLINE_TRAFFIC.get(args.workload), "algorithmic_bytes_per_launch": comp[dom],
+                     "pipeline_GBps": (in_bytes + out_bytes) / (ms / 1000.0) / 1e9,
+                     "slowest_kernel": names[slowest], "slowest_share": parts[slowest] / sum(parts) if sum(parts) else None},
         "kernel_ms": {"vertical": parts[0], "horizontal": parts[1], "fixup": parts[2]},
         "flagged_pixels": st.flagged, "flagged_fraction": st.flagged / out_px,
+        "flagged_left_to_fp64": st.flagged_exact,
         "plain_fp64": {"value": world * out_px / 1e6 / (ms64 / 1000.0), "ms_per_step": ms64,
                        "kernel_ms": {"vertical": st64.ms_part[0], "horizontal": st64.ms_part[1]}},
         "speedup_vs_plain": ms64 / ms,

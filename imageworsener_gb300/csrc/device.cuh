@@ -86,7 +86,67 @@ struct Job {
 	double gsw[3];
 	int intclamp, negate, blacken;
 	int seed;
+
+	// double-float copies for the fast form's re-evaluation tier (null
+	// otherwise): decode table per intermediate channel, alpha table, and the
+	// weights of weight set 0 of each dimension, indexed like their CSR lists
+	const float2 *df_tab[kMaxCh];
+	const float2 *df_atab;
+	const float2 *df_wv, *df_wh;
 };
+
+// ---- double-float ("df") arithmetic ----
+// A value hi + lo of two floats with |lo| <= ulp(hi)/2: 48 significant bits
+// on the FP32 pipe.  Error-free transformations (Knuth's TwoSum, Dekker's
+// Fast2Sum, the FMA product error) and the double-word algorithms of Joldes,
+// Muller and Popescu ("Tight and rigorous error bounds for basic building
+// blocks of double-word arithmetic", ACM TOMS 44(2), 2017), whose relative
+// error bounds with u = 2^-24 are: DW+DW (accurate) 3u^2/(1-4u), DW*DW 5u^2,
+// DW/FP 3.5u^2.  Every operation is a separately rounded IEEE FP32 operation.
+struct dfl { float hi, lo; };
+
+__device__ __forceinline__ dfl df_two_sum(float a, float b)
+{
+	const float s = __fadd_rn(a, b);
+	const float bb = __fsub_rn(s, a);
+	return {s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
+}
+
+__device__ __forceinline__ dfl df_fast_two_sum(float a, float b)   // |a| >= |b| or a == 0
+{
+	const float s = __fadd_rn(a, b);
+	return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+
+__device__ __forceinline__ dfl df_add(dfl x, dfl y)
+{
+	const dfl s = df_two_sum(x.hi, y.hi), t = df_two_sum(x.lo, y.lo);
+	const dfl v = df_fast_two_sum(s.hi, __fadd_rn(s.lo, t.hi));
+	return df_fast_two_sum(v.hi, __fadd_rn(t.lo, v.lo));
+}
+
+__device__ __forceinline__ dfl df_mul(dfl x, dfl y)
+{
+	const float ch = __fmul_rn(x.hi, y.hi);
+	const float cl1 = __fmaf_rn(x.hi, y.hi, -ch);
+	const float tl0 = __fmul_rn(x.lo, y.lo);
+	const float tl1 = __fmaf_rn(x.hi, y.lo, tl0);
+	const float cl2 = __fmaf_rn(x.lo, y.hi, tl1);
+	return df_fast_two_sum(ch, __fadd_rn(cl1, cl2));
+}
+
+__device__ __forceinline__ dfl df_div_f(dfl x, float y)
+{
+	const float th = __fdiv_rn(x.hi, y);
+	const float ph = __fmul_rn(th, y);
+	const float pl = __fmaf_rn(th, y, -ph);
+	const float dh = __fsub_rn(x.hi, ph);
+	const float dt = __fsub_rn(dh, pl);
+	const float d = __fadd_rn(dt, x.lo);
+	return df_fast_two_sum(th, __fdiv_rn(d, y));
+}
+
+__device__ __forceinline__ dfl df_of(float2 v) { return {v.x, v.y}; }
 
 // ---- exact double helpers ----
 __device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a, b); }

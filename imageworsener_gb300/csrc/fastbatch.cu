@@ -50,6 +50,17 @@ __global__ void __launch_bounds__(kVPxThreads) kb_vstream_px(const FJob *jobs, c
 	vstream_px_tile<NS, NCH, ALPHA, DEPTH, PX>(sF, s_dyn, local % sF.vgx, local / sF.vgx);
 }
 
+template<int NS, int NCH, bool ALPHA, int DEPTH, int PX>
+__global__ void __launch_bounds__(kBulkThreads, 2) kb_vbulk(const FJob *jobs, const int *idx, const int *start, int n)
+{
+	extern __shared__ __align__(128) unsigned char s_bulk[];
+	__shared__ FJob sF;
+	const int g = find_image(start, n, blockIdx.x);
+	load_job(sF, jobs + idx[g]);
+	const int local = blockIdx.x - start[g];
+	vbulk_tile<NS, NCH, ALPHA, DEPTH, PX>(sF, s_bulk, local % sF.vgx, local / sF.vgx);
+}
+
 template<int NS, int NPL, int DEPTH>
 __global__ void __launch_bounds__(kVThreads) kb_vstream(const FJob *jobs, const int *idx, const int *start, int n)
 {
@@ -91,6 +102,11 @@ const void *batch_vkernel(const VVariant &v)
 	if(v.kind == 2 && v.ns == NS_ && v.nch == NPL_ && v.depth == D_) return (const void *)kb_vstream<NS_, NPL_, D_>;
 #define IWG_BGA(NPL_, D_) \
 	if(v.kind == 3 && v.nch == NPL_ && v.depth == D_) return (const void *)kb_vgather<NPL_, D_>;
+#define IWG_BBU(NS_, NCH_, A_, D_, PX_) \
+	if(v.kind == 4 && v.ns == NS_ && v.nch == NCH_ && v.alpha == (int)A_ && v.depth == D_ && v.px == PX_) \
+		return (const void *)kb_vbulk<NS_, NCH_, A_, D_, PX_>;
+	IWG_VBULK_VARIANTS(IWG_BBU)
+#undef IWG_BBU
 	IWG_VPX_VARIANTS(IWG_BPX)
 	IWG_VSTREAM_VARIANTS(IWG_BST)
 	IWG_VGATHER_VARIANTS(IWG_BGA)
@@ -125,13 +141,16 @@ struct Group {
 struct BatchArena {
 	void *p = nullptr;
 	size_t cap = 0;
-	bool ensure(size_t n)
+	bool ensure(size_t n, cudaStream_t st)   // stream-ordered: never waits for other streams
 	{
 		if(n <= cap) return true;
-		if(p) cudaFree(p);
+		if(p) cudaFreeAsync(p, st);
 		p = nullptr;
 		cap = 0;
-		if(cudaMalloc(&p, n + n / 4) != cudaSuccess) return false;
+		if(cudaMallocAsync(&p, n + n / 4, st) != cudaSuccess) {
+			cudaGetLastError();
+			return false;
+		}
 		cap = n + n / 4;
 		return true;
 	}
@@ -145,7 +164,7 @@ BatchArena &arena()
 
 }  // namespace
 
-int fast_launch_batch(cudaStream_t st, void *const *items, int n, std::string &err)
+int fast_launch_batch(cudaStream_t st, void *const *items, int n, std::string &err, cudaEvent_t after_vertical)
 {
 	if(n <= 0) return 0;
 	std::vector<Group> vg, hg;
@@ -196,7 +215,7 @@ int fast_launch_batch(cudaStream_t st, void *const *items, int n, std::string &e
 		}
 	}
 	BatchArena &A = arena();
-	if(!A.ensure(host.size())) {
+	if(!A.ensure(host.size(), st)) {
 		err = "Out of GPU memory (batch tables)";
 		return -1;
 	}
@@ -224,6 +243,7 @@ int fast_launch_batch(cudaStream_t st, void *const *items, int n, std::string &e
 		return true;
 	};
 	for(Group &g : vg) if(!launch(g)) return -1;
+	if(after_vertical) cudaEventRecord(after_vertical, st);
 	for(Group &g : hg) if(!launch(g)) return -1;
 	return launches;
 }

@@ -34,7 +34,10 @@ struct FTail {        // quantisation of one output channel, float tables
 	const int *code;  // P+2
 	const float *rev; // M+1
 	const float *nc;  // 255
+	const float *lut; // kLutCells: entries of the searched table (nc, or U[1..P]) <= cell/kLutCells
 };
+
+constexpr int kLutCells = 1024;
 
 struct FJob {
 	// input
@@ -86,6 +89,7 @@ struct FJob {
 	int *flag_count;
 	int *flag_list;            // entries (pixel, mask, image, 0)
 	int img;                   // index of the image in a batch (0 alone)
+	int *err_flag;             // set by a kernel whose bounded wait ran out
 	int vgx, vgy, hgx;         // blocks of the vertical pass (x, bands or rows), horizontal pass (x)
 };
 static_assert(sizeof(FJob) <= 4096, "FJob is passed by value as a kernel parameter");
@@ -279,6 +283,211 @@ __device__ __forceinline__ float u2f(unsigned int v)
 	return __fsub_rn(__uint_as_float(0x4b000000u | v), 8388608.0f);
 }
 
+
+// ---- asynchronous bulk copies and mbarriers (inline PTX, sm_90 and later) ----
+__device__ __forceinline__ unsigned smem_u32(const void *p)
+{
+	return (unsigned)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(unsigned long long *bar, unsigned count)
+{
+	asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long *bar, unsigned bytes)
+{
+	asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(unsigned long long *bar)
+{
+	asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+// Waits for the phase of 'parity' to complete; gives up (false) after a
+// bounded number of polls (each poll may suspend the thread briefly).
+__device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned parity)
+{
+	for(int it = 0; it < (1 << 21); it++) {
+		unsigned done;
+		asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+			: "=r"(done) : "r"(smem_u32(bar)), "r"(parity) : "memory");
+		if(done) return true;
+	}
+	return false;
+}
+
+// Global -> shared copy of 'bytes' (multiple of 16, both addresses 16-byte
+// aligned) that counts its bytes on 'bar'.
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned bytes, unsigned long long *bar)
+{
+	asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+		::"r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar)) : "memory");
+}
+
+constexpr int kBulkConsumers = 256;   // threads that decode and accumulate
+constexpr int kBulkThreads = kBulkConsumers + 32;   // plus one producer warp
+constexpr int kBulkStages = 8;        // rows in flight per block
+
+// Vertical pass, streaming, with the rows of a strip staged in shared memory
+// by asynchronous bulk copies.  A producer warp keeps kBulkStages rows of the
+// block's strip (kBulkConsumers * PX pixels) in flight; consumer threads
+// read their PX pixels of a row from shared memory, then decode and
+// accumulate exactly as vstream_px_tile (same slot scheme, same results).
+// Every wait is bounded: a wait that runs out sets F.err_flag, the producer
+// waits (bounded) for the copies it issued, and the block returns.
+template<int NS, int NCH, bool ALPHA, int DEPTH, int PX>
+__device__ __forceinline__ void vbulk_tile(const FJob &F, unsigned char *s_raw, int bx, int band)
+{
+	constexpr int BPP = NCH * (DEPTH / 8);
+	constexpr int NW = PX * BPP / 4;
+	static_assert(NW == 4, "one 16-byte group per consumer and row");
+	constexpr int STRIP = kBulkConsumers * PX * BPP;     // bytes of a full strip row
+	unsigned char *ring = s_raw;                          // kBulkStages * STRIP
+	unsigned long long *full = reinterpret_cast<unsigned long long *>(s_raw + kBulkStages * STRIP);
+	unsigned long long *empty = full + kBulkStages;
+	int *abort_flag = reinterpret_cast<int *>(empty + kBulkStages);
+	float *s_tab = reinterpret_cast<float *>(s_raw + kBulkStages * STRIP + 256);
+	const int jb = band * F.rows_per_band;
+	const int je = min(jb + F.rows_per_band, F.mid_h);
+	if(jb >= je) return;
+	const int p0 = F.first_pos[jb], p1 = F.last_pos[je - 1];
+	const int nq = p1 - p0 + 1;
+	float *s_w = s_tab + F.dec_tab_floats;
+	int2 *s_fin = reinterpret_cast<int2 *>(s_w + (size_t)nq * NS);
+	for(int k = threadIdx.x; k < F.dec_tab_floats; k += blockDim.x) s_tab[k] = F.dec_tab[k];
+	for(int k = threadIdx.x; k < nq * NS; k += blockDim.x) {
+		const int q = k / NS, sl = k - q * NS;
+		s_w[k] = F.sw[(size_t)(p0 - F.pmin + q) * 8 + sl];
+	}
+	for(int k = threadIdx.x; k < nq; k += blockDim.x) s_fin[k] = F.pinfo[p0 - F.pmin + k];
+	if(threadIdx.x == 0) {
+		for(int k = 0; k < kBulkStages; k++) {
+			mbar_init(full + k, 1);
+			mbar_init(empty + k, kBulkConsumers / 32);
+		}
+		*abort_flag = 0;
+		asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+	}
+	__syncthreads();
+
+	const int strip_x = bx * kBulkConsumers * PX;        // first pixel of the strip
+	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+	if(warp == kBulkConsumers / 32) {
+		// producer
+		if(lane != 0) return;
+		const uint8_t *base = F.in + (size_t)(F.crop_x + strip_x) * BPP + (unsigned long long)F.crop_y * F.in_bpr;
+		const int strip_px = min(kBulkConsumers * PX, F.mid_w - strip_x);
+		const unsigned bytes = (unsigned)((strip_px * BPP + 15) & ~15);
+		const int last_row = F.in_rows - 1;
+		int issued = 0;
+		bool ok = true;
+		for(int q = 0; q < nq && ok; q++) {
+			const int st = q % kBulkStages, use = q / kBulkStages;
+			if(use > 0 && !mbar_wait(empty + st, (use - 1) & 1)) { ok = false; break; }
+			if(*(volatile int *)abort_flag) { ok = false; break; }
+			const int row = min(max(p0 + q, 0), last_row);
+			mbar_expect_tx(full + st, bytes);
+			bulk_g2s(ring + (size_t)st * STRIP, base + (unsigned long long)row * F.in_bpr, bytes, full + st);
+			issued = q + 1;
+		}
+		if(!ok) {
+			atomicExch(F.err_flag, 1);
+			*(volatile int *)abort_flag = 1;
+		}
+		// every issued copy lands before the block's shared memory goes away
+		for(int q = max(0, issued - kBulkStages); q < issued; q++) mbar_wait(full + q % kBulkStages, (q / kBulkStages) & 1);
+		return;
+	}
+
+	// consumers
+	const int x0 = strip_x + threadIdx.x * PX;
+	const bool any = x0 < F.mid_w;
+	const bool full_px = x0 + PX <= F.mid_w;
+	const float ainv = F.alpha_inv;
+	const unsigned long long plane = F.plane;
+	const int mid_w = F.mid_w;
+	float *const interm = F.interm;
+	float acc[NS][PX][NCH];
+#pragma unroll
+	for(int s = 0; s < NS; s++)
+#pragma unroll
+		for(int px = 0; px < PX; px++)
+#pragma unroll
+			for(int c = 0; c < NCH; c++) acc[s][px][c] = 0.0f;
+
+	for(int q = 0; q < nq; q++) {
+		const int st = q % kBulkStages, use = q / kBulkStages;
+		if(!mbar_wait(full + st, use & 1)) {
+			atomicExch(F.err_flag, 1);
+			*(volatile int *)abort_flag = 1;
+			return;
+		}
+		uint32_t cur[NW];
+		{
+			const uint4 v = reinterpret_cast<const uint4 *>(ring + (size_t)st * STRIP)[threadIdx.x];
+			cur[0] = v.x; cur[1] = v.y; cur[2] = v.z; cur[3] = v.w;
+		}
+		__syncwarp();
+		if(lane == 0) mbar_arrive(empty + st);
+		float val[PX][NCH];
+#pragma unroll
+		for(int px = 0; px < PX; px++) {
+			float a = 1.0f;
+#pragma unroll
+			for(int c = 0; c < NCH; c++) {
+				const int sidx = px * NCH + c;
+				unsigned int code;
+				if(DEPTH == 8) code = __byte_perm(cur[sidx >> 2], 0u, 0x4440u + (sidx & 3));
+				else code = __byte_perm(cur[sidx >> 1], 0u, (sidx & 1) ? 0x4423u : 0x4401u);
+				if(ALPHA && c == NCH - 1) {
+					a = __fmul_rn(u2f(code), ainv);
+					val[px][c] = a;
+				}
+				else val[px][c] = dec_table<DEPTH>(s_tab, code);
+			}
+			if(ALPHA) {
+#pragma unroll
+				for(int c = 0; c < NCH - 1; c++) val[px][c] = __fmul_rn(val[px][c], a);
+			}
+		}
+		float ws[NS];
+#pragma unroll
+		for(int s = 0; s < NS; s++) ws[s] = s_w[q * NS + s];
+#pragma unroll
+		for(int s = 0; s < NS; s++)
+#pragma unroll
+			for(int px = 0; px < PX; px++)
+#pragma unroll
+				for(int c = 0; c < NCH; c++) acc[s][px][c] = __fmaf_rn(val[px][c], ws[s], acc[s][px][c]);
+		const int2 fin = s_fin[q];
+		for(int k = 0; k < fin.y; k++) {
+			const int j = fin.x + k;
+			const int sj = j % NS;
+			const bool keep = any && j >= jb && j < je;
+#pragma unroll
+			for(int s = 0; s < NS; s++) {
+				if(s == sj) {
+					if(keep) {
+						float *o = interm + (unsigned long long)j * mid_w + x0;
+#pragma unroll
+						for(int px = 0; px < PX; px++) {
+							if(full_px || x0 + px < mid_w) {
+#pragma unroll
+								for(int c = 0; c < NCH; c++) o[(unsigned long long)c * plane + px] = acc[s][px][c];
+							}
+						}
+					}
+#pragma unroll
+					for(int px = 0; px < PX; px++)
+#pragma unroll
+						for(int c = 0; c < NCH; c++) acc[s][px][c] = 0.0f;
+				}
+			}
+		}
+	}
+}
 
 // Vertical pass, streaming, PX pixels per thread.  Same scheme as
 // k_vstream, arranged for memory-level parallelism and few instructions
@@ -481,6 +690,16 @@ __device__ __forceinline__ void vgather_tile(const FJob &F, float *s_tab, int bx
 // horizontal pass + guarded quantisation
 // ---------------------------------------------------------------------------
 
+// count_le_f for v in [0, 1], starting from the count at the start of v's
+// cell (v * kLutCells is exact, so the cell's start is <= v) and stepping up.
+__device__ __forceinline__ int count_le_lut(const float *t, int n, const float *lut, float v)
+{
+	const int cell = min(max((int)__fmul_rn(v, (float)kLutCells), 0), kLutCells - 1);
+	int k = (int)__ldg(lut + cell);
+	while(k < n && __ldg(t + k) <= v) k++;
+	return k;
+}
+
 __device__ __forceinline__ int count_le_f(const float *t, int n, float v)
 {
 	int lo = 0, hi = n;
@@ -500,12 +719,12 @@ __device__ __forceinline__ int quantize_guarded(const FTail &T, float v, float E
 	const float Ep = __fmaf_rn(E, 1.0000001f, __fmaf_rn(fabsf(v), 2.4e-7f, 1e-37f));
 	const float lo_v = __fsub_rn(v, Ep), hi_v = __fadd_rn(v, Ep);
 	if(T.use_nc) {
-		int c = count_le_f(T.nc, 255, v);
+		int c = count_le_lut(T.nc, 255, T.lut, v);
 		if(c > 0 && !(T.nc[c - 1] < lo_v)) return -1;
 		if(c < 255 && !(T.nc[c] > hi_v)) return -1;
 		return c;
 	}
-	int k = count_le_f(T.U + 1, T.P, v);
+	int k = count_le_lut(T.U + 1, T.P, T.lut, v);
 	bool near_lo = k > 0 && !(T.U[k] < lo_v);          // v within E of the bracket's lower edge
 	bool near_hi = k < T.P && !(T.U[k + 1] > hi_v);    // ... or of the next bracket
 	if(near_lo || near_hi) {
@@ -523,8 +742,11 @@ __device__ __forceinline__ int quantize_guarded(const FTail &T, float v, float E
 	if(k == T.P) return lo;
 	const float a = T.rev[lo], b = T.rev[hi];
 	const float den = __fsub_rn(b, a);
-	const float f = __fdiv_rn(__fsub_rn(v, a), den);
-	const float mf = __fdiv_rn(__fmaf_rn(fabsf(a) + fabsf(b), 1.2e-7f, Ep), den) + 1e-6f;
+	// one correctly rounded reciprocal for both quotients: f is within 1.5 ulp
+	// (< 2e-7) of the rounded division, well inside the 1e-6 slack of mf
+	const float rd = __frcp_rn(den);
+	const float f = __fmul_rn(__fsub_rn(v, a), rd);
+	const float mf = __fmaf_rn(__fmul_rn(__fmaf_rn(fabsf(a) + fabsf(b), 1.2e-7f, Ep), rd), 1.0000004f, 1e-6f);
 	float thr = 0.5f;
 	if(T.dfam == IW_DITHERFAMILY_ORDERED) thr = ((float)dither_rank(T.dsub, x, y) + 0.5f) * 0.015625f;
 	int decided;
@@ -583,7 +805,7 @@ __device__ __forceinline__ void hpass_pixel(const FJob &F, int i, int j)
 	int alpha_code = -1;
 	unsigned int redo = 0;
 	const unsigned int all = (1u << F.mid_n) - 1u;
-	float A = 0.0f, EA = 0.0f;
+	float A = 0.0f, EA = 0.0f, rA = 0.0f, rden = 0.0f;
 #pragma unroll
 	for(int k = 0; k < dev::kMaxCh; k++) {
 		codes[k] = -1;
@@ -602,9 +824,11 @@ __device__ __forceinline__ void hpass_pixel(const FJob &F, int i, int j)
 			if(alpha_code == 0 && F.blacken) { codes[k] = 0; continue; }
 			const float den = __fsub_rn(A, EA);
 			if(!(den > 0.0f)) { redo |= F.k_bit[k] | F.k_bit[0]; continue; }
-			const float q = __fdiv_rn(val, A);
-			err = __fdiv_rn(__fmaf_rn(fabsf(q), EA, err), den);
-			err = __fmaf_rn(fabsf(q), 1.2e-7f, err);
+			if(rA == 0.0f) { rA = __frcp_rn(A); rden = __frcp_rn(den); }   // shared by the colour channels
+			// q within 1.5 ulp of val/A; the bound's quotient rounded up by its own error
+			const float q = __fmul_rn(val, rA);
+			err = __fmul_rn(__fmul_rn(__fmaf_rn(fabsf(q), EA, err), rden), 1.0000004f);
+			err = __fmaf_rn(fabsf(q), 2.4e-7f, err);
 			val = q;
 		}
 		const int c = quantize_guarded(F.k_tail[k], val, err, i, j);
@@ -638,7 +862,7 @@ __device__ __forceinline__ void hpass_pixel(const FJob &F, int i, int j)
 
 // Vertical kernel variant of a prepared image (which template instance).
 struct VVariant {
-	int kind = 0;    // 1: k_vstream_px, 2: k_vstream, 3: k_vgather
+	int kind = 0;    // 1: k_vstream_px, 2: k_vstream, 3: k_vgather, 4: k_vbulk
 	int ns = 0, nch = 0, alpha = 0, depth = 0, px = 0;
 	bool operator==(const VVariant &o) const
 	{
@@ -661,6 +885,12 @@ struct FastState {
 	size_t o_fp = 0, o_lp = 0, o_src = 0, o_pi = 0, o_sw = 0;
 	bool streaming = false;
 	size_t flag_entries = 0;   // capacity of the flag list (one entry per output pixel)
+	// double-float tier of the re-evaluation: tables (cached device copies)
+	// and weights (in the blob)
+	const float2 *df_tab[dev::kMaxCh] = {nullptr, nullptr, nullptr, nullptr};
+	const float2 *df_atab = nullptr;
+	size_t o_wvdf = 0, o_whdf = 0;
+	bool df = false;
 };
 
 // Template instances of the vertical kernels, shared by the per-image and
@@ -674,6 +904,10 @@ struct FastState {
 	X(4, 3, false, 8, 4) \
 	X(4, 2, true, 8, 4) X(6, 2, true, 8, 4) X(8, 2, true, 8, 4) \
 	X(4, 1, false, 8, 8) X(6, 1, false, 8, 8) X(8, 1, false, 8, 8)
+// Instances of the bulk-copy vertical kernel: (NS, channels, alpha, depth, PX)
+// with one 16-byte group per consumer thread and row.
+// (more slots or more pixels per thread spill registers at this block size)
+#define IWG_VBULK_VARIANTS(X) X(4, 4, true, 16, 2)
 // (NS, planes, depth)
 #define IWG_VSTREAM_VARIANTS(X) \
 	X(4, 1, 8) X(4, 2, 8) X(4, 3, 8) X(4, 4, 8) X(6, 1, 8) X(6, 2, 8) X(6, 3, 8) X(6, 4, 8) \

@@ -32,7 +32,7 @@ namespace iwg {
 
 using namespace dev;
 
-void launch_fix_flagged(cudaStream_t st, const Job &J, const int *count, const int *list);
+void launch_fix_flagged(cudaStream_t st, const Job &J, int *count, const int *list);
 
 namespace {
 
@@ -43,6 +43,13 @@ __global__ void __launch_bounds__(kVThreads) k_vstream(FJob F)
 {
 	extern __shared__ __align__(16) float s_tab[];
 	vstream_tile<NS, NPL, DEPTH>(F, s_tab, blockIdx.x, blockIdx.y);
+}
+
+template<int NS, int NCH, bool ALPHA, int DEPTH, int PX>
+__global__ void __launch_bounds__(kBulkThreads, 2) k_vbulk(FJob F)
+{
+	extern __shared__ __align__(128) unsigned char s_bulk[];
+	vbulk_tile<NS, NCH, ALPHA, DEPTH, PX>(F, s_bulk, blockIdx.x, blockIdx.y);
 }
 
 template<int NS, int NCH, bool ALPHA, int DEPTH, int PX>
@@ -121,6 +128,33 @@ const float *dev_derived(const std::shared_ptr<const std::vector<double>> &v, in
 	const float *d = upload_vec(*f);
 	if(d) C.dev[key] = {std::static_pointer_cast<const void>(v), std::static_pointer_cast<const void>(f), (void *)d};
 	return d;
+}
+
+// Double-float copy of a double table: (hi, lo) = (fl32(d), fl32(d - hi)),
+// within 2^-48 |d| of d.
+std::shared_ptr<std::vector<float>> as_dfloat(const std::vector<double> &v)
+{
+	auto f = std::make_shared<std::vector<float>>(2 * v.size());
+	for(size_t i = 0; i < v.size(); i++) {
+		const float hi = (float)v[i];
+		(*f)[2 * i] = hi;
+		(*f)[2 * i + 1] = std::isfinite(v[i]) ? (float)(v[i] - (double)hi) : 0.0f;
+	}
+	return f;
+}
+
+// Search start points for a float copy of an ascending table t[first ..
+// first+n): cell i holds the number of entries <= i / kLutCells.
+std::shared_ptr<std::vector<float>> make_lut(const std::vector<double> &t, int first, int n)
+{
+	auto f = std::make_shared<std::vector<float>>(kLutCells);
+	int k = 0;
+	for(int i = 0; i < kLutCells; i++) {
+		const float c = (float)i / (float)kLutCells;
+		while(k < n && (float)t[first + k] <= c) k++;
+		(*f)[i] = (float)k;
+	}
+	return f;
 }
 
 std::shared_ptr<std::vector<float>> as_float(const std::vector<double> &v)
@@ -245,7 +279,11 @@ bool fast_eligible(const Plan &P, const Job &J, FastInfo &fi)
 	for(int oc = 0; oc < P.out_n; oc++) {
 		int f = P.out[oc].q.dfam;
 		if(f != IW_DITHERFAMILY_NONE && f != IW_DITHERFAMILY_ORDERED) return false;
-		if(P.out[oc].q.P > 65535) return false;
+		// Above 4096 output levels the FP32 bound (about taps * 2^-24 of the
+		// value) spans a large share of a step: at 16-bit output most pixels
+		// get flagged (measured: about 90 %), and re-evaluating each with its
+		// own vertical sums costs more than the plain form, which shares them.
+		if(P.out[oc].q.P > 4095) return false;
 	}
 	if(P.wsets[0][0]->edge_value != 0.0 || P.wsets[1][0]->edge_value != 0.0) return false;
 	(void)J;
@@ -259,7 +297,7 @@ bool fast_eligible(const Plan &P, const Job &J, FastInfo &fi)
 void fast_launch_impl(cudaStream_t st, void *state, void (*mark)(void *), void *markarg)
 {
 	FastState &S = *static_cast<FastState *>(state);
-	cudaMemsetAsync(S.F.flag_count, 0, sizeof(int), st);
+	cudaMemsetAsync(S.F.flag_count, 0, 3 * sizeof(int), st);
 	void *fargs[] = {&S.F};
 	cudaLaunchKernel(S.vkernel, S.vgrid, dim3(S.vthreads), fargs, S.vsmem, st);
 	mark(markarg);
@@ -402,6 +440,8 @@ static FastState *fast_build(const Plan &P, const Job &J, bool batch, std::strin
 	size_t o_hw = add(hwf.data(), hwf.size() * 4);
 	size_t o_voff = add(WV.off.data(), WV.off.size() * 4), o_vsrc = add(WV.src.data(), WV.src.size() * 4);
 	size_t o_vw = add(vwf.data(), vwf.size() * 4);
+	std::vector<float> wvdf = *as_dfloat(WV.w), whdf = *as_dfloat(WH.w);
+	size_t o_wvdf = add(wvdf.data(), wvdf.size() * 4), o_whdf = add(whdf.data(), whdf.size() * 4);
 	size_t o_fp = 0, o_lp = 0, o_src = 0, o_pi = 0, o_sw = 0;
 	if(S.ok) {
 		o_fp = add(S.first_pos.data(), S.first_pos.size() * 4);
@@ -428,12 +468,39 @@ static FastState *fast_build(const Plan &P, const Job &J, bool batch, std::strin
 		T.code = dev_table(q.code);
 		T.rev = dev_derived(q.rev, 1, as_float);
 		T.nc = q.use_nc ? dev_derived(q.nc, 1, as_float) : nullptr;
-		if(!T.U || !T.X || !T.code || !T.rev || (q.use_nc && !T.nc)) { err = "Out of GPU memory (fast tables)"; return nullptr; }
+		// start points for the table searches (counted with the same float compares)
+		T.lut = q.use_nc ? dev_derived(q.nc, 401, [](const std::vector<double> &t) { return make_lut(t, 0, (int)t.size()); })
+		                 : dev_derived(q.U, 400, [](const std::vector<double> &t) { return make_lut(t, 1, (int)t.size() - 2); });
+		if(!T.U || !T.X || !T.code || !T.rev || (q.use_nc && !T.nc) || !T.lut) { err = "Out of GPU memory (fast tables)"; return nullptr; }
 	}
 	for(int k = 0; k < P.mid_n; k++) F.k_tail[k] = tails[F.k_out[k] >= 0 ? F.k_out[k] : 0];
 
+	// ---- double-float tables for the re-evaluation tier (cached)
+	const float2 *df_tab[dev::kMaxCh] = {nullptr, nullptr, nullptr, nullptr};
+	const float2 *df_atab = nullptr;
+	bool df_ok = true;
+	{
+		auto df_of_table = [&](const std::shared_ptr<const std::vector<double>> &t) {
+			return (const float2 *)dev_derived(t, 300, as_dfloat);
+		};
+		const int ncodes = 1 << P.in_depth;
+		for(int m = 0; m < P.mid_n; m++) {
+			const MidChannel &mc = P.mid[m];
+			if(mc.in_ch >= P.in_nphys) continue;   // virtual channel: value 1
+			df_tab[m] = df_of_table(input_table(P.cs_in.cstype, P.cs_in.gamma, P.in_max, ncodes, mc.lin_cs));
+			if(!df_tab[m]) df_ok = false;
+		}
+		if(IW_IMGTYPE_HAS_ALPHA(P.in_logtype) && P.in_alpha < P.in_nphys) {
+			df_atab = df_of_table(input_table(P.cs_in.cstype, P.cs_in.gamma, P.in_max, ncodes, true));
+			if(!df_atab) df_ok = false;
+		}
+	}
+
 	// ---- kernel selection
 	auto *FS = new FastState();
+	for(int m = 0; m < dev::kMaxCh; m++) FS->df_tab[m] = df_tab[m];
+	FS->df_atab = df_atab;
+	FS->df = df_ok;
 	const int gx = (F.mid_w + kVThreads - 1) / kVThreads;
 	FS->vsmem = (size_t)dec_floats * sizeof(float);
 	FS->vgrid = dim3(gx, F.mid_h);
@@ -491,6 +558,41 @@ static FastState *fast_build(const Plan &P, const Job &J, bool batch, std::strin
 			} \
 		} \
 	}
+	// rows staged by asynchronous bulk copies: input in device memory, rows
+	// 16-byte aligned
+	bool in_device = false;
+	{
+		cudaPointerAttributes pa{};
+		if(cudaPointerGetAttributes(&pa, J.in) == cudaSuccess) in_device = pa.type == cudaMemoryTypeDevice;
+		cudaGetLastError();
+	}
+#define IWG_VBULK(NS_, NCH_, A_, D_, PX_) \
+	if(!FS->vkernel && in_device && ident && S.arith && S.ns == NS_ && nplanes == NCH_ && (F.alpha_src >= 0) == A_ && \
+		P.in_depth == D_ && v_base % 16 == 0 && P.in_bpr % 16 == 0) { \
+		const int gxb_ = (F.mid_w + kBulkConsumers * PX_ - 1) / (kBulkConsumers * PX_); \
+		int bands = std::max(1, std::min(F.mid_h, batch ? (F.mid_h + 47) / 48 : (2 * 152 + gxb_ / 2) / gxb_)); \
+		F.rows_per_band = (F.mid_h + bands - 1) / bands; \
+		bands = (F.mid_h + F.rows_per_band - 1) / F.rows_per_band; \
+		int nq_max = 0; \
+		for(int b_ = 0; b_ < bands; b_++) { \
+			const int jb_ = b_ * F.rows_per_band, je_ = std::min(jb_ + F.rows_per_band, F.mid_h); \
+			nq_max = std::max(nq_max, S.last_pos[je_ - 1] - S.first_pos[jb_] + 1); \
+		} \
+		const size_t sm_ = (size_t)kBulkStages * kBulkConsumers * PX_ * NCH_ * (D_ / 8) + 256 + \
+			(size_t)dec_floats * sizeof(float) + (size_t)nq_max * (NS_ * sizeof(float) + sizeof(int2)); \
+		const void *k_ = (const void *)k_vbulk<NS_, NCH_, A_, D_, PX_>; \
+		if(sm_ <= 200 * 1024 && \
+			cudaFuncSetAttribute(k_, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_) == cudaSuccess) { \
+			FS->vkernel = k_; \
+			FS->vgrid = dim3(gxb_, bands); \
+			FS->vthreads = kBulkThreads; \
+			FS->vsmem = sm_; \
+			FS->vv.kind = 4; FS->vv.ns = NS_; FS->vv.nch = NCH_; FS->vv.alpha = A_; FS->vv.depth = D_; FS->vv.px = PX_; \
+		} \
+		cudaGetLastError(); \
+	}
+	IWG_VBULK_VARIANTS(IWG_VBULK)
+#undef IWG_VBULK
 	IWG_VPX_VARIANTS(IWG_VPX)
 #undef IWG_VPX
 	if(S.ok) {
@@ -516,6 +618,7 @@ static FastState *fast_build(const Plan &P, const Job &J, bool batch, std::strin
 	FS->o_hoff = o_hoff; FS->o_hsrc = o_hsrc; FS->o_hw = o_hw;
 	FS->o_voff = o_voff; FS->o_vsrc = o_vsrc; FS->o_vw = o_vw;
 	FS->o_fp = o_fp; FS->o_lp = o_lp; FS->o_src = o_src; FS->o_pi = o_pi; FS->o_sw = o_sw;
+	FS->o_wvdf = o_wvdf; FS->o_whdf = o_whdf;
 	FS->streaming = S.ok;
 	FS->flag_entries = (size_t)F.out_w * F.out_h;
 	return FS;
@@ -528,6 +631,7 @@ static void fast_place(FastState *FS, const uint8_t *base, int *flag_count, int 
 	FJob &F = FS->F;
 	F.flag_count = flag_count;
 	F.flag_list = flag_list;
+	F.err_flag = flag_count + 2;
 	F.img = img;
 	F.hoff = (const int *)(base + FS->o_hoff);
 	F.hsrc = (const int *)(base + FS->o_hsrc);
@@ -535,6 +639,11 @@ static void fast_place(FastState *FS, const uint8_t *base, int *flag_count, int 
 	F.voff = (const int *)(base + FS->o_voff);
 	F.vsrc = (const int *)(base + FS->o_vsrc);
 	F.vw = (const float *)(base + FS->o_vw);
+	Job &J = FS->J;
+	for(int m = 0; m < dev::kMaxCh; m++) J.df_tab[m] = FS->df ? FS->df_tab[m] : nullptr;
+	J.df_atab = FS->df ? FS->df_atab : nullptr;
+	J.df_wv = FS->df ? (const float2 *)(base + FS->o_wvdf) : nullptr;
+	J.df_wh = FS->df ? (const float2 *)(base + FS->o_whdf) : nullptr;
 	if(FS->streaming) {
 		F.first_pos = (const int *)(base + FS->o_fp);
 		F.last_pos = (const int *)(base + FS->o_lp);
@@ -553,10 +662,11 @@ bool fast_prepare(cudaStream_t st, const Plan &P, Job &J, FastInfo &fi, std::str
 	const size_t flag_off = (FS->blob.size() + 255) & ~(size_t)255;
 	const size_t need = flag_off + 256 + FS->flag_entries * 16;
 	if(need > C.scratch_cap) {
-		if(C.scratch) cudaFree(C.scratch);
+		if(C.scratch) cudaFreeAsync(C.scratch, st);
 		C.scratch = nullptr;
 		C.scratch_cap = 0;
-		if(cudaMalloc(&C.scratch, need + need / 8) != cudaSuccess) {
+		if(cudaMallocAsync(&C.scratch, need + need / 8, st) != cudaSuccess) {
+			cudaGetLastError();
 			delete FS;
 			err = "Out of GPU memory (fast form)";
 			return false;
@@ -592,6 +702,15 @@ int fast_item_htaps(const void *item) { return static_cast<const FastState *>(it
 void fast_item_place(void *item, const uint8_t *dev_blob, int *flag_count, int *flag_list, int img)
 {
 	fast_place(static_cast<FastState *>(item), dev_blob, flag_count, flag_list, img);
+}
+
+void fast_item_job_df(const void *item, Job &J)
+{
+	const Job &K = static_cast<const FastState *>(item)->J;
+	for(int m = 0; m < dev::kMaxCh; m++) J.df_tab[m] = K.df_tab[m];
+	J.df_atab = K.df_atab;
+	J.df_wv = K.df_wv;
+	J.df_wh = K.df_wh;
 }
 
 void fast_item_free(void *item) { delete static_cast<FastState *>(item); }

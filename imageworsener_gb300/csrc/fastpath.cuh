@@ -51,7 +51,11 @@ int fast_item_htaps(const void *item);             // widest horizontal window
 void fast_item_place(void *item, const uint8_t *dev_blob, int *flag_count, int *flag_list, int img);
 // Launches the vertical and horizontal passes of n placed images, one launch
 // per kernel variant (fastbatch.cu).  Returns the number of launches, -1 on error.
-int fast_launch_batch(cudaStream_t st, void *const *items, int n, std::string &err);
+int fast_launch_batch(cudaStream_t st, void *const *items, int n, std::string &err,
+	cudaEvent_t after_vertical = nullptr);
+// Copies the image's double-float re-evaluation pointers (set by placement)
+// into the caller's job record.
+void fast_item_job_df(const void *item, dev::Job &J);
 void fast_item_free(void *item);
 
 }  // namespace iwg

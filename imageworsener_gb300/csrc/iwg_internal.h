@@ -163,7 +163,8 @@ struct DimRequest {
 struct Stats {   // per call, readable through the iwg_* extension API
 	double ms_total = 0, ms_device = 0;
 	double ms_part[4] = {0, 0, 0, 0};   // per launch group: vertical, horizontal, fix-up / scan
-	long long flagged = 0;       // samples re-evaluated exactly (fast form)
+	long long flagged = 0;       // pixels re-evaluated (fast form)
+	long long flagged_exact = 0; // of them, pixels the double-float tier left to FP64
 	int form = 0;                // 0 = plain FP64, 1 = FP32 + guard band
 	int kernels = 0;             // kernel launches issued
 	int zero_copy = 0;           // kernels read/wrote the host image buffers directly

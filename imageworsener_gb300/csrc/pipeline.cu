@@ -245,6 +245,32 @@ __device__ __forceinline__ void errdiff_weights(int dsub, double *c)
 	for(int k = 0; k < 12; k++) c[k] = ddiv((double)num[sub][k], den[sub]);
 }
 
+constexpr int kScanChunk = 256;   // samples staged per warp for the serial walk
+
+// The reference's clamp to [0, 1] ("if(v<0) v=0; if(v>1) v=1"), by integer
+// tests of the bit pattern (NaN passes through, as there); -0 becomes +0,
+// which compares and adds like -0 everywhere downstream.
+// a <= b for non-NaN doubles by integer comparison of order-preserving keys
+// (negative values' magnitude bits are flipped).  -0 and +0 differ in key,
+// but a difference of equal finite values is +0, so -0 does not occur where
+// this is used.
+__device__ __forceinline__ bool dle_bits(double a, double b)
+{
+	long long ka = __double_as_longlong(a), kb = __double_as_longlong(b);
+	ka ^= (ka >> 63) & 0x7fffffffffffffffLL;
+	kb ^= (kb >> 63) & 0x7fffffffffffffffLL;
+	return ka <= kb;
+}
+
+__device__ __forceinline__ double clamp01_bits(double v)
+{
+	const long long b = __double_as_longlong(v);
+	if((b & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL) return v;   // NaN
+	if(b < 0) return 0.0;
+	if(b > 0x3ff0000000000000LL) return 1.0;
+	return v;
+}
+
 // Bracket index k (U[k] <= v < U[k+1]) of v >= +0, by binary search.
 __device__ __forceinline__ int bracket_index(const DQuant &q, long long vb)
 {
@@ -268,16 +294,15 @@ __device__ __forceinline__ int bracket_index(const DQuant &q, long long vb)
 //   3. all lanes send the row's errors to the next two rows (e1, e2), each
 //      lane owning target positions and adding the contributions in the order
 //      the reference adds them (sample x-2f, x-f, x, x+f, x+2f); rows shift.
-// Error buffer of a channel: e0, e1, e2, the row's errors and the row's
-// brackets, out_w doubles each.
-__device__ void errdiff_warp(const Job &J, int oc)
+// Error buffer of a channel: e0, e1, e2 and the row's errors, out_w doubles
+// each; the staged chunk lives in shared memory (kScanChunk samples).
+__device__ void errdiff_warp(const Job &J, int oc, double *sv, double *se, int *sk)
 {
 	const int lane = threadIdx.x & 31;
 	const DOut &o = J.outc[oc];
 	const DQuant &q = o.q;
 	const int W = J.out_w;
 	double *e0 = J.errbuf + (unsigned long long)oc * 5 * W, *e1 = e0 + W, *e2 = e1 + W, *er = e2 + W;
-	int *kb = reinterpret_cast<int *>(er + W);
 	const long long *U = reinterpret_cast<const long long *>(q.U);
 	const long long *X = reinterpret_cast<const long long *>(q.X);
 	double c[12];
@@ -288,54 +313,57 @@ __device__ void errdiff_warp(const Job &J, int oc)
 	for(int y = 0; y < J.out_h; y++) {
 		const int f = (y % 2) ? -1 : 1;
 		const double *row = J.scanbuf + ((unsigned long long)oc * J.out_h + y) * W;
-		for(int t = lane; t < W; t += 32) {
-			double v = row[t];
-			if(v < 0.0) v = 0.0;
-			if(v > 1.0) v = 1.0;
-			kb[t] = v == v ? bracket_index(q, __double_as_longlong(dadd(v, 0.0))) : 0;
-		}
-		__syncwarp();
-		if(lane == 0) {
-			double err1 = 0.0, err2 = 0.0;     // errors of the previous two samples
-			bool has1 = false, has2 = false;
-			for(int z = 0; z < W; z++) {
-				const int x = (y % 2) ? W - 1 - z : z;
+		double err1 = 0.0, err2 = 0.0;     // errors of the previous two samples of the row
+		bool has1 = false, has2 = false;
+		for(int z0 = 0; z0 < W; z0 += kScanChunk) {
+			const int cn = min(kScanChunk, W - z0);
+			// stage the chunk (in processing order): value, carried error, bracket
+			for(int zz = lane; zz < cn; zz += 32) {
+				const int x = (y % 2) ? W - 1 - (z0 + zz) : z0 + zz;
 				double v = row[x];
+				sv[zz] = v;
+				se[zz] = e0[x];
 				if(v < 0.0) v = 0.0;
 				if(v > 1.0) v = 1.0;
-				// e0[x] as the reference has it when it reaches x: the carried
-				// error, then x-2f's contribution, then x-f's
-				double e = e0[x];
-				if(has2) e = dadd(e, dmul(err2, c[1]));
-				if(has1) e = dadd(e, dmul(err1, c[0]));
-				v = dadd(v, e);
-				if(v > 1.0) v = 1.0;
-				else if(v < 0.0) v = 0.0;
-				int code;
-				double err = skip;
-				if(v != v) code = 0;
-				else {
-					const long long vb = __double_as_longlong(dadd(v, 0.0));   // -0 becomes +0 (same value)
-					int k = kb[x];
-					while(k < q.P && __ldg(U + k + 1) <= vb) k++;
-					while(k > 0 && __ldg(U + k) > vb) k--;
-					const int lo = q.code[k], hi = q.code[k + 1];
-					if(k == q.P || vb < __ldg(X + k)) code = lo;
-					else {
-						const double d_lo = dsub(v, q.rev[lo]), d_hi = dsub(q.rev[hi], v);
-						if(d_hi <= d_lo) { err = -d_hi; code = hi; }
-						else { err = d_lo; code = lo; }
-					}
-				}
-				er[x] = err;
-				// this sample's contributions reach x+f (c0) and x+2f (c1) when those exist
-				const bool sent = err == err;
-				err2 = err1; has2 = has1 && (x + f >= 0 && x + f < W);
-				err1 = err; has1 = sent;
-				store_code(J, oc, x, y, (unsigned int)code);
+				sk[zz] = v == v ? bracket_index(q, __double_as_longlong(dadd(v, 0.0))) : 0;
 			}
+			__syncwarp();
+			if(lane == 0) {
+				for(int zz = 0; zz < cn; zz++) {
+					const int x = (y % 2) ? W - 1 - (z0 + zz) : z0 + zz;
+					// e0[x] as the reference has it when it reaches x: the carried
+					// error, then x-2f's contribution (known a sample earlier, off
+					// the dependency chain), then x-f's
+					double e = se[zz];
+					if(has2) e = dadd(e, dmul(err2, c[1]));
+					if(has1) e = dadd(e, dmul(err1, c[0]));
+					const double v = clamp01_bits(dadd(clamp01_bits(sv[zz]), e));
+					const long long vb = __double_as_longlong(v);
+					int code;
+					double err = skip;
+					bool sent = false;
+					if((vb & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL) code = 0;   // NaN
+					else {
+						int k = sk[zz];
+						while(k < q.P && __ldg(U + k + 1) <= vb) k++;
+						while(k > 0 && __ldg(U + k) > vb) k--;
+						const int lo = q.code[k], hi = q.code[k + 1];
+						if(k == q.P || vb < __ldg(X + k)) code = lo;
+						else {
+							const double d_lo = dsub(v, q.rev[lo]), d_hi = dsub(q.rev[hi], v);
+							if(dle_bits(d_hi, d_lo)) { err = -d_hi; code = hi; }
+							else { err = d_lo; code = lo; }
+							sent = true;
+						}
+					}
+					er[x] = err;
+					err2 = err1; has2 = has1;
+					err1 = err; has1 = sent;
+					store_code(J, oc, x, y, (unsigned int)code);
+				}
+			}
+			__syncwarp();
 		}
-		__syncwarp();
 		for(int t = lane; t < W; t += 32) {
 			double a1 = e1[t], a2 = e2[t];
 #pragma unroll
@@ -461,11 +489,13 @@ __device__ void random_warp(const Job &J, int oc)
 	}
 }
 
-// One warp per output channel of the image.
+// One warp per output channel of the image (at most four warps per block).
 __device__ __forceinline__ void scan_warp(const Job &J, int oc)
 {
-	if(oc >= J.out_n || !J.outc[oc].scan) return;
-	if(J.outc[oc].q.dfam == IW_DITHERFAMILY_ERRDIFF) errdiff_warp(J, oc);
+	__shared__ double s_v[dev::kMaxCh][kScanChunk], s_e[dev::kMaxCh][kScanChunk];
+	__shared__ int s_k[dev::kMaxCh][kScanChunk];
+	if(oc >= J.out_n || oc >= dev::kMaxCh || !J.outc[oc].scan) return;
+	if(J.outc[oc].q.dfam == IW_DITHERFAMILY_ERRDIFF) errdiff_warp(J, oc, s_v[oc], s_e[oc], s_k[oc]);
 	else random_warp(J, oc);
 }
 
@@ -548,6 +578,199 @@ __device__ __forceinline__ int nth_bit(unsigned int mask, int r)
 	return __ffs(mask) - 1;
 }
 
+// ---- double-float tier of the re-evaluation ----
+//
+// A flagged pixel is first re-evaluated in double-float arithmetic (48-bit,
+// on the FP32 pipe) with a rigorous bound against the reference's FP64
+// computation.  Every float32 intermediate the pixel reads is certified:
+// the reference's sum S_ref lies within delta of the double-float sum, and
+// if no float rounding boundary lies in that interval, fl32(S_ref) is the
+// float nearest the double-float value, exactly.  The horizontal sum,
+// the float alpha and the division get the same treatment, and the output
+// code is taken only if it is the same over the whole remaining interval
+// (with a margin for the rounding of the ordered-dither fraction).  Anything
+// uncertain leaves the pixel to the FP64 path.  Bounds (u = 2^-24, n taps,
+// A = sum of |term|): decode / weight conversion 2u^2 each, products 5u^2,
+// additions 3u^2 relative to the partial sum, all within 24*n*u^2*A for a
+// vertical sum; the reference's own rounding adds (2n+2)*2^-53*A.
+
+// True if every real within 'delta' of hi + lo rounds to the float hi.
+__device__ __forceinline__ bool rounds_to_hi(dfl x, float delta)
+{
+	const float up = __fsub_rn(nextafterf(x.hi, INFINITY), x.hi);
+	const float down = __fsub_rn(x.hi, nextafterf(x.hi, -INFINITY));
+	return isfinite(up) && isfinite(down) && __fsub_rn(x.lo, delta) > -0.5f * down && __fadd_rn(x.lo, delta) < 0.5f * up;
+}
+
+// The reference's float intermediates of every channel in 'mask' at (column
+// x, row j), if all are certain.  The channels share the vertical weights
+// (the fast form has one weight set per dimension), so each tap's pixel is
+// read and its alpha decoded once for all of them.
+__device__ __forceinline__ bool interm_df_all(const Job &J, unsigned int mask, int x, int j, float *out, int stride)
+{
+	const DWeights &W = J.wv[J.mid[0].wv];
+	dfl acc[dev::kMaxCh];
+	float A[dev::kMaxCh];
+#pragma unroll
+	for(int m = 0; m < dev::kMaxCh; m++) { acc[m] = {0.0f, 0.0f}; A[m] = 0.0f; }
+	const int px = J.crop_x + x;
+	int n = 1;
+	// the alpha sample is read only for premultiplied channels, and only when
+	// it is stored (a virtual alpha is 1; images without alpha have no table)
+	bool need_alpha = false;
+#pragma unroll
+	for(int m = 0; m < dev::kMaxCh; m++)
+		if(m < J.mid_n && ((mask >> m) & 1u) && J.mid[m].unassoc) need_alpha = true;
+	need_alpha = need_alpha && J.in_alpha < J.in_nphys && J.df_atab != nullptr;
+	auto add_tap = [&](int src, dfl w, bool copy) {
+		const int py = J.crop_y + src;
+		dfl a = {1.0f, 0.0f};
+		if(need_alpha) a = df_of(J.df_atab[raw_code(J, px, py, J.in_alpha)]);
+#pragma unroll
+		for(int m = 0; m < dev::kMaxCh; m++) {
+			if(m >= J.mid_n || !((mask >> m) & 1u)) continue;
+			const DMid &mc = J.mid[m];
+			dfl v = {1.0f, 0.0f};
+			if(mc.in_ch < J.in_nphys) v = df_of(J.df_tab[m][raw_code(J, px, py, mc.in_ch)]);
+			if(mc.unassoc && need_alpha) v = df_mul(v, a);
+			if(copy) {
+				acc[m] = v;
+				A[m] = fabsf(v.hi);
+			}
+			else {
+				acc[m] = df_add(acc[m], df_mul(v, w));
+				A[m] = __fmaf_rn(fabsf(v.hi), fabsf(w.hi), A[m]);
+			}
+		}
+	};
+	if(W.kind == 1) {
+		const int src = W.src[j];
+		if(src >= 0) add_tap(src, {1.0f, 0.0f}, true);
+	}
+	else {
+		const int tb = W.off[j], te = W.off[j + 1];
+		n = te - tb;
+		for(int t = tb; t < te; t++) {
+			const int src = W.src[t];
+			if(src >= 0) add_tap(src, df_of(J.df_wv[t]), false);   // edge taps add 0
+		}
+	}
+	bool ok = true;
+	const float kd = (float)(24 * n) * 3.5527137e-15f + (float)(2 * n + 2) * 1.1102231e-16f;
+#pragma unroll
+	for(int m = 0; m < dev::kMaxCh; m++) {
+		if(m >= J.mid_n || !((mask >> m) & 1u)) continue;
+		const float delta = __fmaf_rn(A[m] * 1.01f, kd, 1e-30f);
+		out[m * stride] = acc[m].hi;
+		// A == 0: every term is exactly zero (the smallest nonzero term, a
+		// premultiplied code-1 sample times a weight, is far above the float
+		// underflow), so the reference's sum is a zero too; its sign never
+		// changes a later result or decision
+		ok = ok && (A[m] == 0.0f || rounds_to_hi(acc[m], delta));
+	}
+	return ok;
+}
+
+// Output code of every v in [vlo, vhi] as quantize_exact computes it;
+// 'ok' false if it is not the same code over the interval.
+__device__ __forceinline__ int quantize_interval(const DQuant &q, double vlo, double vhi, int x, int y, bool &ok)
+{
+	const int clo = quantize_exact(q, vlo, x, y), chi = quantize_exact(q, vhi, x, y);
+	if(clo != chi) ok = false;
+	if(q.dfam == IW_DITHERFAMILY_ORDERED && !q.use_nc) {
+		// the rounded dither fraction may wobble by a few ulps: keep away from the threshold
+		const double thr = ddiv((double)dither_rank(q.dsub, x, y) + 0.5, 64.0);
+		for(int e = 0; e < 2; e++) {
+			double v = e ? vhi : vlo;
+			if(v < 0.0) v = 0.0;
+			if(v > 1.0) v = 1.0;
+			if(v != v) continue;
+			const Bracket b = bracket_exact(q, v);
+			if(b.exact) continue;
+			const double f = ddiv(b.d_lo, dadd(b.d_lo, b.d_hi));
+			if(fabs(dsub(f, thr)) <= 1.8e-15) ok = false;
+		}
+	}
+	return clo;
+}
+
+// Re-evaluates flagged pixel (i, j) in double-float (whole warp); returns
+// true (warp-uniform) with the codes stored if every decision was certain.
+__device__ bool fix_pixel_df(const Job &J, int i, int j, unsigned int mask, float *my, int maxt, int lane)
+{
+	bool bad = false;
+	{
+		// one lane per horizontal tap, all masked channels at once
+		const DWeights &W = J.wh[J.mid[0].wh];
+		const int t0 = W.kind == 1 ? i : W.off[i];
+		const int nt = W.kind == 1 ? 1 : W.off[i + 1] - t0;
+		for(int t = lane; t < nt; t += 32) {
+			const int src = W.src[t0 + t];
+			if(src >= 0 && !interm_df_all(J, mask, src, j, my + t, maxt)) bad = true;
+		}
+	}
+	if(__any_sync(0xffffffffu, bad)) return false;
+	__syncwarp();
+	const bool mine = lane < J.mid_n && ((mask >> lane) & 1u);
+	dfl s = {0.0f, 0.0f};
+	float A = 0.0f;
+	int nh = 1;
+	if(mine) {
+		const DWeights &W = J.wh[J.mid[lane].wh];
+		if(W.kind == 1) {
+			if(W.src[i] >= 0) s.hi = my[lane * maxt];
+			A = fabsf(s.hi);
+		}
+		else {
+			const int t0 = W.off[i];
+			nh = W.off[i + 1] - t0;
+			for(int t = 0; t < nh; t++) {
+				if(W.src[t0 + t] < 0) continue;
+				const float I = my[lane * maxt + t];
+				const dfl w = df_of(J.df_wh[t0 + t]);
+				s = df_add(s, df_mul({I, 0.0f}, w));
+				A = __fmaf_rn(fabsf(I), fabsf(w.hi), A);
+			}
+		}
+	}
+	const float ds = __fmaf_rn(A * 1.01f, (float)(20 * nh) * 3.5527137e-15f + (float)(2 * nh + 2) * 1.1102231e-16f, 1e-30f);
+	// the float alpha the reference divides by
+	const int al = J.mid_alpha >= 0 ? J.mid_alpha : 0;
+	bool a_ok = true;
+	if(mine && lane == al && J.mid_alpha >= 0) a_ok = A == 0.0f || rounds_to_hi(s, ds);   // A == 0: exact zero
+	const float a32 = __shfl_sync(0xffffffffu, s.hi, al);
+	if(!__shfl_sync(0xffffffffu, a_ok ? 1 : 0, al)) return false;
+	int code = -1, oc = -1;
+	bool is_alpha = false, ok = true;
+	if(mine) {
+		const DMid &mc = J.mid[lane];
+		is_alpha = mc.ctype == IW_CHANNELTYPE_ALPHA;
+		oc = mc.out_ch;
+		dfl v = s;
+		float dv = ds;
+		if(mc.unassoc && a32 != 0.0f) {
+			v = df_div_f(s, a32);
+			dv = __fmaf_rn(fabsf(v.hi), 2.9e-14f + 1.2e-16f, __fdiv_rn(ds, fabsf(a32)) * 1.0001f);
+		}
+		if(oc >= 0) {
+			const double vd = dadd((double)v.hi, (double)v.lo);
+			const double d = (double)dv * 1.01 + fabs(vd) * 4.5e-16 + 1e-300;
+			code = quantize_interval(J.outc[oc].q, dsub(vd, d), dadd(vd, d), i, j, ok);
+		}
+	}
+	if(__any_sync(0xffffffffu, !ok)) return false;
+	const int ac = __shfl_sync(0xffffffffu, code, al);
+	const int alpha_code = (J.mid_alpha >= 0 && J.mid[al].out_ch >= 0) ? ac : -1;
+	if(code >= 0) {
+		if(!is_alpha) {
+			if(J.negate) code = J.outc[oc].maxcc - code;
+			if(J.blacken && alpha_code == 0) code = 0;
+		}
+		store_code(J, oc, i, j, (unsigned int)code);
+	}
+	return true;
+}
+
 // Exact re-evaluation of the pixels the fast form flagged, one warp per
 // pixel.  FP64 throughput is what limits this kernel, so the work is spread
 // over as many lanes as a pixel offers: first the lanes recompute the
@@ -557,7 +780,7 @@ __device__ __forceinline__ int nth_bit(unsigned int mask, int r)
 // quantisation -- with the alpha value and alpha code passed between lanes.
 // The result equals pixel_exact()'s.  Scratch: 'maxt' floats per channel per warp.
 template<bool BATCH>
-__global__ void k_fix_flagged_warp(Job J1, const Job *jobs, const int *count, const int *list, int maxt)
+__global__ void k_fix_flagged_warp(Job J1, const Job *jobs, int *count, const int *list, int maxt)
 {
 	extern __shared__ float fix_cache[];
 	const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, wpb = blockDim.x >> 5;
@@ -569,6 +792,12 @@ __global__ void k_fix_flagged_warp(Job J1, const Job *jobs, const int *count, co
 		const int p = e.x;
 		const unsigned int mask = (unsigned int)e.y & ((1u << J.mid_n) - 1u);
 		const int i = p % J.out_w, j = p / J.out_w;
+		if(J.df_wv && fix_pixel_df(J, i, j, mask, my, maxt, lane)) {
+			__syncwarp();
+			continue;
+		}
+		if(lane == 0) atomicAdd(count + 1, 1);   // pixels that needed the FP64 path
+		__syncwarp();
 		const int ntask = __popc(mask) * maxt;
 		for(int k = lane; k < ntask; k += 32) {
 			const int r = k / maxt, t = k - r * maxt;
@@ -620,7 +849,7 @@ __global__ void k_fix_flagged_warp(Job J1, const Job *jobs, const int *count, co
 
 // Fallback for very wide horizontal windows: one thread per flagged pixel.
 template<bool BATCH>
-__global__ void k_fix_flagged_thread(Job J1, const Job *jobs, const int *count, const int *list)
+__global__ void k_fix_flagged_thread(Job J1, const Job *jobs, int *count, const int *list)
 {
 	const int n = *count;
 	for(int f = blockIdx.x * blockDim.x + threadIdx.x; f < n; f += gridDim.x * blockDim.x) {
@@ -634,7 +863,7 @@ __global__ void k_fix_flagged_thread(Job J1, const Job *jobs, const int *count, 
 }
 
 // Launches the exact re-evaluation of flagged pixels on 'st'.
-void launch_fix_flagged(cudaStream_t st, const Job &J, const int *count, const int *list)
+void launch_fix_flagged(cudaStream_t st, const Job &J, int *count, const int *list)
 {
 	int maxt = 1;
 	for(int m = 0; m < J.mid_n; m++) maxt = maxt > J.wh[J.mid[m].wh].max_taps ? maxt : J.wh[J.mid[m].wh].max_taps;
@@ -649,7 +878,7 @@ void launch_fix_flagged(cudaStream_t st, const Job &J, const int *count, const i
 
 // The same for a batch: flag entries name their image in 'jobs' (device
 // memory); maxt is the widest horizontal window of any image.
-void launch_fix_flagged_batch(cudaStream_t st, const Job *jobs, int maxt, const int *count, const int *list)
+void launch_fix_flagged_batch(cudaStream_t st, const Job *jobs, int maxt, int *count, const int *list)
 {
 	const size_t per_warp = (size_t)dev::kMaxCh * maxt * sizeof(float);
 	int wpb = 4;
@@ -666,17 +895,25 @@ void launch_fix_flagged_batch(cudaStream_t st, const Job *jobs, int maxt, const 
 
 namespace {
 
+// Grow-only device buffer, allocated and freed in stream order on its lane's
+// stream, so growing it never waits for work on other streams (a plain
+// cudaFree would wait for the whole device).
 struct DevBuf {
 	void *p = nullptr;
 	size_t cap = 0;
+	cudaStream_t st = nullptr;
 	bool ensure(size_t n)
 	{
 		if(n <= cap) return true;
-		if(p) cudaFree(p);
+		if(p) cudaFreeAsync(p, st);
 		p = nullptr;
 		cap = 0;
-		size_t want = n + n / 8 + 4096;
-		if(cudaMalloc(&p, want) != cudaSuccess) { p = nullptr; return false; }
+		size_t want = n + n / 4 + 4096;
+		if(cudaMallocAsync(&p, want, st) != cudaSuccess) {
+			cudaGetLastError();
+			p = nullptr;
+			return false;
+		}
 		cap = want;
 		return true;
 	}
@@ -904,6 +1141,16 @@ bool ensure_init(DeviceState &S, std::string &err)
 		err = "cudaStreamCreate failed";
 		return false;
 	}
+	for(DevBuf *b : {&S.in, &S.interm, &S.out, &S.scan, &S.err, &S.params, &S.flags, &S.batch_io, &S.batch_tab})
+		b->st = S.stream;
+	{   // keep freed stream-ordered memory in the pool rather than returning it at every synchronise
+		cudaMemPool_t pool;
+		if(cudaDeviceGetDefaultMemPool(&pool, S.device) == cudaSuccess) {
+			unsigned long long keep = ~0ULL;
+			cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+		}
+		cudaGetLastError();
+	}
 	S.init = true;
 	return true;
 }
@@ -944,16 +1191,19 @@ template<class Mark>
 int plain_launch(cudaStream_t st, const Plan &P, const Job &J, Mark mark);
 
 // Transfer mode of a context: "gpu:upload" = "copy" (cudaMemcpy from / to the
-// caller's pageable buffers, the default: fastest measured on Grace), "stage"
-// (pinned staging with host copy threads) or "zero" (kernels read and write
-// the caller's host buffers in place; needs pageable memory access, and is
-// slow on the first touch of fresh pages).  'resident' runs need the input
-// on the device.
+// caller's pageable buffers), "stage" (pinned staging with host copy threads)
+// or "zero" (kernels read and write the caller's host buffers in place; needs
+// pageable memory access, and is slow on the first touch of fresh pages).
+// Default: "copy" for one image (fastest measured for a large image on
+// Grace), "stage" for batches (many pageable copies are slow one by one, and
+// they synchronise with work already queued).  'resident' runs need the
+// input on the device.
 enum { UP_ZERO = 0, UP_COPY = 1, UP_STAGE = 2 };
-static int upload_mode(iw_context *ctx, const DeviceState &S, bool resident)
+static int upload_mode(iw_context *ctx, const DeviceState &S, bool resident, bool many = false)
 {
 	const char *u = get_option(ctx, "gpu:upload");
-	int m = UP_COPY;
+	int m = many ? UP_STAGE : UP_COPY;
+	if(u && !strcmp(u, "copy")) m = UP_COPY;
 	if(u && !strcmp(u, "stage")) m = UP_STAGE;
 	else if(u && !strcmp(u, "zero")) m = UP_ZERO;
 	if(m == UP_ZERO && (!S.pageable || resident)) m = UP_COPY;
@@ -1182,10 +1432,18 @@ bool run_pipeline(iw_context *ctx, Plan &P, int warmup, int iters, int lane)
 	cudaError_t ce = cudaStreamSynchronize(st);
 	if(ce == cudaSuccess) ce = cudaGetLastError();
 	ctx->stats.flagged = 0;
+	ctx->stats.flagged_exact = 0;
 	if(ce == cudaSuccess && fast && fi.flag_count_dev) {
-		int nflag = 0;
-		ce = cudaMemcpy(&nflag, fi.flag_count_dev, sizeof(int), cudaMemcpyDeviceToHost);
-		ctx->stats.flagged = nflag;
+		int nflag[3] = {0, 0, 0};
+		ce = cudaMemcpy(nflag, fi.flag_count_dev, 3 * sizeof(int), cudaMemcpyDeviceToHost);
+		ctx->stats.flagged = nflag[0];
+		ctx->stats.flagged_exact = nflag[1];
+		if(ce == cudaSuccess && nflag[2]) {
+			fast_release(fi);
+			for(cudaEvent_t e : ev) cudaEventDestroy(e);
+			iw_set_error(ctx, "A device wait ran out of time (vertical pass)");
+			return false;
+		}
 	}
 	double total_ms = 0, part[8] = {0, 0, 0, 0, 0, 0, 0, 0};
 	if(ce == cudaSuccess && marks_per_it >= 2) {
@@ -1247,8 +1505,8 @@ bool run_batch(const std::vector<iw_context *> &ctxs, const std::vector<Plan *> 
 	}
 	if(sel.empty()) return true;
 
-	// one transfer mode for the batch: the first image's (as run_pipeline)
-	const int upmode = upload_mode(ctxs[sel[0]], S, false);
+	// one transfer mode for the batch: the first image's
+	const int upmode = upload_mode(ctxs[sel[0]], S, false, true);
 	const bool zc = upmode == UP_ZERO;
 	// buffers of every image, the packed weight lists and the flag list in one block
 	size_t top = 0;
@@ -1329,6 +1587,9 @@ bool run_batch(const std::vector<iw_context *> &ctxs, const std::vector<Plan *> 
 	for(int k = 0; k < m; k++) {
 		fast_item_place(items[k], tbase + o_blob[k], flag_count, flag_list, k);
 		maxt = std::max(maxt, fast_item_htaps(items[k]));
+		// the job record gets the image's placed double-float pointers
+		fast_item_job_df(items[k], djobs[k]);
+		memcpy(tab.data() + o_jobs + (size_t)k * sizeof(Job), &djobs[k], sizeof(Job));
 	}
 
 	cudaStream_t st = S.stream;
@@ -1350,9 +1611,13 @@ bool run_batch(const std::vector<iw_context *> &ctxs, const std::vector<Plan *> 
 		}
 		if(!stage_h2d(S.stager, st, xs)) return fail_all("Out of pinned host memory");
 	}
-	cudaMemsetAsync(flag_count, 0, sizeof(int), st);
+	cudaMemsetAsync(flag_count, 0, 3 * sizeof(int), st);
+	cudaEvent_t ev_h, ev_f;
+	cudaEventCreate(&ev_h);
+	cudaEventCreate(&ev_f);
 	cudaEventRecord(e0, st);
-	int launches = fast_launch_batch(st, items.data(), m, err);
+	int launches = fast_launch_batch(st, items.data(), m, err, ev_h);
+	cudaEventRecord(ev_f, st);
 	if(launches >= 0) {
 		launch_fix_flagged_batch(st, (const Job *)(tbase + o_jobs), maxt, flag_count, flag_list);
 		launches++;
@@ -1373,12 +1638,23 @@ bool run_batch(const std::vector<iw_context *> &ctxs, const std::vector<Plan *> 
 	}
 	cudaError_t ce = cudaStreamSynchronize(st);
 	if(ce == cudaSuccess) ce = cudaGetLastError();
-	int nflagged = 0;
-	float ms = 0;
-	if(ce == cudaSuccess) ce = cudaMemcpy(&nflagged, flag_count, sizeof(int), cudaMemcpyDeviceToHost);
-	if(ce == cudaSuccess) cudaEventElapsedTime(&ms, e0, e1);
+	int nflagged[3] = {0, 0, 0};
+	float ms = 0, ms_v = 0, ms_h = 0, ms_f = 0;
+	if(ce == cudaSuccess) ce = cudaMemcpy(nflagged, flag_count, 3 * sizeof(int), cudaMemcpyDeviceToHost);
+	if(ce == cudaSuccess && nflagged[2]) {
+		err = "A device wait ran out of time (vertical pass); nothing was written";
+		launches = -1;
+	}
+	if(ce == cudaSuccess) {
+		cudaEventElapsedTime(&ms, e0, e1);
+		cudaEventElapsedTime(&ms_v, e0, ev_h);
+		cudaEventElapsedTime(&ms_h, ev_h, ev_f);
+		cudaEventElapsedTime(&ms_f, ev_f, e1);
+	}
 	cudaEventDestroy(e0);
 	cudaEventDestroy(e1);
+	cudaEventDestroy(ev_h);
+	cudaEventDestroy(ev_f);
 	if(launches < 0) return fail_all(err.c_str());
 	if(ce != cudaSuccess) {
 		std::string msg = std::string("CUDA error: ") + cudaGetErrorString(ce);
@@ -1391,7 +1667,11 @@ bool run_batch(const std::vector<iw_context *> &ctxs, const std::vector<Plan *> 
 		ctx->stats.zero_copy = zc;
 		ctx->stats.kernels = launches;
 		ctx->stats.ms_device = ms;
-		ctx->stats.flagged = nflagged;
+		ctx->stats.ms_part[0] = ms_v;
+		ctx->stats.ms_part[1] = ms_h;
+		ctx->stats.ms_part[2] = ms_f;
+		ctx->stats.flagged = nflagged[0];
+		ctx->stats.flagged_exact = nflagged[1];
 		status[item_img[k]] = 1;
 		fast_item_free(items[k]);
 	}
@@ -1425,7 +1705,7 @@ bool run_batch_plain(const std::vector<iw_context *> &ctxs, const std::vector<Pl
 		sel.push_back(i);
 	}
 	if(sel.empty()) return true;
-	const int upmode = upload_mode(ctxs[sel[0]], S, false);
+	const int upmode = upload_mode(ctxs[sel[0]], S, false, true);
 	const bool zc = upmode == UP_ZERO;
 	size_t top = 0;
 	auto take = [&](size_t bytes) { size_t at = (top + 255) & ~(size_t)255; top = at + bytes; return at; };
@@ -1581,6 +1861,7 @@ extern "C" int iwg_get_stats(struct iw_context *ctx, struct iwg_stats *out)
 	out->form = ctx->stats.form;
 	out->kernels = ctx->stats.kernels;
 	out->zero_copy = ctx->stats.zero_copy;
+	out->flagged_exact = ctx->stats.flagged_exact;
 	return 1;
 }
 

@@ -29,11 +29,13 @@ struct iwg_stats {
 	double ms_part[4];     /* the same, per launch group: [0] vertical pass,
 	                          [1] horizontal pass + quantisation, [2] exact
 	                          re-evaluation (fp32 form) or serial dither scan */
-	long long flagged;     /* pixels recomputed in FP64 by the fp32 form */
+	long long flagged;     /* pixels the fp32 form re-evaluated (double-float, then FP64) */
 	int form;              /* 0 = fp64, 1 = fp32 + guard band */
 	int kernels;           /* kernel launches per pass */
 	int zero_copy;         /* 1: kernels read the input and wrote the output in
 	                          host memory directly (no staging copies) */
+	long long flagged_exact; /* of the flagged pixels, those the double-float
+	                          tier could not decide and FP64 recomputed */
 };
 
 /* Copies the statistics of the context's last run into *out.  Returns 1. */

@@ -112,3 +112,4 @@ def test_stats_report_form(gpulib):
         assert st.form == want
         if form == "fp32":
             assert st.flagged < 0.05 * 250 * 250
+            assert 0 <= st.flagged_exact <= st.flagged
