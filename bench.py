@@ -400,6 +400,7 @@ def serving_leg(lib: IWLib, rate: float, seconds: float, thumbs, ups):
     srv = d.iwg_server_create(8 << 30, 0, 0)
     ready = queue.Queue(maxsize=512)
     lat = {}
+    phases = {}
     out_px = {}
     stop = threading.Event()
 
@@ -418,6 +419,7 @@ def serving_leg(lib: IWLib, rate: float, seconds: float, thumbs, ups):
             for i in range(n):
                 k = buf[i].tag
                 lat[k] = (buf[i].latency_ms, buf[i].ok)
+                phases[k] = (buf[i].planned_ms, buf[i].started_ms, buf[i].ran_ms, buf[i].latency_ms)
                 lib.iw_destroy_context(ctxs.pop(k))
             if stop.is_set() and len(lat) >= len(sched):
                 break
@@ -452,10 +454,20 @@ def serving_leg(lib: IWLib, rate: float, seconds: float, thumbs, ups):
     pct = lambda q: ls[min(len(ls) - 1, int(q * len(ls)))] if ls else None
     done_px = sum(out_px[k] for k in snap)
 
+    ph = dict(phases)
+
     def cls(sel):
-        v = sorted(snap[k][0] for k in snap if sel(sched[k]))
+        keys = [k for k in snap if sel(sched[k])]
+        v = sorted(snap[k][0] for k in keys)
+        med = lambda xs: sorted(xs)[len(xs) // 2] if xs else None
+        # median time in each stage: planning (submit -> planned), waiting for
+        # the device, on the device, post-pass
+        stages = {"plan": med([ph[k][0] for k in keys if k in ph]),
+                  "wait": med([ph[k][1] - ph[k][0] for k in keys if k in ph]),
+                  "device": med([ph[k][2] - ph[k][1] for k in keys if k in ph]),
+                  "post": med([ph[k][3] - ph[k][2] for k in keys if k in ph])}
         return {"n": len(v), "p50_ms": v[len(v) // 2] if v else None,
-                "p99_ms": v[min(len(v) - 1, int(0.99 * len(v)))] if v else None}
+                "p99_ms": v[min(len(v) - 1, int(0.99 * len(v)))] if v else None, "stage_p50_ms": stages}
     return {"rate_req_s": rate, "seconds": seconds, "requests": len(sched), "completed": len(snap),
             "failed": sum(1 for v in snap.values() if not v[1]),
             "errdiff_requests": sum(1 for x in sched if x[2]), "upscale_requests": sum(1 for x in sched if x[1] == "up"),
@@ -467,7 +479,8 @@ def serving_leg(lib: IWLib, rate: float, seconds: float, thumbs, ups):
                          "errdiff_up": cls(lambda x: x[1] == "up" and x[2])},
             "lanes": {"batches": info.batches, "batched_requests": info.batched_requests,
                       "device_ms": info.device_ms, "scan_lane_batches": info.slow_batches,
-                      "scan_lane_requests": info.slow_requests, "scan_lane_device_ms": info.slow_device_ms}}
+                      "scan_lane_requests": info.slow_requests, "scan_lane_device_ms": info.slow_device_ms,
+                      "batch_wall_ms": info.batch_wall_ms, "rest_wall_ms": info.rest_wall_ms, "plan_ms": info.plan_ms}}
 
 
 def main():

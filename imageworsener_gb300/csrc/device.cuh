@@ -34,6 +34,7 @@ struct DQuant {
 	const int *code;       // P+2
 	const double *rev;     // maxcc+1
 	const double *nc;      // 255
+	const long long *rec;  // error diffusion: 8 words per bracket (P+1)
 	const float *Uf;       // float copies (fast form)
 	const float *revf;
 };

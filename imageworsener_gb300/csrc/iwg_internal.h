@@ -68,6 +68,11 @@ struct Quant {
 	std::shared_ptr<const std::vector<int>> code;    // P+2: bracket -> output code (code[P+1] = code[P])
 	std::shared_ptr<const std::vector<double>> rev;  // M+1: code -> linear value
 	std::shared_ptr<const std::vector<double>> nc;   // 255 midpoints (use_nc only)
+	// error diffusion only: per bracket k, 8 words {U[k], U[k+1], X[k], C[k]
+	// (bit patterns), rev[code[k]], rev[code[k+1]] (bit patterns),
+	// code[k] | code[k+1] << 32, 0}, where C[k] is the least v whose ceiling
+	// is at least as near as its floor (rev_hi - v <= v - rev_lo, each rounded)
+	std::shared_ptr<const std::vector<long long>> rec;
 };
 
 // ---------------------------------------------------------------------------
@@ -267,6 +272,10 @@ void nc_fill(int cstype, double gamma, double *nc);
 void optimize(iw_context *ctx);
 
 // pipeline.cu
+// Device lanes (independent streams, buffers and table caches): lane 0 serves
+// the public entry points; a request server runs its serial dither scans on
+// lanes 1 .. kLanes-1.
+constexpr int kLanes = 5;
 bool run_pipeline(iw_context *ctx, Plan &P, int warmup = 0, int iters = 1, int lane = 0);
 // Whether an output channel is quantised by a serial scan (api.cpp).
 bool plan_needs_scan(const Plan &P);

@@ -283,83 +283,184 @@ __device__ __forceinline__ int bracket_index(const DQuant &q, long long vb)
 	return lo;
 }
 
+// One bracket's decision record (the 8 words of DQuant::rec).
+struct EdRec {
+	long long lo, hi, x, c;   // bit patterns: U[k], U[k+1], X[k], C[k]
+	double rev_lo, rev_hi;
+	int code_lo, code_hi;
+};
+
+__device__ __forceinline__ EdRec ed_rec(const long long *rec, int k)
+{
+	const longlong2 *r = reinterpret_cast<const longlong2 *>(rec + 8 * (long long)k);
+	const longlong2 a = __ldg(r), b = __ldg(r + 1), c = __ldg(r + 2), d = __ldg(r + 3);
+	EdRec e;
+	e.lo = a.x; e.hi = a.y; e.x = b.x; e.c = b.y;
+	e.rev_lo = __longlong_as_double(c.x);
+	e.rev_hi = __longlong_as_double(c.y);
+	e.code_lo = (int)(unsigned int)(unsigned long long)d.x;
+	e.code_hi = (int)(unsigned int)((unsigned long long)d.x >> 32);
+	return e;
+}
+
+__device__ __forceinline__ bool is_nan_bits(double v)
+{
+	return (__double_as_longlong(v) & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL;
+}
+
 // Error diffusion of one channel by one warp.  Per row:
-//   1. all lanes clamp the row's values and find their brackets (the value
-//      before its error is added; the error moves it by about one code);
+//   1. all lanes clamp the row's values and find their brackets and the
+//      brackets' bounds (the value before its error is added; the error moves
+//      it by about one code);
 //   2. lane 0 walks the samples in the reference's order doing only what
 //      the next sample depends on -- the value plus its accumulated error
 //      (the error carried from the previous rows plus the two in-row
 //      contributions, kept in registers and added in the reference's order),
-//      the decision from the nearby bracket, and the sample's error;
+//      the decision, and the sample's error;
 //   3. all lanes send the row's errors to the next two rows (e1, e2), each
 //      lane owning target positions and adding the contributions in the order
-//      the reference adds them (sample x-2f, x-f, x, x+f, x+2f); rows shift.
-// Error buffer of a channel: e0, e1, e2 and the row's errors, out_w doubles
-// each; the staged chunk lives in shared memory (kScanChunk samples).
-__device__ void errdiff_warp(const Job &J, int oc, double *sv, double *se, int *sk)
+//      the reference adds them (sample x-2f, x-f, x, x+f, x+2f); rows rotate.
+// On GB300 every FP64 instruction holds the SM sub-partition's FP64 unit for
+// tens of cycles whether one lane or 32 are active, and the walk is one
+// dependent chain, so step 2 is kept short: four FP64 operations per sample
+// for Floyd-Steinberg (the in-row product and sum, the value plus error, the
+// sample's error) and a few integer ones -- the bracket from the staged
+// bounds, one record load, two compares for the decision.  Products with a
+// zero weight are skipped: they add a signed zero to an accumulator that
+// starts at +0 and can never become -0 (a sum of nonzero values that cancels
+// is +0), which leaves it unchanged.
+// Error buffer of a channel: three rotating error rows and the row's errors,
+// out_w doubles each; the staged chunk lives in shared memory (kScanChunk).
+__device__ __forceinline__ void errdiff_warp(const Job &J, int oc)
 {
+	__shared__ double s_v[dev::kMaxCh][kScanChunk], s_e[dev::kMaxCh][kScanChunk];
+	__shared__ long long s_lo[dev::kMaxCh][kScanChunk], s_hi[dev::kMaxCh][kScanChunk];
+	__shared__ int s_k[dev::kMaxCh][kScanChunk];
+	double *const sv = s_v[oc], *const se = s_e[oc];
+	long long *const slo = s_lo[oc], *const shi = s_hi[oc];
+	int *const sk = s_k[oc];
 	const int lane = threadIdx.x & 31;
 	const DOut &o = J.outc[oc];
 	const DQuant &q = o.q;
-	const int W = J.out_w;
-	double *e0 = J.errbuf + (unsigned long long)oc * 5 * W, *e1 = e0 + W, *e2 = e1 + W, *er = e2 + W;
-	const long long *U = reinterpret_cast<const long long *>(q.U);
-	const long long *X = reinterpret_cast<const long long *>(q.X);
+	const int W = J.out_w, H = J.out_h, P = q.P;
+	const long long *const U = reinterpret_cast<const long long *>(q.U);
+	const long long *const rec = q.rec;
+	uint8_t *const out = J.out;
+	const unsigned long long out_bpr = J.out_bpr;
+	const int out_n = J.out_n, wide = J.out_depth == 8 ? 0 : 1;
+	const double *const scan = J.scanbuf + (unsigned long long)oc * H * W;
+	double *e0 = J.errbuf + (unsigned long long)oc * 5 * W, *e1 = e0 + W, *e2 = e1 + W;
+	double *const er = e2 + W;
 	double c[12];
 	errdiff_weights(q.dsub, c);
+	bool nz1[5], nz2[5];   // nonzero weights toward the next row / the row after, source offset k = -2..2
+	bool any2 = false;
+#pragma unroll
+	for(int k = 0; k < 5; k++) {
+		nz1[k] = c[6 - k] != 0.0;
+		nz2[k] = c[11 - k] != 0.0;
+		any2 = any2 || nz2[k];
+	}
+	const bool c1nz = c[1] != 0.0;
+	const double c0 = c[0], c1 = c[1];
 	for(int x = lane; x < 3 * W; x += 32) e0[x] = 0.0;
 	__syncwarp();
 	const double skip = __longlong_as_double(0x7ff8dead0000beefLL);   // a NaN: the sample sent no error
-	for(int y = 0; y < J.out_h; y++) {
+	for(int y = 0; y < H; y++) {
 		const int f = (y % 2) ? -1 : 1;
-		const double *row = J.scanbuf + ((unsigned long long)oc * J.out_h + y) * W;
+		const double *row = scan + (unsigned long long)y * W;
+		uint8_t *const orow = out + (unsigned long long)y * out_bpr + ((size_t)oc << wide);
 		double err1 = 0.0, err2 = 0.0;     // errors of the previous two samples of the row
 		bool has1 = false, has2 = false;
 		for(int z0 = 0; z0 < W; z0 += kScanChunk) {
 			const int cn = min(kScanChunk, W - z0);
-			// stage the chunk (in processing order): value, carried error, bracket
-			for(int zz = lane; zz < cn; zz += 32) {
-				const int x = (y % 2) ? W - 1 - (z0 + zz) : z0 + zz;
-				double v = row[x];
-				sv[zz] = v;
-				se[zz] = e0[x];
-				if(v < 0.0) v = 0.0;
-				if(v > 1.0) v = 1.0;
-				sk[zz] = v == v ? bracket_index(q, __double_as_longlong(dadd(v, 0.0))) : 0;
+			const int xb = (y % 2) ? W - 1 - z0 : z0;   // x of the chunk's first sample
+			// stage the chunk (in processing order): clamped value, carried
+			// error, bracket (-1 for NaN) and the bracket's bounds
+			{
+				constexpr int kPer = kScanChunk / 32;
+				double rv[kPer], re[kPer];
+#pragma unroll
+				for(int i = 0; i < kPer; i++) {   // all loads first: they overlap
+					const int zz = lane + 32 * i;
+					const int x = xb + zz * f;
+					rv[i] = zz < cn ? row[x] : 0.0;
+					re[i] = zz < cn ? e0[x] : 0.0;
+				}
+#pragma unroll
+				for(int i = 0; i < kPer; i++) {
+					const int zz = lane + 32 * i;
+					if(zz >= cn) break;
+					const double v = clamp01_bits(rv[i]);   // +0 for any negative value, NaN kept
+					sv[zz] = v;
+					se[zz] = re[i];
+					const int k = is_nan_bits(v) ? -1 : bracket_index(q, __double_as_longlong(v));
+					sk[zz] = k;
+					slo[zz] = k < 0 ? 0 : __ldg(U + k);
+					shi[zz] = k < 0 ? 0 : __ldg(U + k + 1);
+				}
 			}
 			__syncwarp();
 			if(lane == 0) {
+				double s_n = sv[0], e_n = se[0];
+				long long lo_n = slo[0], hi_n = shi[0];
+				int k_n = sk[0];
 				for(int zz = 0; zz < cn; zz++) {
-					const int x = (y % 2) ? W - 1 - (z0 + zz) : z0 + zz;
+					const int x = xb + zz * f;
+					const double sval = s_n;
+					double e = e_n;
+					const long long lo0 = lo_n, hi0 = hi_n;
+					const int k0 = k_n;
+					if(zz + 1 < cn) {   // the next sample's staged values, ahead of the chain
+						s_n = sv[zz + 1];
+						e_n = se[zz + 1];
+						lo_n = slo[zz + 1];
+						hi_n = shi[zz + 1];
+						k_n = sk[zz + 1];
+					}
+					// the records of the staged bracket and its neighbours, loaded
+					// while the FP64 chain runs
+					const int kc = k0 < 0 ? 0 : k0;
+					const EdRec rm = ed_rec(rec, kc > 0 ? kc - 1 : 0), r0 = ed_rec(rec, kc),
+						rp = ed_rec(rec, kc < P ? kc + 1 : P);
 					// e0[x] as the reference has it when it reaches x: the carried
-					// error, then x-2f's contribution (known a sample earlier, off
-					// the dependency chain), then x-f's
-					double e = se[zz];
-					if(has2) e = dadd(e, dmul(err2, c[1]));
-					if(has1) e = dadd(e, dmul(err1, c[0]));
-					const double v = clamp01_bits(dadd(clamp01_bits(sv[zz]), e));
-					const long long vb = __double_as_longlong(v);
-					int code;
+					// error, then x-2f's contribution, then x-f's
+					if(has2 && c1nz) e = dadd(e, dmul(err2, c1));
+					if(has1) e = dadd(e, dmul(err1, c0));
+					int code = 0;
 					double err = skip;
 					bool sent = false;
-					if((vb & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL) code = 0;   // NaN
-					else {
-						int k = sk[zz];
-						while(k < q.P && __ldg(U + k + 1) <= vb) k++;
-						while(k > 0 && __ldg(U + k) > vb) k--;
-						const int lo = q.code[k], hi = q.code[k + 1];
-						if(k == q.P || vb < __ldg(X + k)) code = lo;
-						else {
-							const double d_lo = dsub(v, q.rev[lo]), d_hi = dsub(q.rev[hi], v);
-							if(dle_bits(d_hi, d_lo)) { err = -d_hi; code = hi; }
-							else { err = d_lo; code = lo; }
+					if(k0 >= 0) {
+						// the reference's clamp; the value is not NaN here
+						const double w = dadd(sval, e);
+						const long long wb = __double_as_longlong(w);
+						const double v = wb < 0 ? 0.0 : (wb > 0x3ff0000000000000LL ? 1.0 : w);
+						const long long vb = __double_as_longlong(v);
+						const bool below = vb < lo0, above = vb >= hi0;
+						EdRec r = below ? rm : (above ? rp : r0);
+						if((below && vb < rm.lo) || (above && vb >= rp.hi)) {   // moved more than one bracket
+							int k = k0;
+							while(k < P && __ldg(U + k + 1) <= vb) k++;
+							while(k > 0 && __ldg(U + k) > vb) k--;
+							r = ed_rec(rec, k);
+						}
+						code = r.code_lo;
+						if(vb >= r.x) {   // not exact (X[P] is +inf)
+							const bool up = vb >= r.c;
+							code = up ? r.code_hi : r.code_lo;
+							err = dsub(v, up ? r.rev_hi : r.rev_lo);
 							sent = true;
 						}
 					}
 					er[x] = err;
 					err2 = err1; has2 = has1;
 					err1 = err; has1 = sent;
-					store_code(J, oc, x, y, (unsigned int)code);
+					uint8_t *const p = orow + ((size_t)x * out_n << wide);
+					if(wide) {
+						p[0] = (uint8_t)(code >> 8);
+						p[1] = (uint8_t)(code & 0xff);
+					}
+					else p[0] = (uint8_t)code;
 				}
 			}
 			__syncwarp();
@@ -368,23 +469,23 @@ __device__ void errdiff_warp(const Job &J, int oc, double *sv, double *se, int *
 			double a1 = e1[t], a2 = e2[t];
 #pragma unroll
 			for(int k = -2; k <= 2; k++) {          // source sample t + k*f, in processing order
+				if(!nz1[k + 2] && !nz2[k + 2]) continue;
 				const int qx = t + k * f;
 				if(qx < 0 || qx >= W) continue;
 				const double err = er[qx];
-				if(err != err) continue;
-				a1 = dadd(a1, dmul(err, c[4 - k]));
-				a2 = dadd(a2, dmul(err, c[9 - k]));
+				if(is_nan_bits(err)) continue;
+				if(nz1[k + 2]) a1 = dadd(a1, dmul(err, c[4 - k]));
+				if(nz2[k + 2]) a2 = dadd(a2, dmul(err, c[9 - k]));
 			}
 			e1[t] = a1;
-			e2[t] = a2;
+			if(any2) e2[t] = a2;
+			e0[t] = 0.0;   // becomes the row after next
 		}
 		__syncwarp();
-		for(int t = lane; t < W; t += 32) {
-			e0[t] = e1[t];
-			e1[t] = e2[t];
-			e2[t] = 0.0;
-		}
-		__syncwarp();
+		double *t0 = e0;
+		e0 = e1;
+		e1 = e2;
+		e2 = t0;
 	}
 }
 
@@ -492,10 +593,8 @@ __device__ void random_warp(const Job &J, int oc)
 // One warp per output channel of the image (at most four warps per block).
 __device__ __forceinline__ void scan_warp(const Job &J, int oc)
 {
-	__shared__ double s_v[dev::kMaxCh][kScanChunk], s_e[dev::kMaxCh][kScanChunk];
-	__shared__ int s_k[dev::kMaxCh][kScanChunk];
 	if(oc >= J.out_n || oc >= dev::kMaxCh || !J.outc[oc].scan) return;
-	if(J.outc[oc].q.dfam == IW_DITHERFAMILY_ERRDIFF) errdiff_warp(J, oc, s_v[oc], s_e[oc], s_k[oc]);
+	if(J.outc[oc].q.dfam == IW_DITHERFAMILY_ERRDIFF) errdiff_warp(J, oc);
 	else random_warp(J, oc);
 }
 
@@ -1011,9 +1110,29 @@ void copy_pieces(const std::vector<Piece> &pieces)
 
 struct Xfer { uint8_t *dev; uint8_t *host; size_t n; };
 
+// Waits for an event or a stream.  A patient wait sleeps between queries
+// instead of spinning: lanes that wait seconds for a serial scan must not take
+// host cores from the planning and copying threads.
+cudaError_t wait_event(cudaEvent_t e, bool patient)
+{
+	if(!patient) return cudaEventSynchronize(e);
+	cudaError_t r;
+	while((r = cudaEventQuery(e)) == cudaErrorNotReady) std::this_thread::sleep_for(std::chrono::microseconds(200));
+	return r;
+}
+
+cudaError_t wait_stream(cudaStream_t st, bool patient)
+{
+	if(!patient) return cudaStreamSynchronize(st);
+	cudaError_t r;
+	while((r = cudaStreamQuery(st)) == cudaErrorNotReady) std::this_thread::sleep_for(std::chrono::microseconds(200));
+	return r;
+}
+
 struct Stager {
 	uint8_t *pin[2] = {nullptr, nullptr};
 	size_t half = 0;
+	bool patient = false;
 	cudaEvent_t ev[2] = {nullptr, nullptr};
 	bool ensure()
 	{
@@ -1046,9 +1165,9 @@ bool stage_h2d(Stager &G, cudaStream_t st, const std::vector<Xfer> &items)
 		dma.clear();
 		fill = 0;
 		slot ^= 1;
-		cudaEventSynchronize(G.ev[slot]);   // the other half is free again
+		wait_event(G.ev[slot], G.patient);   // the other half is free again
 	};
-	cudaEventSynchronize(G.ev[0]);
+	wait_event(G.ev[0], G.patient);
 	for(const Xfer &x : items) {
 		size_t off = 0;
 		while(off < x.n) {
@@ -1092,7 +1211,7 @@ bool stage_d2h(Stager &G, cudaStream_t st, const std::vector<Xfer> &items)
 	};
 	for(size_t g = 0; g < groups.size() && g < 2; g++) issue(g);
 	for(size_t g = 0; g < groups.size(); g++) {
-		if(cudaEventSynchronize(G.ev[g & 1]) != cudaSuccess) return false;
+		if(wait_event(G.ev[g & 1], G.patient) != cudaSuccess) return false;
 		std::vector<Piece> out = groups[g].out;
 		for(Piece &p : out) p.src = G.pin[g & 1] + (uintptr_t)p.src;
 		copy_pieces(out);
@@ -1105,6 +1224,7 @@ bool stage_d2h(Stager &G, cudaStream_t st, const std::vector<Xfer> &items)
 // device copies of the shared host tables.  Calls are serialised on it.
 struct DeviceState {
 	std::mutex mu;
+	int lane = 0;
 	bool init = false;
 	std::string init_error;
 	int device = 0;
@@ -1118,12 +1238,20 @@ struct DeviceState {
 };
 
 // Lanes: independent device states (stream, buffers, table cache), so that a
-// request server can keep a lane of long serial work (dither scans) apart
-// from its batches.  Lane 0 serves the public entry points.
+// request server can keep long serial work (dither scans) on lanes of its own,
+// apart from its batches and from each other.  Lane 0 serves the public entry
+// points.  A lane's stream and buffers are created on its first use.
 DeviceState &state(int lane = 0)
 {
-	static DeviceState *s[2] = {new DeviceState(), new DeviceState()};   // never destroyed: outlive other statics
-	return *s[lane & 1];
+	static DeviceState *s[kLanes] = {};   // never destroyed: outlive other statics
+	static std::once_flag once;
+	std::call_once(once, [] {
+		for(int k = 0; k < kLanes; k++) {
+			s[k] = new DeviceState();
+			s[k]->lane = k;
+		}
+	});
+	return *s[(unsigned)lane % (unsigned)kLanes];
 }
 
 bool ensure_init(DeviceState &S, std::string &err)
@@ -1137,17 +1265,28 @@ bool ensure_init(DeviceState &S, std::string &err)
 	}
 	cudaGetDevice(&S.device);
 	cudaDeviceGetAttribute(&S.pageable, cudaDevAttrPageableMemoryAccess, S.device);
-	if(cudaStreamCreateWithFlags(&S.stream, cudaStreamNonBlocking) != cudaSuccess) {
+	// lane 0 (the public entry points, a server's batches) on the highest
+	// priority: the block scheduler then serves it first while long scans of
+	// other lanes hold part of the GPU
+	int least = 0, greatest = 0;
+	cudaDeviceGetStreamPriorityRange(&least, &greatest);
+	if(cudaStreamCreateWithPriority(&S.stream, cudaStreamNonBlocking, S.lane == 0 ? greatest : least) != cudaSuccess) {
 		err = "cudaStreamCreate failed";
 		return false;
 	}
 	for(DevBuf *b : {&S.in, &S.interm, &S.out, &S.scan, &S.err, &S.params, &S.flags, &S.batch_io, &S.batch_tab})
 		b->st = S.stream;
-	{   // keep freed stream-ordered memory in the pool rather than returning it at every synchronise
+	S.stager.patient = S.lane != 0;
+	{   // keep freed stream-ordered memory in the pool rather than returning it at
+		// every synchronise; and never let an allocation on one lane reuse memory
+		// whose free on another lane's stream is still pending (the pool would
+		// make the first stream wait for the second, e.g. behind a long scan)
 		cudaMemPool_t pool;
 		if(cudaDeviceGetDefaultMemPool(&pool, S.device) == cudaSuccess) {
 			unsigned long long keep = ~0ULL;
 			cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+			int no = 0;
+			cudaMemPoolSetAttribute(pool, cudaMemPoolReuseAllowInternalDependencies, &no);
 		}
 		cudaGetLastError();
 	}
@@ -1321,7 +1460,8 @@ static bool make_job(iw_context *ctx, const Plan &P, DeviceState &S, Packer &pk,
 		D.q.code = cached_table(S, q.code);
 		D.q.rev = cached_table(S, q.rev);
 		D.q.nc = cached_table(S, q.nc);
-		if(!D.q.U || !D.q.X || !D.q.code || !D.q.rev || (q.use_nc && !D.q.nc)) {
+		D.q.rec = cached_table(S, q.rec);
+		if(!D.q.U || !D.q.X || !D.q.code || !D.q.rev || (q.use_nc && !D.q.nc) || (q.rec && !D.q.rec)) {
 			iw_set_error(ctx, "Out of GPU memory (tables)");
 			return false;
 		}
@@ -1429,7 +1569,7 @@ bool run_pipeline(iw_context *ctx, Plan &P, int warmup, int iters, int lane)
 	}
 	if(upmode == UP_COPY) cudaMemcpyAsync(ctx->img2.pixels, S.out.p, out_bytes, cudaMemcpyDeviceToHost, st);
 	if(upmode == UP_STAGE) stage_d2h(S.stager, st, {Xfer{(uint8_t *)S.out.p, (uint8_t *)ctx->img2.pixels, out_bytes}});
-	cudaError_t ce = cudaStreamSynchronize(st);
+	cudaError_t ce = wait_stream(st, S.lane != 0);
 	if(ce == cudaSuccess) ce = cudaGetLastError();
 	ctx->stats.flagged = 0;
 	ctx->stats.flagged_exact = 0;
@@ -1636,7 +1776,7 @@ bool run_batch(const std::vector<iw_context *> &ctxs, const std::vector<Plan *> 
 		}
 		stage_d2h(S.stager, st, xs);
 	}
-	cudaError_t ce = cudaStreamSynchronize(st);
+	cudaError_t ce = wait_stream(st, S.lane != 0);
 	if(ce == cudaSuccess) ce = cudaGetLastError();
 	int nflagged[3] = {0, 0, 0};
 	float ms = 0, ms_v = 0, ms_h = 0, ms_f = 0;
@@ -1804,7 +1944,7 @@ bool run_batch_plain(const std::vector<iw_context *> &ctxs, const std::vector<Pl
 	if(upmode == UP_COPY)
 		for(const Xfer &x : xout) cudaMemcpyAsync(x.host, x.dev, x.n, cudaMemcpyDeviceToHost, st);
 	if(upmode == UP_STAGE) stage_d2h(S.stager, st, xout);
-	cudaError_t ce = cudaStreamSynchronize(st);
+	cudaError_t ce = wait_stream(st, S.lane != 0);
 	if(ce == cudaSuccess) ce = cudaGetLastError();
 	float ms = 0;
 	if(ce == cudaSuccess) cudaEventElapsedTime(&ms, e0, e1);

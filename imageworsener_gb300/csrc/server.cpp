@@ -10,9 +10,15 @@
 //     the GPU are planned meanwhile and join the next batch, so the GPU goes
 //     from one batch to the next without waiting for the host.  Requests
 //     with error-diffusion or random dither end in a serial scan that can take
-//     far longer than a batch; a second dispatcher runs them on a second
-//     device lane (own stream and buffers), concurrently with the batches;
-//   * finishing: the output post-pass, then the request is reported done.
+//     far longer than a batch; they go to scan workers, each with a device
+//     lane of its own (stream and buffers), running concurrently with the
+//     batches and with each other.  Small and large scans queue apart and have
+//     workers of their own, so a small request never waits behind a long scan;
+//     a worker runs everything of its class that is queued as one batch (one
+//     block per image, all scans at once);
+//   * finishing: the output post-pass, then the request is reported done;
+//     large outputs have finishing threads of their own, so that the
+//     post-pass of a large image never delays a small one.
 // Each request's bytes equal what iw_process_image() gives it alone.
 #include "iwg_internal.h"
 #include "imagew_gb300.h"
@@ -37,6 +43,8 @@ struct Request {
 	int ok = 0;
 	SrvClock::time_point t_submit;
 	double latency_ms = 0;
+	double planned_ms = 0, started_ms = 0, ran_ms = 0;   // phase ends, from submit
+	double since_submit() const { return std::chrono::duration<double, std::milli>(SrvClock::now() - t_submit).count(); }
 };
 
 }  // namespace iwg
@@ -47,19 +55,31 @@ struct iwg_server {
 	std::mutex mu;
 	std::condition_variable cv_intake, cv_planned, cv_done, cv_finish;
 	std::condition_variable cv_slow;
-	std::deque<iwg::Request *> intake, planned, slow, finishing, done;
+	std::deque<iwg::Request *> intake, planned, done;
+	std::deque<iwg::Request *> finishing[2];   // post-pass: small, large outputs
+	std::deque<iwg::Request *> slow[2];   // serial-scan requests: small, large
 	bool stopping = false;
 	int in_flight = 0;                 // submitted, not yet polled out
-	std::vector<std::thread> planners, finishers;
-	std::thread dispatcher, slow_dispatcher;
+	std::vector<std::thread> planners, finishers, scan_workers;
+	std::thread dispatcher;
+	size_t slow_bytes = 0;             // device bytes held by the scan workers' requests
 	// statistics
 	long long batches = 0, batched_requests = 0;
 	double device_ms = 0;
-	long long slow_batches = 0, slow_requests = 0;   // second lane (serial dither scans)
+	long long slow_batches = 0, slow_requests = 0;   // scan lanes (serial dither scans)
 	double slow_device_ms = 0;
+	double batch_wall_ms = 0, rest_wall_ms = 0, plan_ms = 0;
 };
 
 namespace {
+
+// Output samples from which a request counts as large (scan workers, post-pass).
+constexpr long long kLargeScan = 1LL << 20;
+
+int size_class(const iwg::Request *r)
+{
+	return (long long)r->plan.out_w * r->plan.out_h * r->plan.out_n >= kLargeScan ? 1 : 0;
+}
 
 void planner_loop(iwg_server *S)
 {
@@ -73,16 +93,20 @@ void planner_loop(iwg_server *S)
 			S->intake.pop_front();
 		}
 		iw_context *ctx = r->ctx;
+		const auto t0 = iwg::SrvClock::now();
 		if(ctx->use_count > 0) iw_set_error(ctx, "Internal: Incorrect attempt to reprocess image");
 		else {
 			ctx->use_count++;
 			r->ok = iwg::build_plan(ctx, r->plan) ? 1 : 0;
 		}
 		if(r->ok) r->bytes = iwg::batch_device_bytes(r->plan);
+		const double ms = std::chrono::duration<double, std::milli>(iwg::SrvClock::now() - t0).count();
+		r->planned_ms = r->since_submit();
 		std::lock_guard<std::mutex> lk(S->mu);
+		S->plan_ms += ms;
 		if(r->ok && iwg::plan_needs_scan(r->plan)) {
-			S->slow.push_back(r);
-			S->cv_slow.notify_one();
+			S->slow[size_class(r)].push_back(r);
+			S->cv_slow.notify_all();
 		}
 		else if(r->ok) {
 			S->planned.push_back(r);
@@ -100,6 +124,7 @@ void planner_loop(iwg_server *S)
 // take one), then hands them to the finishing stage.
 void run_plain(iwg_server *S, std::vector<iwg::Request *> &batch, int lane)
 {
+	for(iwg::Request *r : batch) r->started_ms = r->since_submit();
 	if(!batch.empty()) {
 		std::vector<iw_context *> cc;
 		std::vector<iwg::Plan *> pp;
@@ -117,14 +142,15 @@ void run_plain(iwg_server *S, std::vector<iwg::Request *> &batch, int lane)
 		}
 		std::lock_guard<std::mutex> lk(S->mu);
 		S->device_ms += dev_ms;
-		if(lane == 1) {
+		if(lane >= 1) {
 			S->slow_batches++;
 			S->slow_requests += (long long)batch.size();
 			S->slow_device_ms += dev_ms;
 		}
 	}
+	for(iwg::Request *r : batch) r->ran_ms = r->since_submit();
 	std::lock_guard<std::mutex> lk(S->mu);
-	for(iwg::Request *r : batch) S->finishing.push_back(r);
+	for(iwg::Request *r : batch) S->finishing[size_class(r)].push_back(r);
 	S->cv_finish.notify_all();
 }
 
@@ -157,12 +183,16 @@ void dispatcher_loop(iwg_server *S)
 		}
 		std::vector<int> status;
 		double dev_ms = 0;
+		const auto t0 = iwg::SrvClock::now();
+		for(iwg::Request *r : batch) r->started_ms = r->since_submit();
 		iwg::run_batch(cc, pp, status, dev_ms);
+		const auto t1 = iwg::SrvClock::now();
 		std::vector<iwg::Request *> rest, finished;
 		for(size_t k = 0; k < batch.size(); k++) {
 			if(status[k] == 0) rest.push_back(batch[k]);
 			else {
 				batch[k]->ok = status[k] == 1;
+				batch[k]->ran_ms = batch[k]->since_submit();
 				finished.push_back(batch[k]);
 			}
 		}
@@ -171,47 +201,64 @@ void dispatcher_loop(iwg_server *S)
 			S->batches++;
 			S->batched_requests += (long long)batch.size();
 			S->device_ms += dev_ms;
-			for(iwg::Request *r : finished) S->finishing.push_back(r);
+			S->batch_wall_ms += std::chrono::duration<double, std::milli>(t1 - t0).count();
+			for(iwg::Request *r : finished) S->finishing[size_class(r)].push_back(r);
 			S->cv_finish.notify_all();
 		}
 		run_plain(S, rest, 0);
+		const double rest_ms = std::chrono::duration<double, std::milli>(iwg::SrvClock::now() - t1).count();
+		std::lock_guard<std::mutex> lk(S->mu);
+		S->rest_wall_ms += rest_ms;
 	}
 }
 
-void slow_loop(iwg_server *S)
+// A scan worker of class 'cls' (0 small, 1 large): takes every queued request
+// of its class that fits the device budget the workers share (a worker may
+// take one request whatever the budget when no other scan holds memory) and
+// runs them as one batch on its own lane.
+void slow_loop(iwg_server *S, int lane, int cls)
 {
+	std::deque<iwg::Request *> &q = S->slow[cls];
 	for(;;) {
 		std::vector<iwg::Request *> batch;
+		size_t bytes = 0;
 		{
 			std::unique_lock<std::mutex> lk(S->mu);
-			S->cv_slow.wait(lk, [&] { return S->stopping || !S->slow.empty(); });
-			if(S->slow.empty()) return;
-			size_t bytes = 0;
-			while(!S->slow.empty() && (int)batch.size() < S->max_batch) {
-				iwg::Request *r = S->slow.front();
-				if(!batch.empty() && bytes + r->bytes > S->budget) break;
+			S->cv_slow.wait(lk, [&] {
+				return (S->stopping && q.empty()) ||
+					(!q.empty() && (S->slow_bytes == 0 || S->slow_bytes + q.front()->bytes <= S->budget));
+			});
+			if(q.empty()) return;
+			while(!q.empty() && (int)batch.size() < S->max_batch) {
+				iwg::Request *r = q.front();
+				if((!batch.empty() || S->slow_bytes > 0) && S->slow_bytes + bytes + r->bytes > S->budget) break;
 				bytes += r->bytes;
 				batch.push_back(r);
-				S->slow.pop_front();
+				q.pop_front();
 			}
+			S->slow_bytes += bytes;
 		}
-		run_plain(S, batch, 1);
+		run_plain(S, batch, lane);
+		std::lock_guard<std::mutex> lk(S->mu);
+		S->slow_bytes -= bytes;
+		S->cv_slow.notify_all();
 	}
 }
 
-void finisher_loop(iwg_server *S)
+void finisher_loop(iwg_server *S, int cls)
 {
+	std::deque<iwg::Request *> &q = S->finishing[cls];
 	for(;;) {
 		iwg::Request *r;
 		{
 			std::unique_lock<std::mutex> lk(S->mu);
-			S->cv_finish.wait(lk, [&] { return S->stopping || !S->finishing.empty(); });
-			if(S->finishing.empty()) {
-				if(S->stopping && S->intake.empty() && S->planned.empty() && S->slow.empty()) return;
+			S->cv_finish.wait(lk, [&] { return S->stopping || !q.empty(); });
+			if(q.empty()) {
+				if(S->stopping && S->intake.empty() && S->planned.empty() && S->slow[0].empty() && S->slow[1].empty()) return;
 				continue;
 			}
-			r = S->finishing.front();
-			S->finishing.pop_front();
+			r = q.front();
+			q.pop_front();
 		}
 		if(r->ok) {
 			iwg::bkgd_label(r->ctx, r->plan);
@@ -236,9 +283,9 @@ extern "C" struct iwg_server *iwg_server_create(size_t device_budget, int max_ba
 	T = std::max(2, T);
 	const int nplan = std::max(1, T - T / 4), nfin = std::max(1, T / 4);
 	for(int k = 0; k < nplan; k++) S->planners.emplace_back(planner_loop, S);
-	for(int k = 0; k < nfin; k++) S->finishers.emplace_back(finisher_loop, S);
+	for(int k = 0; k < 2 * nfin; k++) S->finishers.emplace_back(finisher_loop, S, k & 1);
 	S->dispatcher = std::thread(dispatcher_loop, S);
-	S->slow_dispatcher = std::thread(slow_loop, S);
+	for(int lane = 1; lane < iwg::kLanes; lane++) S->scan_workers.emplace_back(slow_loop, S, lane, lane & 1);
 	return S;
 }
 
@@ -276,6 +323,9 @@ extern "C" int iwg_server_poll(struct iwg_server *S, struct iwg_completion *out,
 		out[n].tag = r->tag;
 		out[n].ok = r->ok;
 		out[n].latency_ms = r->latency_ms;
+		out[n].planned_ms = r->planned_ms;
+		out[n].started_ms = r->started_ms;
+		out[n].ran_ms = r->ran_ms;
 		S->in_flight--;
 		delete r;
 		n++;
@@ -288,13 +338,16 @@ extern "C" int iwg_server_info(struct iwg_server *S, struct iwg_server_stats *ou
 	if(!S || !out) return 0;
 	std::lock_guard<std::mutex> lk(S->mu);
 	out->in_flight = S->in_flight;
-	out->queued = (int)(S->intake.size() + S->planned.size() + S->slow.size());
+	out->queued = (int)(S->intake.size() + S->planned.size() + S->slow[0].size() + S->slow[1].size());
 	out->batches = S->batches;
 	out->batched_requests = S->batched_requests;
 	out->device_ms = S->device_ms;
 	out->slow_batches = S->slow_batches;
 	out->slow_requests = S->slow_requests;
 	out->slow_device_ms = S->slow_device_ms;
+	out->batch_wall_ms = S->batch_wall_ms;
+	out->rest_wall_ms = S->rest_wall_ms;
+	out->plan_ms = S->plan_ms;
 	return 1;
 }
 
@@ -304,8 +357,8 @@ extern "C" void iwg_server_destroy(struct iwg_server *S)
 	{
 		// finish everything submitted, then stop the stages
 		std::unique_lock<std::mutex> lk(S->mu);
-		S->cv_done.wait(lk, [&] { return S->intake.empty() && S->planned.empty() && S->slow.empty() &&
-			S->finishing.empty() && (int)S->done.size() >= S->in_flight; });
+		S->cv_done.wait(lk, [&] { return S->intake.empty() && S->planned.empty() && S->slow[0].empty() && S->slow[1].empty() &&
+			S->finishing[0].empty() && S->finishing[1].empty() && (int)S->done.size() >= S->in_flight; });
 		S->stopping = true;
 		S->cv_intake.notify_all();
 		S->cv_planned.notify_all();
@@ -314,7 +367,7 @@ extern "C" void iwg_server_destroy(struct iwg_server *S)
 	}
 	for(std::thread &t : S->planners) t.join();
 	S->dispatcher.join();
-	S->slow_dispatcher.join();
+	for(std::thread &t : S->scan_workers) t.join();
 	for(std::thread &t : S->finishers) t.join();
 	for(iwg::Request *r : S->done) delete r;
 	delete S;

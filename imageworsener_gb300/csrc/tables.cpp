@@ -179,8 +179,34 @@ void nc_fill(int cstype, double gamma, double *nc)
 	}
 }
 
+// Decision records of error diffusion (src/imagew-main.c:727-748): in
+// bracket k a sample v below X[k] is exact (no error sent); above it the
+// reference compares d_ceil = rev_hi - v with d_floor = v - rev_lo, each
+// rounded.  The first is non-increasing in v and the second non-decreasing,
+// so "d_ceil <= d_floor" holds from a least v on: C[k], found by bisection on
+// the bit patterns.  The sent error is then v - rev[code] either way
+// (-(rev_hi - v) rounds to the same value as v - rev_hi).
+void rec_fill(int P, const double *U, const double *X, const int *code, const double *rev, long long *rec)
+{
+	for(int k = 0; k <= P; k++) {
+		const double rl = rev[code[k]], rh = rev[code[k + 1]];
+		double c = std::numeric_limits<double>::infinity();
+		if(k < P) c = lowest_true([&](double v) { return rh - v <= v - rl; }, 0.5 * (rl + rh));
+		long long *r = rec + 8 * (size_t)k;
+		r[0] = (long long)dbits(U[k]);
+		r[1] = (long long)dbits(U[k + 1]);
+		r[2] = (long long)dbits(X[k]);
+		r[3] = (long long)dbits(c);
+		r[4] = (long long)dbits(rl);
+		r[5] = (long long)dbits(rh);
+		r[6] = (long long)(((unsigned long long)(unsigned int)code[k + 1] << 32) | (unsigned int)code[k]);
+		r[7] = 0;
+	}
+}
+
 void build_quant(Quant &q)
 {
+	static std::map<std::tuple<int, uint64_t, int, int>, std::shared_ptr<const std::vector<long long>>> rec_cache;
 	static std::map<std::tuple<int, uint64_t, int, int>, QuantTables> cache;
 	static std::map<std::tuple<int, uint64_t>, std::shared_ptr<const std::vector<double>>> nc_cache;
 
@@ -202,6 +228,15 @@ void build_quant(Quant &q)
 	q.X = it->second.X;
 	q.code = it->second.code;
 	q.rev = it->second.rev;
+	if(q.dfam == IW_DITHERFAMILY_ERRDIFF) {
+		auto rit = rec_cache.find(key);
+		if(rit == rec_cache.end()) {
+			auto rec = std::make_shared<std::vector<long long>>(8 * (size_t)(q.P + 1));
+			rec_fill(q.P, q.U->data(), q.X->data(), q.code->data(), q.rev->data(), rec->data());
+			rit = rec_cache.emplace(key, rec).first;
+		}
+		q.rec = rit->second;
+	}
 	if(q.use_nc) {
 		auto nkey = std::make_tuple(q.cstype, dbits(q.gamma));
 		auto nit = nc_cache.find(nkey);

@@ -300,13 +300,15 @@ def run_batch(lib: IWLib, jobs: Sequence[Job]) -> list[Result]:
 
 
 class Completion(C.Structure):
-    _fields_ = [("tag", C.c_ulonglong), ("ok", C.c_int), ("latency_ms", C.c_double)]
+    _fields_ = [("tag", C.c_ulonglong), ("ok", C.c_int), ("latency_ms", C.c_double), ("planned_ms", C.c_double),
+                ("started_ms", C.c_double), ("ran_ms", C.c_double)]
 
 
 class ServerStats(C.Structure):
     _fields_ = [("in_flight", C.c_int), ("queued", C.c_int), ("batches", C.c_longlong),
                 ("batched_requests", C.c_longlong), ("device_ms", C.c_double), ("slow_batches", C.c_longlong),
-                ("slow_requests", C.c_longlong), ("slow_device_ms", C.c_double)]
+                ("slow_requests", C.c_longlong), ("slow_device_ms", C.c_double), ("batch_wall_ms", C.c_double),
+                ("rest_wall_ms", C.c_double), ("plan_ms", C.c_double)]
 
 
 def server_api(lib: IWLib):

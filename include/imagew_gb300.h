@@ -70,8 +70,10 @@ IW_EXPORT(int) iwg_process_batch(struct iw_context **ctxs, int n);
 /* ---- request server: continuous batching under a device-memory budget ----
  * A server owns host threads that plan submitted contexts as they arrive, a
  * dispatcher that runs every planned request fitting the budget as one batch
- * (as iwg_process_batch) while the next requests are being planned, and
- * threads that run the output post-pass.  Each request's output is exactly
+ * (as iwg_process_batch) while the next requests are being planned, scan
+ * workers that run requests ending in a serial dither scan (error diffusion,
+ * random dither) on device lanes of their own -- a large one alone, small ones
+ * together -- and threads that run the output post-pass.  Each request's output is exactly
  * what iw_process_image() gives it alone.  The caller keeps ownership of the
  * contexts: a context may be read or destroyed once its completion was polled. */
 struct iwg_server;
@@ -79,6 +81,9 @@ struct iwg_completion {
 	unsigned long long tag;  /* as given to iwg_server_submit */
 	int ok;                  /* 1: processed; 0: failed (error set on the context) */
 	double latency_ms;       /* submit -> completion */
+	double planned_ms;       /* submit -> planning done */
+	double started_ms;       /* submit -> its device work began (0 if it never ran) */
+	double ran_ms;           /* submit -> its device work ended (the rest is the post-pass) */
 };
 struct iwg_server_stats {
 	int in_flight;               /* submitted, completion not yet polled */
@@ -86,9 +91,12 @@ struct iwg_server_stats {
 	long long batches;           /* device batches run */
 	long long batched_requests;  /* requests in them */
 	double device_ms;            /* device time of the batched passes */
-	long long slow_batches;      /* of them on the lane for serial dither scans */
+	long long slow_batches;      /* of them on the scan workers' lanes (serial dither scans) */
 	long long slow_requests;
 	double slow_device_ms;
+	double batch_wall_ms;        /* host wall time of the dispatcher's batched calls */
+	double rest_wall_ms;         /* ... and of the requests they left to the plain form */
+	double plan_ms;              /* planning time, summed over requests */
 };
 /* device_budget: bytes of device memory one batch may hold (0: 8 GiB);
  * max_batch: requests per batch (0: 4096); host_threads (0: all cores). */
