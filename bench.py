@@ -480,7 +480,11 @@ def serving_leg(lib: IWLib, rate: float, seconds: float, thumbs, ups):
             "lanes": {"batches": info.batches, "batched_requests": info.batched_requests,
                       "device_ms": info.device_ms, "scan_lane_batches": info.slow_batches,
                       "scan_lane_requests": info.slow_requests, "scan_lane_device_ms": info.slow_device_ms,
-                      "batch_wall_ms": info.batch_wall_ms, "rest_wall_ms": info.rest_wall_ms, "plan_ms": info.plan_ms}}
+                      "batch_wall_ms": info.batch_wall_ms, "rest_wall_ms": info.rest_wall_ms, "plan_ms": info.plan_ms,
+                      "batch_phase_ms": dict(zip(("prepare", "upload", "launch_passes", "launch_fixup", "wait_download",
+                                                  "rest", "of_which_tables", "of_which_attributes",
+                                                  "of_which_d2h_wait", "of_which_d2h_copy"),
+                                                 list(info.batch_phase_ms)))}}
 
 
 def main():

@@ -8,8 +8,10 @@
 // each result is byte-identical to processing the image alone.
 #include "fastkern.cuh"
 #include "fastpath.cuh"
+#include "iwg_internal.h"
 
 #include <algorithm>
+#include <chrono>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -164,6 +166,25 @@ BatchArena &arena()
 
 }  // namespace
 
+void preload_batch_kernels()
+{
+	cudaFuncAttributes a;
+#define IWG_PRE_BU(NS_, NCH_, A_, D_, PX_) cudaFuncGetAttributes(&a, (const void *)kb_vbulk<NS_, NCH_, A_, D_, PX_>);
+#define IWG_PRE_PX(NS_, NCH_, A_, D_, PX_) cudaFuncGetAttributes(&a, (const void *)kb_vstream_px<NS_, NCH_, A_, D_, PX_>);
+#define IWG_PRE_ST(NS_, NPL_, D_) cudaFuncGetAttributes(&a, (const void *)kb_vstream<NS_, NPL_, D_>);
+#define IWG_PRE_GA(NPL_, D_) cudaFuncGetAttributes(&a, (const void *)kb_vgather<NPL_, D_>);
+	IWG_VBULK_VARIANTS(IWG_PRE_BU)
+	IWG_VPX_VARIANTS(IWG_PRE_PX)
+	IWG_VSTREAM_VARIANTS(IWG_PRE_ST)
+	IWG_VGATHER_VARIANTS(IWG_PRE_GA)
+#undef IWG_PRE_BU
+#undef IWG_PRE_PX
+#undef IWG_PRE_ST
+#undef IWG_PRE_GA
+	for(int npl = 1; npl <= 4; npl++) cudaFuncGetAttributes(&a, batch_hkernel(npl));
+	cudaGetLastError();
+}
+
 int fast_launch_batch(cudaStream_t st, void *const *items, int n, std::string &err, cudaEvent_t after_vertical)
 {
 	if(n <= 0) return 0;
@@ -214,6 +235,7 @@ int fast_launch_batch(cudaStream_t st, void *const *items, int n, std::string &e
 			g.off_start = add(g.start.data(), g.start.size() * sizeof(int));
 		}
 	}
+	const auto t_tab = std::chrono::steady_clock::now();
 	BatchArena &A = arena();
 	if(!A.ensure(host.size(), st)) {
 		err = "Out of GPU memory (batch tables)";
@@ -221,15 +243,18 @@ int fast_launch_batch(cudaStream_t st, void *const *items, int n, std::string &e
 	}
 	uint8_t *base = (uint8_t *)A.p;
 	cudaMemcpyAsync(base, host.data(), host.size(), cudaMemcpyHostToDevice, st);
+	batch_phase_add(6, std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_tab).count());
 	const FJob *djobs = (const FJob *)(base + off_jobs);
 	int launches = 0;
 	auto launch = [&](Group &g) -> bool {
 		if(g.blocks == 0) return true;
+		const auto t_attr = std::chrono::steady_clock::now();
 		if(g.smem > 48 * 1024 &&
 			cudaFuncSetAttribute(g.kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g.smem) != cudaSuccess) {
 			err = "batch: shared memory request refused";
 			return false;
 		}
+		batch_phase_add(7, std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_attr).count());
 		const int *didx = (const int *)(base + g.off_idx);
 		const int *dstart = (const int *)(base + g.off_start);
 		int ng = (int)g.idx.size();

@@ -715,4 +715,26 @@ void fast_item_job_df(const void *item, Job &J)
 
 void fast_item_free(void *item) { delete static_cast<FastState *>(item); }
 
+void preload_fast_kernels()
+{
+	cudaFuncAttributes a;
+#define IWG_PRE_BU(NS_, NCH_, A_, D_, PX_) cudaFuncGetAttributes(&a, (const void *)k_vbulk<NS_, NCH_, A_, D_, PX_>);
+#define IWG_PRE_PX(NS_, NCH_, A_, D_, PX_) cudaFuncGetAttributes(&a, (const void *)k_vstream_px<NS_, NCH_, A_, D_, PX_>);
+#define IWG_PRE_ST(NS_, NPL_, D_) cudaFuncGetAttributes(&a, (const void *)k_vstream<NS_, NPL_, D_>);
+#define IWG_PRE_GA(NPL_, D_) cudaFuncGetAttributes(&a, (const void *)k_vgather<NPL_, D_>);
+	IWG_VBULK_VARIANTS(IWG_PRE_BU)
+	IWG_VPX_VARIANTS(IWG_PRE_PX)
+	IWG_VSTREAM_VARIANTS(IWG_PRE_ST)
+	IWG_VGATHER_VARIANTS(IWG_PRE_GA)
+#undef IWG_PRE_BU
+#undef IWG_PRE_PX
+#undef IWG_PRE_ST
+#undef IWG_PRE_GA
+	cudaFuncGetAttributes(&a, (const void *)k_hpass_fast<1>);
+	cudaFuncGetAttributes(&a, (const void *)k_hpass_fast<2>);
+	cudaFuncGetAttributes(&a, (const void *)k_hpass_fast<3>);
+	cudaFuncGetAttributes(&a, (const void *)k_hpass_fast<4>);
+	cudaGetLastError();
+}
+
 }  // namespace iwg

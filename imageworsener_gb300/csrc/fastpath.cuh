@@ -51,6 +51,13 @@ int fast_item_htaps(const void *item);             // widest horizontal window
 void fast_item_place(void *item, const uint8_t *dev_blob, int *flag_count, int *flag_list, int img);
 // Launches the vertical and horizontal passes of n placed images, one launch
 // per kernel variant (fastbatch.cu).  Returns the number of launches, -1 on error.
+// Load every kernel of the fast form (per image / batched) now: with lazy
+// module loading a kernel's first launch loads it, which can wait for work
+// running on other streams.
+void preload_fast_kernels();
+void preload_batch_kernels();
+void preload_noalloc_kernels();   // noalloc.cu
+
 int fast_launch_batch(cudaStream_t st, void *const *items, int n, std::string &err,
 	cudaEvent_t after_vertical = nullptr);
 // Copies the image's double-float re-evaluation pointers (set by placement)

@@ -277,6 +277,14 @@ void optimize(iw_context *ctx);
 // lanes 1 .. kLanes-1.
 constexpr int kLanes = 5;
 bool run_pipeline(iw_context *ctx, Plan &P, int warmup = 0, int iters = 1, int lane = 0);
+// Host wall time of the batched calls' phases, summed (ms): preparation,
+// uploads, the passes' launches, the fix-up's launch, device wait with
+// downloads, the rest; then, inside the passes' launches, the table upload and
+// the attribute calls; within the downloads (lane 0, staged), the wait for
+// the device and the host copies.
+constexpr int kBatchPhases = 10;
+void batch_phase_ms(double *out);
+void batch_phase_add(int phase, double ms);
 // Whether an output channel is quantised by a serial scan (api.cpp).
 bool plan_needs_scan(const Plan &P);
 // Device bytes an image holds while it runs in a batch (api.cpp).

@@ -227,6 +227,15 @@ bool device_can_access(const void *p, int dev, bool pageable)
 }
 
 }  // namespace
+
+void preload_noalloc_kernels()
+{
+	cudaFuncAttributes a;
+	cudaFuncGetAttributes(&a, (const void *)k_na_vpass);
+	cudaFuncGetAttributes(&a, (const void *)k_na_hpass);
+	cudaGetLastError();
+}
+
 }  // namespace iwg
 
 using namespace iwg;

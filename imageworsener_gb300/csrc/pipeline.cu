@@ -138,13 +138,28 @@ __device__ __forceinline__ double unassoc_and_bkgd(const Job &J, const DMid &mc,
 // plain form for all pixels and by the fast form for flagged pixels.
 // 'mask' selects the intermediate channels to evaluate (bit m); the alpha
 // channel must be included whenever a colour channel is.
+// Output codes of one pixel, kept in registers (an array indexed by a run-time
+// channel would live in local memory, and a kernel that needs local memory
+// can make the driver wait for the whole device when it launches).
+struct Codes4 {
+	int c0 = -1, c1 = -1, c2 = -1, c3 = -1;
+	__device__ __forceinline__ void set(int k, int v)
+	{
+		if(k == 0) c0 = v;
+		else if(k == 1) c1 = v;
+		else if(k == 2) c2 = v;
+		else c3 = v;
+	}
+	__device__ __forceinline__ int operator[](int k) const { return k == 0 ? c0 : (k == 1 ? c1 : (k == 2 ? c2 : c3)); }
+};
+static_assert(dev::kMaxCh == 4, "Codes4 holds four channels");
+
 template<class Interm>
 __device__ void pixel_exact(const Job &J, int i, int j, bool apply_post, Interm interm, unsigned int mask = 0xfu)
 {
 	double a = 0.0;
 	int alpha_code = -1;
-	int codes[dev::kMaxCh];
-	for(int oc = 0; oc < dev::kMaxCh; oc++) codes[oc] = -1;
+	Codes4 codes;
 	int alt = checker_alt(J, i, j);
 	for(int k = 0; k < J.mid_n; k++) {
 		int m = J.order[k];
@@ -165,12 +180,12 @@ __device__ void pixel_exact(const Job &J, int i, int j, bool apply_post, Interm 
 		}
 		if(o.scan) {
 			J.scanbuf[((unsigned long long)oc * J.out_h + j) * J.out_w + i] = v;
-			codes[oc] = -1;
+			codes.set(oc, -1);
 			continue;
 		}
 		int c = quantize_exact(o.q, v, i, j);
 		if(is_alpha) alpha_code = c;
-		codes[oc] = c;
+		codes.set(oc, c);
 	}
 	if(J.out_float) return;
 	for(int oc = 0; oc < J.out_n; oc++) {
@@ -234,15 +249,17 @@ __device__ __forceinline__ Bracket bracket_bits(const DQuant &q, double v)
 // The twelve error-diffusion weights of subtype 'dsub': numerators over a
 // denominator (positions x+1 x+2 / x-2 x-1 x x+1 x+2 / the same on the row
 // after next), as separately rounded quotients like the reference's.
+__constant__ signed char c_ed_num[8][12] = {
+	{7,0, 0,3,5,1,0, 0,0,0,0,0}, {7,5, 3,5,7,5,3, 1,3,5,3,1}, {8,4, 2,4,8,4,2, 1,2,4,2,1},
+	{8,4, 2,4,8,4,2, 0,0,0,0,0}, {5,3, 2,4,5,4,2, 0,2,3,2,0}, {4,3, 1,2,3,2,1, 0,0,0,0,0},
+	{2,0, 0,1,1,0,0, 0,0,0,0,0}, {1,1, 0,1,1,1,0, 0,0,1,0,0}};
+__constant__ double c_ed_den[8] = {16.0, 48.0, 42.0, 32.0, 32.0, 16.0, 4.0, 8.0};
+
 __device__ __forceinline__ void errdiff_weights(int dsub, double *c)
 {
-	const signed char num[8][12] = {
-		{7,0, 0,3,5,1,0, 0,0,0,0,0}, {7,5, 3,5,7,5,3, 1,3,5,3,1}, {8,4, 2,4,8,4,2, 1,2,4,2,1},
-		{8,4, 2,4,8,4,2, 0,0,0,0,0}, {5,3, 2,4,5,4,2, 0,2,3,2,0}, {4,3, 1,2,3,2,1, 0,0,0,0,0},
-		{2,0, 0,1,1,0,0, 0,0,0,0,0}, {1,1, 0,1,1,1,0, 0,0,1,0,0}};
-	const double den[8] = {16.0, 48.0, 42.0, 32.0, 32.0, 16.0, 4.0, 8.0};
 	const int sub = (dsub >= 0 && dsub <= 7) ? dsub : 0;
-	for(int k = 0; k < 12; k++) c[k] = ddiv((double)num[sub][k], den[sub]);
+#pragma unroll
+	for(int k = 0; k < 12; k++) c[k] = ddiv((double)c_ed_num[sub][k], c_ed_den[sub]);
 }
 
 constexpr int kScanChunk = 256;   // samples staged per warp for the serial walk
@@ -328,9 +345,12 @@ __device__ __forceinline__ bool is_nan_bits(double v)
 // bounds, one record load, two compares for the decision.  Products with a
 // zero weight are skipped: they add a signed zero to an accumulator that
 // starts at +0 and can never become -0 (a sum of nonzero values that cancels
-// is +0), which leaves it unchanged.
+// is +0), which leaves it unchanged.  For the same reason a sample that sends
+// no error (an exact one) is given the error +0: its contributions change
+// nothing, so the walk and the spreading need no test for it.
 // Error buffer of a channel: three rotating error rows and the row's errors,
 // out_w doubles each; the staged chunk lives in shared memory (kScanChunk).
+template<bool C1>   // C1: the weight of sample x+2f in the same row is nonzero
 __device__ __forceinline__ void errdiff_warp(const Job &J, int oc)
 {
 	__shared__ double s_v[dev::kMaxCh][kScanChunk], s_e[dev::kMaxCh][kScanChunk];
@@ -361,17 +381,14 @@ __device__ __forceinline__ void errdiff_warp(const Job &J, int oc)
 		nz2[k] = c[11 - k] != 0.0;
 		any2 = any2 || nz2[k];
 	}
-	const bool c1nz = c[1] != 0.0;
 	const double c0 = c[0], c1 = c[1];
 	for(int x = lane; x < 3 * W; x += 32) e0[x] = 0.0;
 	__syncwarp();
-	const double skip = __longlong_as_double(0x7ff8dead0000beefLL);   // a NaN: the sample sent no error
 	for(int y = 0; y < H; y++) {
 		const int f = (y % 2) ? -1 : 1;
 		const double *row = scan + (unsigned long long)y * W;
 		uint8_t *const orow = out + (unsigned long long)y * out_bpr + ((size_t)oc << wide);
 		double err1 = 0.0, err2 = 0.0;     // errors of the previous two samples of the row
-		bool has1 = false, has2 = false;
 		for(int z0 = 0; z0 < W; z0 += kScanChunk) {
 			const int cn = min(kScanChunk, W - z0);
 			const int xb = (y % 2) ? W - 1 - z0 : z0;   // x of the chunk's first sample
@@ -425,11 +442,10 @@ __device__ __forceinline__ void errdiff_warp(const Job &J, int oc)
 						rp = ed_rec(rec, kc < P ? kc + 1 : P);
 					// e0[x] as the reference has it when it reaches x: the carried
 					// error, then x-2f's contribution, then x-f's
-					if(has2 && c1nz) e = dadd(e, dmul(err2, c1));
-					if(has1) e = dadd(e, dmul(err1, c0));
+					if(C1) e = dadd(e, dmul(err2, c1));
+					e = dadd(e, dmul(err1, c0));
 					int code = 0;
-					double err = skip;
-					bool sent = false;
+					double err = 0.0;
 					if(k0 >= 0) {
 						// the reference's clamp; the value is not NaN here
 						const double w = dadd(sval, e);
@@ -449,12 +465,11 @@ __device__ __forceinline__ void errdiff_warp(const Job &J, int oc)
 							const bool up = vb >= r.c;
 							code = up ? r.code_hi : r.code_lo;
 							err = dsub(v, up ? r.rev_hi : r.rev_lo);
-							sent = true;
 						}
 					}
 					er[x] = err;
-					err2 = err1; has2 = has1;
-					err1 = err; has1 = sent;
+					err2 = err1;
+					err1 = err;
 					uint8_t *const p = orow + ((size_t)x * out_n << wide);
 					if(wide) {
 						p[0] = (uint8_t)(code >> 8);
@@ -473,7 +488,6 @@ __device__ __forceinline__ void errdiff_warp(const Job &J, int oc)
 				const int qx = t + k * f;
 				if(qx < 0 || qx >= W) continue;
 				const double err = er[qx];
-				if(is_nan_bits(err)) continue;
 				if(nz1[k + 2]) a1 = dadd(a1, dmul(err, c[4 - k]));
 				if(nz2[k + 2]) a2 = dadd(a2, dmul(err, c[9 - k]));
 			}
@@ -594,7 +608,11 @@ __device__ void random_warp(const Job &J, int oc)
 __device__ __forceinline__ void scan_warp(const Job &J, int oc)
 {
 	if(oc >= J.out_n || oc >= dev::kMaxCh || !J.outc[oc].scan) return;
-	if(J.outc[oc].q.dfam == IW_DITHERFAMILY_ERRDIFF) errdiff_warp(J, oc);
+	if(J.outc[oc].q.dfam == IW_DITHERFAMILY_ERRDIFF) {
+		const int sub = J.outc[oc].q.dsub;
+		if(sub <= 0 || sub == 6 || sub > 7) errdiff_warp<false>(J, oc);   // Floyd-Steinberg, Sierra "4A": no x+2f weight
+		else errdiff_warp<true>(J, oc);
+	}
 	else random_warp(J, oc);
 }
 
@@ -638,20 +656,27 @@ __device__ __forceinline__ int find_job(const int *start, int n, int b)
 	return lo;
 }
 
-__global__ void kb_vpass_exact(const Job *jobs, const int *start, int n)
+// The batched plain passes walk their logical blocks with a block stride, so
+// that a lane of long background work can run them on a capped grid and leave
+// room on the SMs for other lanes.
+__global__ void kb_vpass_exact(const Job *jobs, const int *start, int n, int total)
 {
-	const int g = find_job(start, n, blockIdx.x);
-	const Job &J = jobs[g];
-	const int local = blockIdx.x - start[g], gx = (J.mid_w + blockDim.x - 1) / blockDim.x;
-	vpass_exact_at(J, (local % gx) * blockDim.x + threadIdx.x, local / gx);
+	for(int b = blockIdx.x; b < total; b += gridDim.x) {
+		const int g = find_job(start, n, b);
+		const Job &J = jobs[g];
+		const int local = b - start[g], gx = (J.mid_w + blockDim.x - 1) / blockDim.x;
+		vpass_exact_at(J, (local % gx) * blockDim.x + threadIdx.x, local / gx);
+	}
 }
 
-__global__ void kb_hpass_exact(const Job *jobs, const int *start, int n)
+__global__ void kb_hpass_exact(const Job *jobs, const int *start, int n, int total)
 {
-	const int g = find_job(start, n, blockIdx.x);
-	const Job &J = jobs[g];
-	const int local = blockIdx.x - start[g], gx = (J.out_w + blockDim.x - 1) / blockDim.x;
-	hpass_exact_at(J, (local % gx) * blockDim.x + threadIdx.x, local / gx);
+	for(int b = blockIdx.x; b < total; b += gridDim.x) {
+		const int g = find_job(start, n, b);
+		const Job &J = jobs[g];
+		const int local = b - start[g], gx = (J.out_w + blockDim.x - 1) / blockDim.x;
+		hpass_exact_at(J, (local % gx) * blockDim.x + threadIdx.x, local / gx);
+	}
 }
 
 // one block per image, one warp per output channel
@@ -661,13 +686,15 @@ __global__ void kb_scan(const Job *jobs)
 	if(J.any_scan) scan_warp(J, threadIdx.x >> 5);
 }
 
-__global__ void kb_finalize(const Job *jobs, const int *start, int n)
+__global__ void kb_finalize(const Job *jobs, const int *start, int n, int total)
 {
-	const int g = find_job(start, n, blockIdx.x);
-	const Job &J = jobs[g];
-	if(!J.any_scan || !(J.negate || J.blacken)) return;
-	const int local = blockIdx.x - start[g], gx = (J.out_w + blockDim.x - 1) / blockDim.x;
-	finalize_at(J, (local % gx) * blockDim.x + threadIdx.x, local / gx);
+	for(int b = blockIdx.x; b < total; b += gridDim.x) {
+		const int g = find_job(start, n, b);
+		const Job &J = jobs[g];
+		if(!J.any_scan || !(J.negate || J.blacken)) continue;
+		const int local = b - start[g], gx = (J.out_w + blockDim.x - 1) / blockDim.x;
+		finalize_at(J, (local % gx) * blockDim.x + threadIdx.x, local / gx);
+	}
 }
 
 // Position of the r-th set bit of 'mask' (r counts from 0).
@@ -1210,12 +1237,22 @@ bool stage_d2h(Stager &G, cudaStream_t st, const std::vector<Xfer> &items)
 		cudaEventRecord(G.ev[g & 1], st);
 	};
 	for(size_t g = 0; g < groups.size() && g < 2; g++) issue(g);
+	using Clk = std::chrono::steady_clock;
+	double t_wait = 0, t_copy = 0;
 	for(size_t g = 0; g < groups.size(); g++) {
+		const Clk::time_point t0 = Clk::now();
 		if(wait_event(G.ev[g & 1], G.patient) != cudaSuccess) return false;
+		const Clk::time_point t1 = Clk::now();
 		std::vector<Piece> out = groups[g].out;
 		for(Piece &p : out) p.src = G.pin[g & 1] + (uintptr_t)p.src;
 		copy_pieces(out);
+		t_wait += std::chrono::duration<double, std::milli>(t1 - t0).count();
+		t_copy += std::chrono::duration<double, std::milli>(Clk::now() - t1).count();
 		if(g + 2 < groups.size()) issue(g + 2);
+	}
+	if(!G.patient) {   // lane 0: account the device wait and the host copies apart
+		batch_phase_add(8, t_wait);
+		batch_phase_add(9, t_copy);
 	}
 	return true;
 }
@@ -1254,6 +1291,26 @@ DeviceState &state(int lane = 0)
 	return *s[(unsigned)lane % (unsigned)kLanes];
 }
 
+// Every kernel of the library, loaded once per process before any lane runs
+// work: under lazy module loading a kernel's first launch loads its module,
+// and that can wait for long scans running on other lanes.
+void preload_kernels()
+{
+	static std::once_flag once;
+	std::call_once(once, [] {
+		cudaFuncAttributes a;
+		for(const void *k : {(const void *)k_vpass_exact, (const void *)k_hpass_exact, (const void *)k_scan,
+			(const void *)k_finalize, (const void *)kb_vpass_exact, (const void *)kb_hpass_exact, (const void *)kb_scan,
+			(const void *)kb_finalize, (const void *)k_fix_flagged_warp<true>, (const void *)k_fix_flagged_warp<false>,
+			(const void *)k_fix_flagged_thread<true>, (const void *)k_fix_flagged_thread<false>})
+			cudaFuncGetAttributes(&a, k);
+		preload_fast_kernels();
+		preload_batch_kernels();
+		preload_noalloc_kernels();
+		cudaGetLastError();
+	});
+}
+
 bool ensure_init(DeviceState &S, std::string &err)
 {
 	if(S.init) return true;
@@ -1277,6 +1334,7 @@ bool ensure_init(DeviceState &S, std::string &err)
 	for(DevBuf *b : {&S.in, &S.interm, &S.out, &S.scan, &S.err, &S.params, &S.flags, &S.batch_io, &S.batch_tab})
 		b->st = S.stream;
 	S.stager.patient = S.lane != 0;
+	preload_kernels();
 	{   // keep freed stream-ordered memory in the pool rather than returning it at
 		// every synchronise; and never let an allocation on one lane reuse memory
 		// whose free on another lane's stream is still pending (the pool would
@@ -1303,7 +1361,8 @@ const T *cached_table(DeviceState &S, const std::shared_ptr<const std::vector<T>
 	void *d = nullptr;
 	size_t n = v->size() * sizeof(T);
 	if(cudaMalloc(&d, n ? n : 16) != cudaSuccess) return nullptr;
-	cudaMemcpy(d, v->data(), n, cudaMemcpyHostToDevice);
+	cudaMemcpyAsync(d, v->data(), n, cudaMemcpyHostToDevice, S.stream);   // the lane's stream, not the legacy one
+	cudaStreamSynchronize(S.stream);
 	S.table_cache[v.get()] = {std::static_pointer_cast<const void>(v), d};
 	return (const T *)d;
 }
@@ -1567,6 +1626,7 @@ bool run_pipeline(iw_context *ctx, Plan &P, int warmup, int iters, int lane)
 		if(timed) marks_per_it = (int)(ev.size() - before);
 		launches = l;
 	}
+	if(S.lane != 0) wait_stream(st, true);   // downloads queued once the kernels are done (as for batches)
 	if(upmode == UP_COPY) cudaMemcpyAsync(ctx->img2.pixels, S.out.p, out_bytes, cudaMemcpyDeviceToHost, st);
 	if(upmode == UP_STAGE) stage_d2h(S.stager, st, {Xfer{(uint8_t *)S.out.p, (uint8_t *)ctx->img2.pixels, out_bytes}});
 	cudaError_t ce = wait_stream(st, S.lane != 0);
@@ -1575,7 +1635,8 @@ bool run_pipeline(iw_context *ctx, Plan &P, int warmup, int iters, int lane)
 	ctx->stats.flagged_exact = 0;
 	if(ce == cudaSuccess && fast && fi.flag_count_dev) {
 		int nflag[3] = {0, 0, 0};
-		ce = cudaMemcpy(nflag, fi.flag_count_dev, 3 * sizeof(int), cudaMemcpyDeviceToHost);
+		ce = cudaMemcpyAsync(nflag, fi.flag_count_dev, 3 * sizeof(int), cudaMemcpyDeviceToHost, st);
+		if(ce == cudaSuccess) ce = cudaStreamSynchronize(st);
 		ctx->stats.flagged = nflag[0];
 		ctx->stats.flagged_exact = nflag[1];
 		if(ce == cudaSuccess && nflag[2]) {
@@ -1616,11 +1677,50 @@ bool run_pipeline(iw_context *ctx, Plan &P, int warmup, int iters, int lane)
 // image keeps its own tables and buffers, so its bytes equal a lone run's.
 // status[i]: 1 done here, 0 left for the caller (run it alone), -1 failed
 // (error set on the context).  'dev_ms' receives the batch's device time.
+// Host wall time of run_batch's phases, summed over calls: job packing and
+// the fast form's host preparation, uploads, the passes' launches, the
+// fix-up's launch, the wait for the device with the downloads, the rest; and
+// inside the passes' launches, the table upload and the attribute calls.
+namespace {
+std::mutex g_phase_mu;
+double g_phase_ms[kBatchPhases] = {};
+using PhaseClock = std::chrono::steady_clock;
+struct PhaseTimer {
+	PhaseClock::time_point t = PhaseClock::now();
+	double d[6] = {0, 0, 0, 0, 0, 0};
+	void mark(int k)
+	{
+		const PhaseClock::time_point n = PhaseClock::now();
+		d[k] += std::chrono::duration<double, std::milli>(n - t).count();
+		t = n;
+	}
+	~PhaseTimer()
+	{
+		mark(5);
+		std::lock_guard<std::mutex> lk(g_phase_mu);
+		for(int k = 0; k < 6; k++) g_phase_ms[k] += d[k];
+	}
+};
+}  // namespace
+
+void batch_phase_add(int k, double ms)
+{
+	std::lock_guard<std::mutex> lk(g_phase_mu);
+	g_phase_ms[k] += ms;
+}
+
+void batch_phase_ms(double *out)
+{
+	std::lock_guard<std::mutex> lk(g_phase_mu);
+	for(int k = 0; k < kBatchPhases; k++) out[k] = g_phase_ms[k];
+}
+
 bool run_batch(const std::vector<iw_context *> &ctxs, const std::vector<Plan *> &plans, std::vector<int> &status,
 	double &dev_ms, int lane)
 {
 	DeviceState &S = state(lane);
 	std::lock_guard<std::mutex> lk(S.mu);
+	PhaseTimer pt;
 	const int n = (int)ctxs.size();
 	status.assign(n, 0);
 	dev_ms = 0;
@@ -1736,6 +1836,7 @@ bool run_batch(const std::vector<iw_context *> &ctxs, const std::vector<Plan *> 
 	cudaEvent_t e0, e1;
 	cudaEventCreate(&e0);
 	cudaEventCreate(&e1);
+	pt.mark(0);
 	cudaMemcpyAsync(base + o_par, S.staging.data(), S.staging.size(), cudaMemcpyHostToDevice, st);
 	cudaMemcpyAsync(tbase, tab.data(), tab.size(), cudaMemcpyHostToDevice, st);
 	if(upmode == UP_COPY)
@@ -1756,13 +1857,16 @@ bool run_batch(const std::vector<iw_context *> &ctxs, const std::vector<Plan *> 
 	cudaEventCreate(&ev_h);
 	cudaEventCreate(&ev_f);
 	cudaEventRecord(e0, st);
+	pt.mark(1);
 	int launches = fast_launch_batch(st, items.data(), m, err, ev_h);
 	cudaEventRecord(ev_f, st);
+	pt.mark(2);
 	if(launches >= 0) {
 		launch_fix_flagged_batch(st, (const Job *)(tbase + o_jobs), maxt, flag_count, flag_list);
 		launches++;
 	}
 	cudaEventRecord(e1, st);
+	pt.mark(3);
 	if(upmode == UP_COPY)
 		for(int k = 0; k < m; k++) {
 			const int i = item_img[k];
@@ -1778,9 +1882,11 @@ bool run_batch(const std::vector<iw_context *> &ctxs, const std::vector<Plan *> 
 	}
 	cudaError_t ce = wait_stream(st, S.lane != 0);
 	if(ce == cudaSuccess) ce = cudaGetLastError();
+	pt.mark(4);
 	int nflagged[3] = {0, 0, 0};
 	float ms = 0, ms_v = 0, ms_h = 0, ms_f = 0;
-	if(ce == cudaSuccess) ce = cudaMemcpy(nflagged, flag_count, 3 * sizeof(int), cudaMemcpyDeviceToHost);
+	if(ce == cudaSuccess) ce = cudaMemcpyAsync(nflagged, flag_count, 3 * sizeof(int), cudaMemcpyDeviceToHost, st);
+	if(ce == cudaSuccess) ce = cudaStreamSynchronize(st);
 	if(ce == cudaSuccess && nflagged[2]) {
 		err = "A device wait ran out of time (vertical pass); nothing was written";
 		launches = -1;
@@ -1936,11 +2042,20 @@ bool run_batch_plain(const std::vector<iw_context *> &ctxs, const std::vector<Pl
 		for(const Xfer &x : xin) cudaMemcpyAsync(x.dev, x.host, x.n, cudaMemcpyHostToDevice, st);
 	if(upmode == UP_STAGE && !stage_h2d(S.stager, st, xin)) return fail_all("Out of pinned host memory");
 	cudaEventRecord(e0, st);
-	kb_vpass_exact<<<(unsigned)bv, 128, 0, st>>>(dj, dsv, m);
-	kb_hpass_exact<<<(unsigned)bh, 128, 0, st>>>(dj, dsh, m);
+	// lane 0 takes the whole GPU; the scan lanes' passes run on at most four
+	// blocks per SM, so that lane 0's batches find room beside them
+	int sms = 152;
+	cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, S.device);
+	const long long cap = S.lane == 0 ? 0x7fffffffLL : 4LL * sms;
+	const int nv = (int)bv, nh = (int)bh;
+	if(bv > 0) kb_vpass_exact<<<(unsigned)std::min<long long>(bv, cap), 128, 0, st>>>(dj, dsv, m, nv);
+	if(bh > 0) kb_hpass_exact<<<(unsigned)std::min<long long>(bh, cap), 128, 0, st>>>(dj, dsh, m, nh);
 	kb_scan<<<m, 32 * maxch, 0, st>>>(dj);
-	kb_finalize<<<(unsigned)bh, 128, 0, st>>>(dj, dsh, m);
+	if(bh > 0) kb_finalize<<<(unsigned)std::min<long long>(bh, cap), 128, 0, st>>>(dj, dsh, m, nh);
 	cudaEventRecord(e1, st);
+	// A scan lane queues its downloads only once its kernels are done: a copy
+	// queued behind a long scan can hold up other streams' copies.
+	if(S.lane != 0) wait_event(e1, true);
 	if(upmode == UP_COPY)
 		for(const Xfer &x : xout) cudaMemcpyAsync(x.host, x.dev, x.n, cudaMemcpyDeviceToHost, st);
 	if(upmode == UP_STAGE) stage_d2h(S.stager, st, xout);

@@ -348,6 +348,7 @@ extern "C" int iwg_server_info(struct iwg_server *S, struct iwg_server_stats *ou
 	out->batch_wall_ms = S->batch_wall_ms;
 	out->rest_wall_ms = S->rest_wall_ms;
 	out->plan_ms = S->plan_ms;
+	iwg::batch_phase_ms(out->batch_phase_ms);
 	return 1;
 }
 

@@ -308,7 +308,7 @@ class ServerStats(C.Structure):
     _fields_ = [("in_flight", C.c_int), ("queued", C.c_int), ("batches", C.c_longlong),
                 ("batched_requests", C.c_longlong), ("device_ms", C.c_double), ("slow_batches", C.c_longlong),
                 ("slow_requests", C.c_longlong), ("slow_device_ms", C.c_double), ("batch_wall_ms", C.c_double),
-                ("rest_wall_ms", C.c_double), ("plan_ms", C.c_double)]
+                ("rest_wall_ms", C.c_double), ("plan_ms", C.c_double), ("batch_phase_ms", C.c_double * 10)]
 
 
 def server_api(lib: IWLib):

@@ -97,6 +97,11 @@ struct iwg_server_stats {
 	double batch_wall_ms;        /* host wall time of the dispatcher's batched calls */
 	double rest_wall_ms;         /* ... and of the requests they left to the plain form */
 	double plan_ms;              /* planning time, summed over requests */
+	double batch_phase_ms[10];   /* batched calls' host time (process-wide sums): preparation,
+	                                uploads, the passes' launches, the fix-up's launch, device
+	                                wait with downloads, the rest; within the passes' launches,
+	                                the table upload and the kernel attribute calls; within the
+	                                staged downloads, the device wait and the host copies */
 };
 /* device_budget: bytes of device memory one batch may hold (0: 8 GiB);
  * max_batch: requests per batch (0: 4096); host_threads (0: all cores). */
