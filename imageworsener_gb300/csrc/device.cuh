@@ -74,6 +74,7 @@ struct Job {
 	int out_w, out_h, out_n, out_depth, out_float;
 	DOut outc[kMaxCh];
 	int any_scan;
+	volatile int *done_flag;      // batched scans: set in mapped host memory once the image's output is final (null: none)
 	double *scanbuf;              // pre-quantisation values of dithered channels that scan serially
 	double *errbuf;               // error rows for error diffusion: [channel][3][out_w]
 

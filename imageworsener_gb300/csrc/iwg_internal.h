@@ -17,6 +17,7 @@
 
 #include <cstddef>
 #include <cstdint>
+#include <functional>
 #include <memory>
 #include <string>
 #include <vector>
@@ -275,7 +276,7 @@ void optimize(iw_context *ctx);
 // Device lanes (independent streams, buffers and table caches): lane 0 serves
 // the public entry points; a request server runs its serial dither scans on
 // lanes 1 .. kLanes-1.
-constexpr int kLanes = 5;
+constexpr int kLanes = 8;
 bool run_pipeline(iw_context *ctx, Plan &P, int warmup = 0, int iters = 1, int lane = 0);
 // Host wall time of the batched calls' phases, summed (ms): preparation,
 // uploads, the passes' launches, the fix-up's launch, device wait with
@@ -292,9 +293,13 @@ size_t batch_device_bytes(const Plan &P);
 // Runs the fast-form images of a batch together (pipeline.cu); see there.
 bool run_batch(const std::vector<iw_context *> &ctxs, const std::vector<Plan *> &plans, std::vector<int> &status,
 	double &dev_ms, int lane = 0);
-// The same in the plain (FP64) form for any image, scans in parallel (pipeline.cu).
+// The same in the plain (FP64) form for any image, scans in parallel
+// (pipeline.cu).  On a lane other than 0, on_done(i) is called for each image
+// as soon as its output is in the caller's buffer (status[i] is then 1 and
+// the context is not touched again); images not reported that way follow the
+// return as usual.
 bool run_batch_plain(const std::vector<iw_context *> &ctxs, const std::vector<Plan *> &plans, std::vector<int> &status,
-	double &dev_ms, int lane = 0);
+	double &dev_ms, int lane = 0, const std::function<void(int)> &on_done = nullptr);
 
 // api.cpp
 const char *get_option(iw_context *ctx, const char *name);

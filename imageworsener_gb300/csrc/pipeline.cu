@@ -679,11 +679,27 @@ __global__ void kb_hpass_exact(const Job *jobs, const int *start, int n, int tot
 	}
 }
 
-// one block per image, one warp per output channel
+// one block per image, one warp per output channel.  With a completion flag
+// the block also does the image's negation / blackening and then reports the
+// image done, so the host can take its output before the rest of the batch
+// ends (without one, kb_finalize follows for the whole batch).
 __global__ void kb_scan(const Job *jobs)
 {
 	const Job &J = jobs[blockIdx.x];
 	if(J.any_scan) scan_warp(J, threadIdx.x >> 5);
+	if(J.done_flag) {
+		__syncthreads();
+		if(J.any_scan && (J.negate || J.blacken)) {
+			const long long npx = (long long)J.out_w * J.out_h;
+			for(long long p = threadIdx.x; p < npx; p += blockDim.x) finalize_at(J, (int)(p % J.out_w), (int)(p / J.out_w));
+		}
+		__threadfence();   // every thread's output stores, device-wide, before the flag
+		__syncthreads();
+		if(threadIdx.x == 0) {
+			__threadfence_system();
+			*J.done_flag = 1;
+		}
+	}
 }
 
 __global__ void kb_finalize(const Job *jobs, const int *start, int n, int total)
@@ -1269,6 +1285,10 @@ struct DeviceState {
 	cudaStream_t stream = nullptr;
 	DevBuf in, interm, out, scan, err, params, flags;
 	DevBuf batch_io, batch_tab;   // batches: buffers + tables of all images
+	cudaStream_t dl_stream = nullptr;   // scan lanes: per-image downloads while the batch's scans run
+	int *done_h = nullptr;              // scan lanes: per-image completion flags (mapped host memory)
+	int *done_d = nullptr;
+	int done_cap = 0;
 	std::map<const void *, std::pair<std::shared_ptr<const void>, void *>> table_cache;
 	std::vector<uint8_t> staging;
 	Stager stager;
@@ -1334,6 +1354,10 @@ bool ensure_init(DeviceState &S, std::string &err)
 	for(DevBuf *b : {&S.in, &S.interm, &S.out, &S.scan, &S.err, &S.params, &S.flags, &S.batch_io, &S.batch_tab})
 		b->st = S.stream;
 	S.stager.patient = S.lane != 0;
+	if(S.lane != 0 && cudaStreamCreateWithPriority(&S.dl_stream, cudaStreamNonBlocking, least) != cudaSuccess) {
+		err = "cudaStreamCreate failed";
+		return false;
+	}
 	preload_kernels();
 	{   // keep freed stream-ordered memory in the pool rather than returning it at
 		// every synchronise; and never let an allocation on one lane reuse memory
@@ -1929,8 +1953,29 @@ bool run_batch(const std::vector<iw_context *> &ctxs, const std::vector<Plan *> 
 // dither scans of all images run at once, one warp per channel.  For images
 // the fast form does not take (error-diffusion / random dither, fp64
 // requests, ...).  status / dev_ms as run_batch.
+// Per-image completion flags of a scan lane: grow-only mapped host memory.
+static bool ensure_done_flags(DeviceState &S, int n)
+{
+	if(n <= S.done_cap) return true;
+	if(S.done_h) cudaFreeHost(S.done_h);
+	S.done_h = nullptr;
+	S.done_d = nullptr;
+	S.done_cap = 0;
+	const int cap = std::max(n, 256);
+	if(cudaHostAlloc((void **)&S.done_h, cap * sizeof(int), cudaHostAllocMapped) != cudaSuccess ||
+		cudaHostGetDevicePointer((void **)&S.done_d, S.done_h, 0) != cudaSuccess) {
+		cudaGetLastError();
+		if(S.done_h) cudaFreeHost(S.done_h);
+		S.done_h = nullptr;
+		S.done_d = nullptr;
+		return false;
+	}
+	S.done_cap = cap;
+	return true;
+}
+
 bool run_batch_plain(const std::vector<iw_context *> &ctxs, const std::vector<Plan *> &plans, std::vector<int> &status,
-	double &dev_ms, int lane)
+	double &dev_ms, int lane, const std::function<void(int)> &on_done)
 {
 	DeviceState &S = state(lane);
 	std::lock_guard<std::mutex> lk(S.mu);
@@ -1994,6 +2039,9 @@ bool run_batch_plain(const std::vector<iw_context *> &ctxs, const std::vector<Pl
 	}
 	if(run.empty()) return true;
 	const int m = (int)run.size();
+	// per-image completion: a scan lane with a caller that takes images one by one
+	const bool per_image = on_done && S.lane != 0 && ensure_done_flags(S, m);
+	if(per_image) memset(S.done_h, 0, m * sizeof(int));
 	// job array and block tables
 	std::vector<Job> djobs(m);
 	std::vector<int> sv(m), sh(m);
@@ -2002,6 +2050,7 @@ bool run_batch_plain(const std::vector<iw_context *> &ctxs, const std::vector<Pl
 	for(int k = 0; k < m; k++) {
 		const Job &J = jobs[run[k]];
 		djobs[k] = J;
+		djobs[k].done_flag = per_image ? S.done_d + k : nullptr;
 		sv[k] = (int)bv;
 		sh[k] = (int)bh;
 		bv += (long long)((J.mid_w + 127) / 128) * J.mid_h;
@@ -2051,25 +2100,77 @@ bool run_batch_plain(const std::vector<iw_context *> &ctxs, const std::vector<Pl
 	if(bv > 0) kb_vpass_exact<<<(unsigned)std::min<long long>(bv, cap), 128, 0, st>>>(dj, dsv, m, nv);
 	if(bh > 0) kb_hpass_exact<<<(unsigned)std::min<long long>(bh, cap), 128, 0, st>>>(dj, dsh, m, nh);
 	kb_scan<<<m, 32 * maxch, 0, st>>>(dj);
-	if(bh > 0) kb_finalize<<<(unsigned)std::min<long long>(bh, cap), 128, 0, st>>>(dj, dsh, m, nh);
+	if(bh > 0 && !per_image) kb_finalize<<<(unsigned)std::min<long long>(bh, cap), 128, 0, st>>>(dj, dsh, m, nh);
 	cudaEventRecord(e1, st);
-	// A scan lane queues its downloads only once its kernels are done: a copy
-	// queued behind a long scan can hold up other streams' copies.
-	if(S.lane != 0) wait_event(e1, true);
-	if(upmode == UP_COPY)
-		for(const Xfer &x : xout) cudaMemcpyAsync(x.host, x.dev, x.n, cudaMemcpyDeviceToHost, st);
-	if(upmode == UP_STAGE) stage_d2h(S.stager, st, xout);
+	std::vector<char> reported(m, 0);
+	if(per_image) {
+		// take each image as its scan block reports it: download on the
+		// lane's second stream, then hand it to the caller
+		const volatile int *flags = S.done_h;
+		int left = m;
+		for(;;) {
+			bool any = false;
+			for(int k = 0; k < m; k++) {
+				if(reported[k] || !flags[k]) continue;
+				const int i = run[k];
+				iw_context *ctx = ctxs[i];
+				reported[k] = 1;
+				left--;
+				any = true;
+				if(!zc) {
+					cudaMemcpyAsync(ctx->img2.pixels, base + o_out[i], out_bytes[i], cudaMemcpyDeviceToHost, S.dl_stream);
+					const cudaError_t de = cudaStreamSynchronize(S.dl_stream);
+					if(de != cudaSuccess) {
+						iw_set_error(ctx, (std::string("CUDA error: ") + cudaGetErrorString(de)).c_str());
+						status[i] = -1;
+						continue;
+					}
+				}
+				ctx->stats.form = 0;
+				ctx->stats.zero_copy = zc;
+				ctx->stats.kernels = 3;
+				ctx->stats.ms_device = 0;   // the batch's device time is not known yet
+				ctx->stats.flagged = 0;
+				status[i] = 1;
+				on_done(i);
+			}
+			if(left == 0) break;
+			if(cudaStreamQuery(st) != cudaErrorNotReady) {   // the kernels ended: a last look, then stop
+				bool late = false;
+				for(int k = 0; k < m; k++) if(!reported[k] && flags[k]) late = true;
+				if(!late) break;
+				continue;
+			}
+			if(!any) std::this_thread::sleep_for(std::chrono::microseconds(200));
+		}
+	}
+	else {
+		// A scan lane queues its downloads only once its kernels are done: a
+		// copy queued behind a long scan can hold up other streams' copies.
+		if(S.lane != 0) wait_event(e1, true);
+		if(upmode == UP_COPY)
+			for(const Xfer &x : xout) cudaMemcpyAsync(x.host, x.dev, x.n, cudaMemcpyDeviceToHost, st);
+		if(upmode == UP_STAGE) stage_d2h(S.stager, st, xout);
+	}
 	cudaError_t ce = wait_stream(st, S.lane != 0);
 	if(ce == cudaSuccess) ce = cudaGetLastError();
 	float ms = 0;
 	if(ce == cudaSuccess) cudaEventElapsedTime(&ms, e0, e1);
 	cudaEventDestroy(e0);
 	cudaEventDestroy(e1);
+	if(ce == cudaSuccess && per_image)
+		for(int k = 0; k < m; k++) if(!reported[k]) ce = cudaErrorUnknown;   // a block ended without its flag
 	if(ce != cudaSuccess) {
 		std::string msg = std::string("CUDA error: ") + cudaGetErrorString(ce);
-		return fail_all(msg.c_str());
+		for(int k = 0; k < m; k++) {
+			if(reported[k]) continue;   // already handed over, its bytes complete
+			iw_set_error(ctxs[run[k]], msg.c_str());
+			status[run[k]] = -1;
+		}
+		return false;
 	}
 	dev_ms = ms;
+	if(per_image) return true;   // every image was handed over as it finished
 	for(int i : run) {
 		iw_context *ctx = ctxs[i];
 		ctx->stats.form = 0;

@@ -125,6 +125,7 @@ void planner_loop(iwg_server *S)
 void run_plain(iwg_server *S, std::vector<iwg::Request *> &batch, int lane)
 {
 	for(iwg::Request *r : batch) r->started_ms = r->since_submit();
+	std::vector<char> handed(batch.size(), 0);
 	if(!batch.empty()) {
 		std::vector<iw_context *> cc;
 		std::vector<iwg::Plan *> pp;
@@ -134,8 +135,20 @@ void run_plain(iwg_server *S, std::vector<iwg::Request *> &batch, int lane)
 		}
 		std::vector<int> status;
 		double dev_ms = 0;
-		iwg::run_batch_plain(cc, pp, status, dev_ms, lane);
+		// on a scan lane each request goes on to its post-pass as soon as its
+		// own scan is done, not when the batch's longest one is
+		auto on_done = [&](int k) {
+			iwg::Request *r = batch[k];
+			r->ok = 1;
+			r->ran_ms = r->since_submit();
+			handed[k] = 1;
+			std::lock_guard<std::mutex> lk(S->mu);
+			S->finishing[size_class(r)].push_back(r);
+			S->cv_finish.notify_all();
+		};
+		iwg::run_batch_plain(cc, pp, status, dev_ms, lane, lane != 0 ? std::function<void(int)>(on_done) : nullptr);
 		for(size_t k = 0; k < batch.size(); k++) {
+			if(handed[k]) continue;
 			if(status[k] == 1) batch[k]->ok = 1;
 			else if(status[k] == 0) batch[k]->ok = iwg::run_pipeline(batch[k]->ctx, batch[k]->plan, 0, 1, lane) ? 1 : 0;
 			else batch[k]->ok = 0;
@@ -148,9 +161,9 @@ void run_plain(iwg_server *S, std::vector<iwg::Request *> &batch, int lane)
 			S->slow_device_ms += dev_ms;
 		}
 	}
-	for(iwg::Request *r : batch) r->ran_ms = r->since_submit();
+	for(size_t k = 0; k < batch.size(); k++) if(!handed[k]) batch[k]->ran_ms = batch[k]->since_submit();
 	std::lock_guard<std::mutex> lk(S->mu);
-	for(iwg::Request *r : batch) S->finishing[size_class(r)].push_back(r);
+	for(size_t k = 0; k < batch.size(); k++) if(!handed[k]) S->finishing[size_class(batch[k])].push_back(batch[k]);
 	S->cv_finish.notify_all();
 }
 
