@@ -679,25 +679,31 @@ __global__ void kb_hpass_exact(const Job *jobs, const int *start, int n, int tot
 	}
 }
 
-// one block per image, one warp per output channel.  With a completion flag
-// the block also does the image's negation / blackening and then reports the
+// One warp per output channel; a block takes images blockIdx.x,
+// blockIdx.x + gridDim.x, ...  The grid is at most one block per SM: two scan
+// warps on one SM sub-partition share its FP64 unit and each runs at about
+// half speed, so a second image on the same SM would finish no sooner than if
+// it waited its turn, and would delay the first.  With a completion flag the
+// block also does the image's negation / blackening and then reports the
 // image done, so the host can take its output before the rest of the batch
 // ends (without one, kb_finalize follows for the whole batch).
-__global__ void kb_scan(const Job *jobs)
+__global__ void kb_scan(const Job *jobs, int n)
 {
-	const Job &J = jobs[blockIdx.x];
-	if(J.any_scan) scan_warp(J, threadIdx.x >> 5);
-	if(J.done_flag) {
-		__syncthreads();
-		if(J.any_scan && (J.negate || J.blacken)) {
-			const long long npx = (long long)J.out_w * J.out_h;
-			for(long long p = threadIdx.x; p < npx; p += blockDim.x) finalize_at(J, (int)(p % J.out_w), (int)(p / J.out_w));
-		}
-		__threadfence();   // every thread's output stores, device-wide, before the flag
-		__syncthreads();
-		if(threadIdx.x == 0) {
-			__threadfence_system();
-			*J.done_flag = 1;
+	for(int g = blockIdx.x; g < n; g += gridDim.x) {
+		const Job &J = jobs[g];
+		if(J.any_scan) scan_warp(J, threadIdx.x >> 5);
+		__syncthreads();   // the shared staging buffers are reused by the next image
+		if(J.done_flag) {
+			if(J.any_scan && (J.negate || J.blacken)) {
+				const long long npx = (long long)J.out_w * J.out_h;
+				for(long long p = threadIdx.x; p < npx; p += blockDim.x) finalize_at(J, (int)(p % J.out_w), (int)(p / J.out_w));
+			}
+			__threadfence();   // every thread's output stores, device-wide, before the flag
+			__syncthreads();
+			if(threadIdx.x == 0) {
+				__threadfence_system();
+				*J.done_flag = 1;
+			}
 		}
 	}
 }
@@ -2099,7 +2105,7 @@ bool run_batch_plain(const std::vector<iw_context *> &ctxs, const std::vector<Pl
 	const int nv = (int)bv, nh = (int)bh;
 	if(bv > 0) kb_vpass_exact<<<(unsigned)std::min<long long>(bv, cap), 128, 0, st>>>(dj, dsv, m, nv);
 	if(bh > 0) kb_hpass_exact<<<(unsigned)std::min<long long>(bh, cap), 128, 0, st>>>(dj, dsh, m, nh);
-	kb_scan<<<m, 32 * maxch, 0, st>>>(dj);
+	kb_scan<<<std::min(m, sms), 32 * maxch, 0, st>>>(dj, m);
 	if(bh > 0 && !per_image) kb_finalize<<<(unsigned)std::min<long long>(bh, cap), 128, 0, st>>>(dj, dsh, m, nh);
 	cudaEventRecord(e1, st);
 	std::vector<char> reported(m, 0);
