@@ -278,6 +278,35 @@ __device__ __forceinline__ void vstream_tile(const FJob &F, float *s_tab, int bx
 
 // Exact float of a small unsigned integer (< 2^23) without an I2F: the code
 // is placed in the mantissa of 2^23 and 2^23 is subtracted.
+// Two floats in one 64-bit register pair, and Blackwell's paired FP32
+// operations on them: each half is rounded exactly like __fmaf_rn /
+// __fmul_rn, in half the instructions.
+__device__ __forceinline__ unsigned long long f2_pack(float lo, float hi)
+{
+	unsigned long long d;
+	asm("mov.b64 %0, {%1, %2};" : "=l"(d) : "f"(lo), "f"(hi));
+	return d;
+}
+
+__device__ __forceinline__ void f2_unpack(unsigned long long v, float &lo, float &hi)
+{
+	asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+
+__device__ __forceinline__ unsigned long long f2_fma(unsigned long long a, unsigned long long b, unsigned long long c)
+{
+	unsigned long long d;
+	asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+	return d;
+}
+
+__device__ __forceinline__ unsigned long long f2_mul(unsigned long long a, unsigned long long b)
+{
+	unsigned long long d;
+	asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+	return d;
+}
+
 __device__ __forceinline__ float u2f(unsigned int v)
 {
 	return __fsub_rn(__uint_as_float(0x4b000000u | v), 8388608.0f);
@@ -409,13 +438,13 @@ __device__ __forceinline__ void vbulk_tile(const FJob &F, unsigned char *s_raw, 
 	const unsigned long long plane = F.plane;
 	const int mid_w = F.mid_w;
 	float *const interm = F.interm;
-	float acc[NS][PX][NCH];
+	static_assert(PX == 2, "accumulators pair the thread's two pixels");
+	static_assert(NS == 4, "one 16-byte load of the slot weights per row (16-byte aligned: the decode table before them holds 256 or 8192 floats)");
+	unsigned long long acc[NS][NCH];   // (pixel 0, pixel 1) per slot and channel
 #pragma unroll
 	for(int s = 0; s < NS; s++)
 #pragma unroll
-		for(int px = 0; px < PX; px++)
-#pragma unroll
-			for(int c = 0; c < NCH; c++) acc[s][px][c] = 0.0f;
+		for(int c = 0; c < NCH; c++) acc[s][c] = 0ULL;
 
 	for(int q = 0; q < nq; q++) {
 		const int st = q % kBulkStages, use = q / kBulkStages;
@@ -431,10 +460,10 @@ __device__ __forceinline__ void vbulk_tile(const FJob &F, unsigned char *s_raw, 
 		}
 		__syncwarp();
 		if(lane == 0) mbar_arrive(empty + st);
-		float val[PX][NCH];
+		float val[PX][NCH], a[PX];
 #pragma unroll
 		for(int px = 0; px < PX; px++) {
-			float a = 1.0f;
+			a[px] = 1.0f;
 #pragma unroll
 			for(int c = 0; c < NCH; c++) {
 				const int sidx = px * NCH + c;
@@ -442,25 +471,28 @@ __device__ __forceinline__ void vbulk_tile(const FJob &F, unsigned char *s_raw, 
 				if(DEPTH == 8) code = __byte_perm(cur[sidx >> 2], 0u, 0x4440u + (sidx & 3));
 				else code = __byte_perm(cur[sidx >> 1], 0u, (sidx & 1) ? 0x4423u : 0x4401u);
 				if(ALPHA && c == NCH - 1) {
-					a = __fmul_rn(u2f(code), ainv);
-					val[px][c] = a;
+					a[px] = __fmul_rn(u2f(code), ainv);
+					val[px][c] = a[px];
 				}
 				else val[px][c] = dec_table<DEPTH>(s_tab, code);
 			}
-			if(ALPHA) {
-#pragma unroll
-				for(int c = 0; c < NCH - 1; c++) val[px][c] = __fmul_rn(val[px][c], a);
-			}
 		}
-		float ws[NS];
+		unsigned long long v2[NCH];
 #pragma unroll
-		for(int s = 0; s < NS; s++) ws[s] = s_w[q * NS + s];
+		for(int c = 0; c < NCH; c++) v2[c] = f2_pack(val[0][c], val[1][c]);
+		if(ALPHA) {
+			const unsigned long long a2 = f2_pack(a[0], a[1]);
 #pragma unroll
-		for(int s = 0; s < NS; s++)
+			for(int c = 0; c < NCH - 1; c++) v2[c] = f2_mul(v2[c], a2);   // premultiply
+		}
+		const float4 wq = *reinterpret_cast<const float4 *>(s_w + q * NS);
+		const float wsv[4] = {wq.x, wq.y, wq.z, wq.w};
 #pragma unroll
-			for(int px = 0; px < PX; px++)
+		for(int s = 0; s < NS; s++) {
+			const unsigned long long w2 = f2_pack(wsv[s], wsv[s]);
 #pragma unroll
-				for(int c = 0; c < NCH; c++) acc[s][px][c] = __fmaf_rn(val[px][c], ws[s], acc[s][px][c]);
+			for(int c = 0; c < NCH; c++) acc[s][c] = f2_fma(v2[c], w2, acc[s][c]);
+		}
 		const int2 fin = s_fin[q];
 		for(int k = 0; k < fin.y; k++) {
 			const int j = fin.x + k;
@@ -472,17 +504,15 @@ __device__ __forceinline__ void vbulk_tile(const FJob &F, unsigned char *s_raw, 
 					if(keep) {
 						float *o = interm + (unsigned long long)j * mid_w + x0;
 #pragma unroll
-						for(int px = 0; px < PX; px++) {
-							if(full_px || x0 + px < mid_w) {
-#pragma unroll
-								for(int c = 0; c < NCH; c++) o[(unsigned long long)c * plane + px] = acc[s][px][c];
-							}
+						for(int c = 0; c < NCH; c++) {
+							float lo, hi;
+							f2_unpack(acc[s][c], lo, hi);
+							o[(unsigned long long)c * plane] = lo;
+							if(full_px) o[(unsigned long long)c * plane + 1] = hi;
 						}
 					}
 #pragma unroll
-					for(int px = 0; px < PX; px++)
-#pragma unroll
-						for(int c = 0; c < NCH; c++) acc[s][px][c] = 0.0f;
+					for(int c = 0; c < NCH; c++) acc[s][c] = 0ULL;
 				}
 			}
 		}

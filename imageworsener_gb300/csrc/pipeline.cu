@@ -798,7 +798,8 @@ __device__ __forceinline__ bool interm_df_all(const Job &J, unsigned int mask, i
 	else {
 		const int tb = W.off[j], te = W.off[j + 1];
 		n = te - tb;
-		for(int t = tb; t < te; t++) {
+#pragma unroll 4
+		for(int t = tb; t < te; t++) {   // unrolled so that the taps' loads are in flight together
 			const int src = W.src[t];
 			if(src >= 0) add_tap(src, df_of(J.df_wv[t]), false);   // edge taps add 0
 		}
@@ -819,26 +820,55 @@ __device__ __forceinline__ bool interm_df_all(const Job &J, unsigned int mask, i
 	return ok;
 }
 
+// Ordered-dither thresholds (rank + 0.5) / 64: exact in float and double,
+// equal to the reference's (double)(rank + 0.5) / 64.0.
+__device__ __forceinline__ float dither_threshold(int rank) { return __fmul_rn((float)rank + 0.5f, 0.015625f); }
+
+// quantize_exact's code for one end of an interval, with FP64 only for the
+// two distances: the clamp, bracket and exactness tests compare bit patterns
+// (order-preserving for non-negative doubles), and the ordered-dither
+// fraction d_lo / (d_lo + d_hi) is taken in FP32.  That fraction is within
+// 3.1e-7 of the reference's double one (each float rounding adds at most
+// 2^-24 relative, the fraction is at most 1), so a decision 1e-6 or more
+// away from the threshold is the reference's; nearer, 'ok' is cleared and
+// the caller falls back to the exact path.
+__device__ __forceinline__ int quantize_end(const DQuant &q, double v, int x, int y, bool &ok)
+{
+	long long vb = __double_as_longlong(v);
+	if((vb & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL) return 0;   // NaN: both candidate codes convert to 0
+	if(vb < 0) vb = 0;                                                  // v < 0 (or -0): +0
+	else if(vb > 0x3ff0000000000000LL) vb = 0x3ff0000000000000LL;       // v > 1: 1
+	if(q.use_nc) {
+		const long long *nc = reinterpret_cast<const long long *>(q.nc);
+		int lo = 0, hi = 255;
+		while(lo < hi) {
+			const int mid = (lo + hi) >> 1;
+			if(__ldg(nc + mid) <= vb) lo = mid + 1; else hi = mid;
+		}
+		return lo;
+	}
+	const int k = bracket_index(q, vb);
+	const int clo = q.code[k], chi = q.code[k + 1];
+	if(k == q.P || vb < __ldg(reinterpret_cast<const long long *>(q.X) + k)) return clo;   // exact
+	const double vc = __longlong_as_double(vb);
+	const double d_lo = dsub(vc, q.rev[clo]), d_hi = dsub(q.rev[chi], vc);
+	if(q.dfam == IW_DITHERFAMILY_ORDERED) {
+		const float fl = (float)d_lo, fh = (float)d_hi;
+		const float f = __fdiv_rn(fl, __fadd_rn(fl, fh));
+		const float thr = dither_threshold(dither_rank(q.dsub, x, y));
+		if(fabsf(__fsub_rn(f, thr)) <= 1e-6f) ok = false;
+		return f >= thr ? chi : clo;
+	}
+	return dle_bits(d_hi, d_lo) ? chi : clo;
+}
+
 // Output code of every v in [vlo, vhi] as quantize_exact computes it;
-// 'ok' false if it is not the same code over the interval.
+// 'ok' false if it is not the same code over the interval (the decision is
+// monotone in v within a bracket, and each end is checked above).
 __device__ __forceinline__ int quantize_interval(const DQuant &q, double vlo, double vhi, int x, int y, bool &ok)
 {
-	const int clo = quantize_exact(q, vlo, x, y), chi = quantize_exact(q, vhi, x, y);
+	const int clo = quantize_end(q, vlo, x, y, ok), chi = quantize_end(q, vhi, x, y, ok);
 	if(clo != chi) ok = false;
-	if(q.dfam == IW_DITHERFAMILY_ORDERED && !q.use_nc) {
-		// the rounded dither fraction may wobble by a few ulps: keep away from the threshold
-		const double thr = ddiv((double)dither_rank(q.dsub, x, y) + 0.5, 64.0);
-		for(int e = 0; e < 2; e++) {
-			double v = e ? vhi : vlo;
-			if(v < 0.0) v = 0.0;
-			if(v > 1.0) v = 1.0;
-			if(v != v) continue;
-			const Bracket b = bracket_exact(q, v);
-			if(b.exact) continue;
-			const double f = ddiv(b.d_lo, dadd(b.d_lo, b.d_hi));
-			if(fabs(dsub(f, thr)) <= 1.8e-15) ok = false;
-		}
-	}
 	return clo;
 }
 
@@ -928,7 +958,7 @@ __device__ bool fix_pixel_df(const Job &J, int i, int j, unsigned int mask, floa
 // quantisation -- with the alpha value and alpha code passed between lanes.
 // The result equals pixel_exact()'s.  Scratch: 'maxt' floats per channel per warp.
 template<bool BATCH>
-__global__ void k_fix_flagged_warp(Job J1, const Job *jobs, int *count, const int *list, int maxt)
+__global__ void __launch_bounds__(128, 8) k_fix_flagged_warp(Job J1, const Job *jobs, int *count, const int *list, int maxt)
 {
 	extern __shared__ float fix_cache[];
 	const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, wpb = blockDim.x >> 5;
@@ -1317,6 +1347,18 @@ DeviceState &state(int lane = 0)
 	return *s[(unsigned)lane % (unsigned)kLanes];
 }
 
+// A kernel that needs 256 bytes of local memory per thread, launched once
+// at initialisation: the driver sizes its local-memory allocation at the
+// first launch that needs more than it has, and that resize waits for the
+// whole device; done here, before any lane runs work, no later launch of the
+// library's kernels (at most a few dozen bytes of spill) has to resize.
+__global__ void k_size_local_memory(int *sink)
+{
+	volatile int buf[64];
+	for(int k = 0; k < 64; k++) buf[k] = k + (int)threadIdx.x;
+	if(sink) sink[threadIdx.x] = buf[(threadIdx.x * 7) & 63];
+}
+
 // Every kernel of the library, loaded once per process before any lane runs
 // work: under lazy module loading a kernel's first launch loads its module,
 // and that can wait for long scans running on other lanes.
@@ -1324,6 +1366,8 @@ void preload_kernels()
 {
 	static std::once_flag once;
 	std::call_once(once, [] {
+		k_size_local_memory<<<1, 32>>>(nullptr);
+		cudaDeviceSynchronize();
 		cudaFuncAttributes a;
 		for(const void *k : {(const void *)k_vpass_exact, (const void *)k_hpass_exact, (const void *)k_scan,
 			(const void *)k_finalize, (const void *)kb_vpass_exact, (const void *)kb_hpass_exact, (const void *)kb_scan,
