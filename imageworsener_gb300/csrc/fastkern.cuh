@@ -811,7 +811,8 @@ __device__ __forceinline__ void hpass_pixel(const FJob &F, int i, int j)
 	const float *rowp[NPL];
 #pragma unroll
 	for(int c = 0; c < NPL; c++) rowp[c] = F.interm + (unsigned long long)c * F.plane + (unsigned long long)j * F.mid_w;
-	for(int t = t0; t < t1; t++) {
+#pragma unroll 4
+	for(int t = t0; t < t1; t++) {   // unrolled: several taps' loads in flight at once
 		const int src = __ldg(F.hsrc + t);
 		if(src < 0) continue;   // transparent edge: value 0
 		const float w = __ldg(F.hw + t), aw = fabsf(w);

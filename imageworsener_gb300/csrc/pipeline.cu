@@ -872,10 +872,42 @@ __device__ __forceinline__ int quantize_interval(const DQuant &q, double vlo, do
 	return clo;
 }
 
+// Starts loading the input window of flagged pixel (i, j) -- the rows of its
+// vertical taps, the byte range of its horizontal taps -- into L1 (whole
+// warp, one prefetch per 32 bytes).  The re-evaluation then reads it with
+// chains of dependent loads (tap -> sample -> decode table) that would
+// otherwise each wait for DRAM.  A hint only: identity orientation, byte
+// samples.
+__device__ __forceinline__ void prefetch_window(const Job &J, int i, int j, int lane)
+{
+	if(J.orient != 0 || J.in_depth < 8) return;
+	const DWeights &WH = J.wh[J.mid[0].wh], &WV = J.wv[J.mid[0].wv];
+	int xlo = 0x7fffffff, xhi = -1;
+	const int t0 = WH.kind == 1 ? i : WH.off[i], nt = WH.kind == 1 ? 1 : WH.off[i + 1] - t0;
+	for(int t = lane; t < nt; t += 32) {
+		const int s = WH.src[t0 + t];
+		if(s >= 0) { xlo = min(xlo, s); xhi = max(xhi, s); }
+	}
+	xlo = __reduce_min_sync(0xffffffffu, xlo);
+	xhi = __reduce_max_sync(0xffffffffu, xhi);
+	if(xhi < 0) return;
+	const unsigned long long bpp = (unsigned long long)J.in_nphys * (J.in_depth / 8);
+	const unsigned long long b0 = (unsigned long long)(J.crop_x + xlo) * bpp, b1 = (unsigned long long)(J.crop_x + xhi + 1) * bpp;
+	const int tb = WV.kind == 1 ? j : WV.off[j], nv = WV.kind == 1 ? 1 : WV.off[j + 1] - tb;
+	for(int t = lane; t < nv; t += 32) {
+		const int s = WV.src[tb + t];
+		if(s < 0) continue;
+		const uint8_t *row = J.in + (unsigned long long)(J.crop_y + s) * J.in_bpr;
+		for(unsigned long long b = b0; b < b1; b += 32) asm volatile("prefetch.global.L1 [%0];" :: "l"(row + b));
+		asm volatile("prefetch.global.L1 [%0];" :: "l"(row + b1 - 1));
+	}
+}
+
 // Re-evaluates flagged pixel (i, j) in double-float (whole warp); returns
 // true (warp-uniform) with the codes stored if every decision was certain.
 __device__ bool fix_pixel_df(const Job &J, int i, int j, unsigned int mask, float *my, int maxt, int lane)
 {
+	prefetch_window(J, i, j, lane);
 	bool bad = false;
 	{
 		// one lane per horizontal tap, all masked channels at once
