@@ -32,7 +32,7 @@ namespace iwg {
 
 using namespace dev;
 
-void launch_fix_flagged(cudaStream_t st, const Job &J, int *count, const int *list);
+void launch_fix_flagged(cudaStream_t st, const Job &J, int *count, int *list, int cap);
 
 namespace {
 
@@ -304,7 +304,7 @@ void fast_launch_impl(cudaStream_t st, void *state, void (*mark)(void *), void *
 	cudaLaunchKernel(S.hkernel, S.hgrid, dim3(kHThreads), fargs, 0, st);
 	mark(markarg);
 	// exact re-evaluation of flagged pixels (recomputes the vertical pass too)
-	launch_fix_flagged(st, S.J, S.F.flag_count, S.F.flag_list);
+	launch_fix_flagged(st, S.J, S.F.flag_count, S.F.flag_list, (int)std::min<size_t>(S.flag_entries, 0x7fffffff));
 	mark(markarg);
 }
 

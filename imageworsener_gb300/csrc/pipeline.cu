@@ -989,8 +989,12 @@ __device__ bool fix_pixel_df(const Job &J, int i, int j, unsigned int mask, floa
 // finishes intermediate channel m -- its horizontal sum, unassociation and
 // quantisation -- with the alpha value and alpha code passed between lanes.
 // The result equals pixel_exact()'s.  Scratch: 'maxt' floats per channel per warp.
+// Pixels the double-float tier cannot certify go to the FP64 path.  They are
+// listed at the tail of the flag list (entry cap-1-L for the L-th), where a
+// block per pixel spreads the work (k_fix_leftover); while that region does
+// not reach the flagged entries (cap - L > n), else the warp does it here.
 template<bool BATCH>
-__global__ void __launch_bounds__(128, 8) k_fix_flagged_warp(Job J1, const Job *jobs, int *count, const int *list, int maxt)
+__global__ void __launch_bounds__(128, 8) k_fix_flagged_warp(Job J1, const Job *jobs, int *count, int *list, int maxt, int cap)
 {
 	extern __shared__ float fix_cache[];
 	const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, wpb = blockDim.x >> 5;
@@ -1006,7 +1010,14 @@ __global__ void __launch_bounds__(128, 8) k_fix_flagged_warp(Job J1, const Job *
 			__syncwarp();
 			continue;
 		}
-		if(lane == 0) atomicAdd(count + 1, 1);   // pixels that needed the FP64 path
+		int slot = 0;
+		if(lane == 0) slot = cap - 1 - atomicAdd(count + 1, 1);   // pixels that needed the FP64 path
+		slot = __shfl_sync(0xffffffffu, slot, 0);
+		if(slot >= n) {   // room at the tail: a block per pixel takes it
+			if(lane == 0) reinterpret_cast<int4 *>(list)[slot] = e;
+			__syncwarp();
+			continue;
+		}
 		__syncwarp();
 		const int ntask = __popc(mask) * maxt;
 		for(int k = lane; k < ntask; k += 32) {
@@ -1057,6 +1068,75 @@ __global__ void __launch_bounds__(128, 8) k_fix_flagged_warp(Job J1, const Job *
 	}
 }
 
+// The FP64 path for the pixels k_fix_flagged_warp listed at the tail, one
+// block per pixel: the block's threads recompute the intermediate values of
+// every (channel, horizontal tap) at once, then warp 0 finishes each channel
+// as k_fix_flagged_warp does (lane m: channel m).
+template<bool BATCH>
+__global__ void __launch_bounds__(256) k_fix_leftover(Job J1, const Job *jobs, const int *count, const int *list, int maxt,
+	int cap)
+{
+	extern __shared__ float fix_cache[];
+	float *my = fix_cache;
+	const int n = *count, left = min(count[1], cap - n);
+	const int lane = threadIdx.x & 31;
+	for(int L = blockIdx.x; L < left; L += gridDim.x) {
+		const int4 e = reinterpret_cast<const int4 *>(list)[cap - 1 - L];
+		const Job &J = BATCH ? jobs[e.z] : J1;
+		const int p = e.x;
+		const unsigned int mask = (unsigned int)e.y & ((1u << J.mid_n) - 1u);
+		const int i = p % J.out_w, j = p / J.out_w;
+		const int ntask = __popc(mask) * maxt;
+		for(int k = threadIdx.x; k < ntask; k += blockDim.x) {
+			const int r = k / maxt, t = k - r * maxt;
+			const int m = nth_bit(mask, r);
+			const DWeights &W = J.wh[J.mid[m].wh];
+			const int t0 = W.kind == 1 ? i : W.off[i];
+			const int nt = W.kind == 1 ? 1 : W.off[i + 1] - t0;
+			if(t < nt) {
+				const int src = W.src[t0 + t];
+				if(src >= 0) my[m * maxt + t] = (float)interm_exact<true>(J, m, src, j);
+			}
+		}
+		__syncthreads();
+		if(threadIdx.x < 32) {
+			const bool mine = lane < J.mid_n && ((mask >> lane) & 1u);
+			double s = 0.0;
+			if(mine) s = hsum_exact(J, lane, i, j, [&](int m, int k, int) { return (double)my[m * maxt + k]; });
+			const int al = J.mid_alpha >= 0 ? J.mid_alpha : 0;
+			const double a = (double)__double2float_rn(__shfl_sync(0xffffffffu, s, al));
+			int code = -1, oc = -1;
+			bool is_alpha = false;
+			if(mine) {
+				const DMid &mc = J.mid[lane];
+				is_alpha = mc.ctype == IW_CHANNELTYPE_ALPHA;
+				oc = mc.out_ch;
+				if(oc >= 0) {
+					const DOut &o = J.outc[oc];
+					const double v = unassoc_and_bkgd(J, mc, o, s, a, checker_alt(J, i, j), is_alpha);
+					if(J.out_float) {
+						float fv = __double2float_rn(v);
+						if(J.negate && !is_alpha) fv = __fsub_rn(1.0f, fv);
+						store_float(J, oc, i, j, fv);
+					}
+					else if(o.scan) J.scanbuf[((unsigned long long)oc * J.out_h + j) * J.out_w + i] = v;
+					else code = quantize_exact(o.q, v, i, j);
+				}
+			}
+			const int ac = __shfl_sync(0xffffffffu, code, al);
+			const int alpha_code = (J.mid_alpha >= 0 && J.mid[al].out_ch >= 0) ? ac : -1;
+			if(code >= 0) {
+				if(!is_alpha) {
+					if(J.negate) code = J.outc[oc].maxcc - code;
+					if(J.blacken && alpha_code == 0) code = 0;
+				}
+				store_code(J, oc, i, j, (unsigned int)code);
+			}
+		}
+		__syncthreads();   // 'my' is reused by the next pixel
+	}
+}
+
 // Fallback for very wide horizontal windows: one thread per flagged pixel.
 template<bool BATCH>
 __global__ void k_fix_flagged_thread(Job J1, const Job *jobs, int *count, const int *list)
@@ -1072,31 +1152,46 @@ __global__ void k_fix_flagged_thread(Job J1, const Job *jobs, int *count, const 
 	}
 }
 
-// Launches the exact re-evaluation of flagged pixels on 'st'.
-void launch_fix_flagged(cudaStream_t st, const Job &J, int *count, const int *list)
+// Launches the exact re-evaluation of flagged pixels on 'st': a warp per
+// pixel (double-float, then FP64), and a block per pixel for those listed at
+// the tail of the flag list (capacity 'cap' entries).  Returns the launches.
+template<bool BATCH>
+static int launch_fix(cudaStream_t st, const Job &J, const Job *jobs, int maxt, int *count, int *list, int cap)
 {
-	int maxt = 1;
-	for(int m = 0; m < J.mid_n; m++) maxt = maxt > J.wh[J.mid[m].wh].max_taps ? maxt : J.wh[J.mid[m].wh].max_taps;
 	const size_t per_warp = (size_t)dev::kMaxCh * maxt * sizeof(float);
 	int wpb = 4;
 	while(wpb > 1 && per_warp * wpb > 48 * 1024) wpb >>= 1;
-	// Flagged pixels are independent and each is a latency-bound FP64 chain:
+	int sms = 152;
+	cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
+	// Flagged pixels are independent and each is a latency-bound chain:
 	// launch enough warps to take them all at once (idle warps exit at once).
-	if(per_warp * wpb <= 48 * 1024) k_fix_flagged_warp<false><<<24 * 152, 32 * wpb, per_warp * wpb, st>>>(J, nullptr, count, list, maxt);
-	else k_fix_flagged_thread<false><<<24 * 152, 64, 0, st>>>(J, nullptr, count, list);
+	// With narrow windows a pixel's FP64 path is short and runs in place,
+	// hidden behind the other warps; from 48 taps on it goes to a block.
+	if(per_warp * wpb <= 48 * 1024) {
+		const bool tail = maxt >= 48;
+		k_fix_flagged_warp<BATCH><<<24 * sms, 32 * wpb, per_warp * wpb, st>>>(J, jobs, count, list, maxt, tail ? cap : 0);
+		if(!tail) return 1;
+		k_fix_leftover<BATCH><<<4 * sms, 256, per_warp, st>>>(J, jobs, count, list, maxt, cap);
+		return 2;
+	}
+	k_fix_flagged_thread<BATCH><<<24 * sms, 64, 0, st>>>(J, jobs, count, list);
+	return 1;
+}
+
+void launch_fix_flagged(cudaStream_t st, const Job &J, int *count, int *list, int cap)
+{
+	int maxt = 1;
+	for(int m = 0; m < J.mid_n; m++) maxt = maxt > J.wh[J.mid[m].wh].max_taps ? maxt : J.wh[J.mid[m].wh].max_taps;
+	launch_fix<false>(st, J, nullptr, maxt, count, list, cap);
 }
 
 // The same for a batch: flag entries name their image in 'jobs' (device
 // memory); maxt is the widest horizontal window of any image.
-void launch_fix_flagged_batch(cudaStream_t st, const Job *jobs, int maxt, int *count, const int *list)
+int launch_fix_flagged_batch(cudaStream_t st, const Job *jobs, int maxt, int *count, int *list, int cap)
 {
-	const size_t per_warp = (size_t)dev::kMaxCh * maxt * sizeof(float);
-	int wpb = 4;
-	while(wpb > 1 && per_warp * wpb > 48 * 1024) wpb >>= 1;
 	Job none;
 	memset(&none, 0, sizeof(none));
-	if(per_warp * wpb <= 48 * 1024) k_fix_flagged_warp<true><<<24 * 152, 32 * wpb, per_warp * wpb, st>>>(none, jobs, count, list, maxt);
-	else k_fix_flagged_thread<true><<<24 * 152, 64, 0, st>>>(none, jobs, count, list);
+	return launch_fix<true>(st, none, jobs, maxt, count, list, cap);
 }
 
 // ===========================================================================
@@ -1404,6 +1499,7 @@ void preload_kernels()
 		for(const void *k : {(const void *)k_vpass_exact, (const void *)k_hpass_exact, (const void *)k_scan,
 			(const void *)k_finalize, (const void *)kb_vpass_exact, (const void *)kb_hpass_exact, (const void *)kb_scan,
 			(const void *)kb_finalize, (const void *)k_fix_flagged_warp<true>, (const void *)k_fix_flagged_warp<false>,
+			(const void *)k_fix_leftover<true>, (const void *)k_fix_leftover<false>,
 			(const void *)k_fix_flagged_thread<true>, (const void *)k_fix_flagged_thread<false>})
 			cudaFuncGetAttributes(&a, k);
 		preload_fast_kernels();
@@ -1968,8 +2064,8 @@ bool run_batch(const std::vector<iw_context *> &ctxs, const std::vector<Plan *> 
 	cudaEventRecord(ev_f, st);
 	pt.mark(2);
 	if(launches >= 0) {
-		launch_fix_flagged_batch(st, (const Job *)(tbase + o_jobs), maxt, flag_count, flag_list);
-		launches++;
+		launches += launch_fix_flagged_batch(st, (const Job *)(tbase + o_jobs), maxt, flag_count, flag_list,
+			(int)std::min<size_t>(nflag, 0x7fffffff));
 	}
 	cudaEventRecord(e1, st);
 	pt.mark(3);
