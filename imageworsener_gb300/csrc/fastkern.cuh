@@ -932,7 +932,7 @@ struct FastState {
 	X(4, 2, true, 16, 4) X(6, 2, true, 16, 4) X(8, 2, true, 16, 4) \
 	X(4, 1, false, 16, 8) X(6, 1, false, 16, 8) X(8, 1, false, 16, 8) \
 	X(4, 4, true, 8, 2) X(6, 4, true, 8, 2) X(8, 4, true, 8, 2) \
-	X(4, 3, false, 8, 4) \
+	X(4, 3, false, 8, 4) X(6, 3, false, 8, 4) X(8, 3, false, 8, 4) \
 	X(4, 2, true, 8, 4) X(6, 2, true, 8, 4) X(8, 2, true, 8, 4) \
 	X(4, 1, false, 8, 8) X(6, 1, false, 8, 8) X(8, 1, false, 8, 8)
 // Instances of the bulk-copy vertical kernel: (NS, channels, alpha, depth, PX)
