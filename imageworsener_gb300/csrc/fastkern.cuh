@@ -811,8 +811,36 @@ __device__ __forceinline__ void hpass_pixel(const FJob &F, int i, int j)
 	const float *rowp[NPL];
 #pragma unroll
 	for(int c = 0; c < NPL; c++) rowp[c] = F.interm + (unsigned long long)c * F.plane + (unsigned long long)j * F.mid_w;
-#pragma unroll 4
-	for(int t = t0; t < t1; t++) {   // unrolled: several taps' loads in flight at once
+	// Four taps at a time: their sources, weights and samples are all loaded
+	// before the first multiply-add, then accumulated in tap order.  A
+	// transparent edge tap (source -1) reads column 0 and contributes 0.
+	int t = t0;
+	for(; t + 4 <= t1; t += 4) {
+		int src[4];
+		float w[4], I[4][NPL];
+#pragma unroll
+		for(int u = 0; u < 4; u++) {
+			src[u] = __ldg(F.hsrc + t + u);
+			w[u] = __ldg(F.hw + t + u);
+		}
+#pragma unroll
+		for(int u = 0; u < 4; u++) {
+			const int sc = src[u] < 0 ? 0 : src[u];
+#pragma unroll
+			for(int c = 0; c < NPL; c++) I[u][c] = __ldg(rowp[c] + sc);
+		}
+#pragma unroll
+		for(int u = 0; u < 4; u++) {
+			const float aw = fabsf(w[u]);
+#pragma unroll
+			for(int c = 0; c < NPL; c++) {
+				const float x = src[u] < 0 ? 0.0f : I[u][c];
+				v[c] = __fmaf_rn(x, w[u], v[c]);
+				T[c] = __fmaf_rn(fabsf(x), aw, T[c]);
+			}
+		}
+	}
+	for(; t < t1; t++) {
 		const int src = __ldg(F.hsrc + t);
 		if(src < 0) continue;   // transparent edge: value 0
 		const float w = __ldg(F.hw + t), aw = fabsf(w);
