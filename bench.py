@@ -64,7 +64,7 @@ WORKLOADS = {
 class Stats(C.Structure):
     _fields_ = [("ms_total", C.c_double), ("ms_device", C.c_double), ("ms_part", C.c_double * 4),
                 ("flagged", C.c_longlong), ("form", C.c_int), ("kernels", C.c_int), ("zero_copy", C.c_int),
-                ("flagged_exact", C.c_longlong)]
+                ("flagged_exact", C.c_longlong), ("vertical_tensor", C.c_int)]
 
 
 _T0 = time.perf_counter()
@@ -188,11 +188,12 @@ def output_digest(lib: IWLib, ctx) -> str:
     return r.digest()
 
 
-def device_timed(lib: IWLib, job, warmup: int, steps: int, form: str):
+def device_timed(lib: IWLib, job, warmup: int, steps: int, form: str, vertical: str = "auto"):
     lib.dll.iwg_process_image_timed.restype = C.c_int
     lib.dll.iwg_process_image_timed.argtypes = [C.c_void_p, C.c_int, C.c_int]
     lib.dll.iwg_get_stats.argtypes = [C.c_void_p, C.POINTER(Stats)]
-    ctx = make_ctx(lib, job, [("iw_set_option", b"gpu:precision", form.encode())])
+    ctx = make_ctx(lib, job, [("iw_set_option", b"gpu:precision", form.encode()),
+                              ("iw_set_option", b"gpu:vertical", vertical.encode())])
     try:
         ok = lib.dll.iwg_process_image_timed(ctx, warmup, steps)
         if not ok:
@@ -549,14 +550,19 @@ def main():
             batched = batch_leg(lib, args.batch_images, min(args.batch_pool, args.batch_images),
                                 os.cpu_count() or 1, 0 if args.no_cpu_baseline else 64)
         large = {}
-        for name in (() if args.no_large else ("small", "downscale", "downscale_fs4")):
-            progress(f"other configuration: {name}")
+        # the large downscale also with its vertical pass on the CUDA cores
+        # (the default puts windows this wide on the tensor cores)
+        legs = (("small", "small", "auto"), ("downscale", "downscale", "auto"),
+                ("downscale_cuda_vertical", "downscale", "cuda"), ("downscale_fs4", "downscale_fs4", "auto"))
+        for label, name, vertical in (() if args.no_large else legs):
+            progress(f"other configuration: {label}")
             ljob = WORKLOADS[name]()
-            lst, ldig = device_timed(lib, ljob, 1, 3, "fp32")
-            large[name] = {"ms": lst.ms_device, "mpix_s": W.out_pixels(ljob) / 1e6 / (lst.ms_device / 1000.0),
-                           "input_gb_s": len(ljob.pixels) / 1e9 / (lst.ms_device / 1000.0), "form": lst.form,
-                           "flagged": lst.flagged, "left_to_fp64": lst.flagged_exact, "kernel_ms": list(lst.ms_part)[:3],
-                           "bit_exact": ldig == golden_digest(name)}
+            lst, ldig = device_timed(lib, ljob, 1, 3, "fp32", vertical)
+            large[label] = {"ms": lst.ms_device, "mpix_s": W.out_pixels(ljob) / 1e6 / (lst.ms_device / 1000.0),
+                            "input_gb_s": len(ljob.pixels) / 1e9 / (lst.ms_device / 1000.0), "form": lst.form,
+                            "vertical_tensor": lst.vertical_tensor, "flagged": lst.flagged,
+                            "left_to_fp64": lst.flagged_exact, "kernel_ms": list(lst.ms_part)[:3],
+                            "bit_exact": ldig == golden_digest(name)}
         serving = None
         if args.serve_seconds > 0:
             progress("serving configuration")

@@ -24,7 +24,7 @@ BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libimagew_gb300.so")
 
 HOST_SRCS = ["api.cpp", "plan.cpp", "weights.cpp", "tables.cpp", "optimize.cpp", "server.cpp"]
-DEVICE_SRCS = ["pipeline.cu", "fastpath.cu", "fastbatch.cu", "noalloc.cu"]
+DEVICE_SRCS = ["pipeline.cu", "fastpath.cu", "fastbatch.cu", "noalloc.cu", "tcvert.cu"]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 

@@ -6,6 +6,7 @@
 
 #include "iwg_internal.h"
 #include "device.cuh"
+#include "tcvert.cuh"
 
 #include <cstdint>
 #include <vector>
@@ -38,6 +39,7 @@ struct FTail {        // quantisation of one output channel, float tables
 };
 
 constexpr int kLutCells = 1024;
+constexpr int kHBlock = 16;   // horizontal taps per partial sum (blocked summation)
 
 struct FJob {
 	// input
@@ -811,45 +813,57 @@ __device__ __forceinline__ void hpass_pixel(const FJob &F, int i, int j)
 	const float *rowp[NPL];
 #pragma unroll
 	for(int c = 0; c < NPL; c++) rowp[c] = F.interm + (unsigned long long)c * F.plane + (unsigned long long)j * F.mid_w;
-	// Four taps at a time: their sources, weights and samples are all loaded
-	// before the first multiply-add, then accumulated in tap order.  A
+	// Taps are summed in blocks of kHBlock: a block's products are accumulated
+	// into a partial sum (fused multiply-adds from 0) that is then added to the
+	// total, so a product passes through at most kHBlock + ceil(n / kHBlock)
+	// roundings instead of n (the host's bound uses that count).  Within a
+	// block, four taps at a time: their sources, weights and samples are all
+	// loaded before the first multiply-add, then accumulated in tap order.  A
 	// transparent edge tap (source -1) reads column 0 and contributes 0.
 	int t = t0;
-	for(; t + 4 <= t1; t += 4) {
-		int src[4];
-		float w[4], I[4][NPL];
+	while(t < t1) {
+		const int tb = min(t + kHBlock, t1);
+		float p[NPL];
 #pragma unroll
-		for(int u = 0; u < 4; u++) {
-			src[u] = __ldg(F.hsrc + t + u);
-			w[u] = __ldg(F.hw + t + u);
-		}
+		for(int c = 0; c < NPL; c++) p[c] = 0.0f;
+		for(; t + 4 <= tb; t += 4) {
+			int src[4];
+			float w[4], I[4][NPL];
 #pragma unroll
-		for(int u = 0; u < 4; u++) {
-			const int sc = src[u] < 0 ? 0 : src[u];
+			for(int u = 0; u < 4; u++) {
+				src[u] = __ldg(F.hsrc + t + u);
+				w[u] = __ldg(F.hw + t + u);
+			}
 #pragma unroll
-			for(int c = 0; c < NPL; c++) I[u][c] = __ldg(rowp[c] + sc);
-		}
+			for(int u = 0; u < 4; u++) {
+				const int sc = src[u] < 0 ? 0 : src[u];
 #pragma unroll
-		for(int u = 0; u < 4; u++) {
-			const float aw = fabsf(w[u]);
+				for(int c = 0; c < NPL; c++) I[u][c] = __ldg(rowp[c] + sc);
+			}
 #pragma unroll
-			for(int c = 0; c < NPL; c++) {
-				const float x = src[u] < 0 ? 0.0f : I[u][c];
-				v[c] = __fmaf_rn(x, w[u], v[c]);
-				T[c] = __fmaf_rn(fabsf(x), aw, T[c]);
+			for(int u = 0; u < 4; u++) {
+				const float aw = fabsf(w[u]);
+#pragma unroll
+				for(int c = 0; c < NPL; c++) {
+					const float x = src[u] < 0 ? 0.0f : I[u][c];
+					p[c] = __fmaf_rn(x, w[u], p[c]);
+					T[c] = __fmaf_rn(fabsf(x), aw, T[c]);
+				}
 			}
 		}
-	}
-	for(; t < t1; t++) {
-		const int src = __ldg(F.hsrc + t);
-		if(src < 0) continue;   // transparent edge: value 0
-		const float w = __ldg(F.hw + t), aw = fabsf(w);
+		for(; t < tb; t++) {
+			const int src = __ldg(F.hsrc + t);
+			if(src < 0) continue;   // transparent edge: value 0
+			const float w = __ldg(F.hw + t), aw = fabsf(w);
 #pragma unroll
-		for(int c = 0; c < NPL; c++) {
-			const float I = __ldg(rowp[c] + src);
-			v[c] = __fmaf_rn(I, w, v[c]);
-			T[c] = __fmaf_rn(fabsf(I), aw, T[c]);
+			for(int c = 0; c < NPL; c++) {
+				const float I = __ldg(rowp[c] + src);
+				p[c] = __fmaf_rn(I, w, p[c]);
+				T[c] = __fmaf_rn(fabsf(I), aw, T[c]);
+			}
 		}
+#pragma unroll
+		for(int c = 0; c < NPL; c++) v[c] = __fadd_rn(v[c], p[c]);
 	}
 	float E[NPL];
 #pragma unroll
@@ -950,6 +964,10 @@ struct FastState {
 	const float2 *df_atab = nullptr;
 	size_t o_wvdf = 0, o_whdf = 0;
 	bool df = false;
+	// vertical pass on the tensor cores (tcvert.cu) instead of vkernel's FJob launch
+	bool tc = false;
+	tc::TcJob T;
+	size_t o_tct = 0, o_tcb = 0, o_tcl = 0;
 };
 
 // Template instances of the vertical kernels, shared by the per-image and

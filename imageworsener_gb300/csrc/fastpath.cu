@@ -13,7 +13,9 @@
 //   decode   |a' - a| <= e_dec + r_dec * a          (e_dec measured over every code)
 //   vertical |I' - I_ref| <= e_dec*W1v + c1 * (|I'| + 2*Wneg_v)
 //   horizontal |v' - v_ref| <= K0 + K1 * sum_k |I'_k||w_k|
-// with c1 = (r_dec + 2u + gamma_nv + gamma_nv^(fp64)) and K0, K1 assembled on
+// with c1 = (r_dec + 2u + gamma_nv + gamma_nv^(fp64)), the horizontal sum's
+// c2 = (u + gamma_(b+nb+1) + gamma_nh^(fp64)) for blocks of b = min(nh, kHBlock)
+// taps (nb = ceil(nh / kHBlock) partial sums), and K0, K1 assembled on
 // the host below; unassociating alpha divides by the float alpha, whose own
 // bound is propagated.
 #include "iwg_internal.h"
@@ -299,7 +301,8 @@ void fast_launch_impl(cudaStream_t st, void *state, void (*mark)(void *), void *
 	FastState &S = *static_cast<FastState *>(state);
 	cudaMemsetAsync(S.F.flag_count, 0, 3 * sizeof(int), st);
 	void *fargs[] = {&S.F};
-	cudaLaunchKernel(S.vkernel, S.vgrid, dim3(S.vthreads), fargs, S.vsmem, st);
+	void *targs[] = {&S.T};
+	cudaLaunchKernel(S.vkernel, S.vgrid, dim3(S.vthreads), S.tc ? targs : fargs, S.vsmem, st);
 	mark(markarg);
 	cudaLaunchKernel(S.hkernel, S.hgrid, dim3(kHThreads), fargs, 0, st);
 	mark(markarg);
@@ -317,7 +320,7 @@ void fast_release(FastInfo &fi)
 // Host preparation of one image: job layout, error model, per-image arrays
 // (in FastState::blob, placed later) and kernel choice.  'batch' picks
 // taller vertical tiles (many images fill the GPU).  Caller holds the cache lock.
-static FastState *fast_build(const Plan &P, const Job &J, bool batch, std::string &err)
+static FastState *fast_build(const Plan &P, const Job &J, bool batch, int tc_mode, std::string &err)
 {
 	FJob F;
 	memset(&F, 0, sizeof(F));
@@ -383,7 +386,7 @@ static FastState *fast_build(const Plan &P, const Job &J, bool batch, std::strin
 	for(int q = 0; q < nplanes; q++) {
 		double r_dec = keys[q].premul ? 3.0 * u : 0.0;
 		double c1 = (r_dec + 2.0 * u + gamma_n(nv + 1, u) + gamma_n(nv + 1, ud)) * 1.01;
-		double c2 = (u + gamma_n(nh + 1, u) + gamma_n(nh + 1, ud)) * 1.01;
+		double c2 = (u + gamma_n(std::min(nh, kHBlock) + (nh + kHBlock - 1) / kHBlock + 1, u) + gamma_n(nh + 1, ud)) * 1.01;
 		double ed = e_dec * (keys[q].premul ? 1.0 : 1.0);
 		double K0 = (ed * W1v * W1h + 2.02 * c1 * Wnv * W1h) * 1.05;
 		double K1 = (1.01 * c1 + c2) * 1.05;
@@ -601,6 +604,62 @@ static FastState *fast_build(const Plan &P, const Job &J, bool batch, std::strin
 	IWG_VGATHER_VARIANTS(IWG_VGATHER)
 #undef IWG_VSTREAM
 #undef IWG_VGATHER
+	// Vertical pass on the tensor cores (tcvert.cu): 8-bit channels decoded
+	// through the input table, no alpha, rows in device memory.  Its bound is
+	// far tighter than an FP32 sum over a wide window (fixed-point quantisation
+	// only), which is what pays for wide windows: fewer flagged pixels.
+	// tc_mode: 0 never, 1 windows of kTcAutoTaps rows or more, 2 whenever eligible.
+	constexpr int kTcAutoTaps = 48;
+	if(!batch && tc_mode != 0 && (tc_mode == 2 || nv >= kTcAutoTaps) && in_device && ident && F.alpha_src < 0 &&
+		P.in_depth == 8 && v_bpp == P.in_nphys && coltab && P.crop_h > 0) {
+		bool all_tab = true;
+		for(int q = 0; q < nplanes; q++)
+			if(!F.pl[q].table || F.pl[q].premul) all_tab = false;
+		std::vector<const std::vector<double> *> tabs(nplanes, coltab.get());
+		tc::TcBuild TB;
+		if(all_tab && tc::tc_build(WV, P.crop_h, nplanes, tabs, TB)) {
+			int dev = 0, sms = 152;
+			if(cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+				sms = 152;
+			cudaGetLastError();
+			const size_t tsm = tc::tc_smem_bytes(nplanes);
+			const bool tvec = v_base % 4 == 0 && P.in_bpr % 4 == 0;
+			const void *tk = tc::tc_kernel(tvec);
+			int strips = 0, bands = 0, bpb = 0;
+			tc::tc_geometry(TB, J.mid_w * nplanes, sms, strips, bands, bpb);
+			if(cudaFuncSetAttribute(tk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsm) == cudaSuccess) {
+				FS->tc = true;
+				FS->vkernel = tk;
+				FS->vgrid = dim3(strips, bands);
+				FS->vthreads = tc::kThreads;
+				FS->vsmem = tsm;
+				FS->vv.kind = 5;
+				tc::TcJob &T = FS->T;
+				memset(&T, 0, sizeof(T));
+				T.in_rows = P.crop_h;
+				T.cols = J.mid_w * nplanes;
+				T.nphys = nplanes;
+				T.mid_w = J.mid_w;
+				T.mid_h = J.mid_h;
+				T.plane = J.interm_plane;
+				T.nblk = TB.nblk;
+				T.blocks_per_band = bpb;
+				T.scale = TB.scale;
+				FS->o_tct = add(TB.tiles.data(), TB.tiles.size());
+				FS->o_tcb = add(TB.blk.data(), TB.blk.size() * sizeof(int4));
+				FS->o_tcl = add(TB.lut.data(), TB.lut.size() * sizeof(uint2));
+				// error model of the exact-integer pass: |I' - I_ref| <= e_abs*1.01 + (2u + gamma_nv^(fp64))*(|I'| + 2*Wneg_v)
+				const double ed_tc = TB.e_abs * 1.01 / std::max(W1v, 1e-300);
+				for(int q = 0; q < nplanes; q++) {
+					double c1 = (2.0 * u + gamma_n(nv + 1, ud)) * 1.01;
+					double c2 = (u + gamma_n(std::min(nh, kHBlock) + (nh + kHBlock - 1) / kHBlock + 1, u) + gamma_n(nh + 1, ud)) * 1.01;
+					F.K0[q] = (float)((ed_tc * W1v * W1h + 2.02 * c1 * Wnv * W1h) * 1.05);
+					F.K1[q] = (float)((1.01 * c1 + c2) * 1.05);
+				}
+			}
+			cudaGetLastError();
+		}
+	}
 	if(!FS->vkernel) { delete FS; err = "fast form: no kernel for this layout"; return nullptr; }
 	switch(nplanes) {
 	case 1: FS->hkernel = (const void *)k_hpass_fast<1>; break;
@@ -639,6 +698,16 @@ static void fast_place(FastState *FS, const uint8_t *base, int *flag_count, int 
 	F.voff = (const int *)(base + FS->o_voff);
 	F.vsrc = (const int *)(base + FS->o_vsrc);
 	F.vw = (const float *)(base + FS->o_vw);
+	if(FS->tc) {
+		tc::TcJob &T = FS->T;
+		T.in = F.in + (size_t)F.crop_x * F.nphys + (unsigned long long)F.crop_y * F.in_bpr;
+		T.in_bpr = F.in_bpr;
+		T.interm = F.interm;
+		T.err_flag = F.err_flag;
+		T.tiles = (const uint4 *)(base + FS->o_tct);
+		T.blk = (const int4 *)(base + FS->o_tcb);
+		T.lut = (const uint2 *)(base + FS->o_tcl);
+	}
 	Job &J = FS->J;
 	for(int m = 0; m < dev::kMaxCh; m++) J.df_tab[m] = FS->df ? FS->df_tab[m] : nullptr;
 	J.df_atab = FS->df ? FS->df_atab : nullptr;
@@ -657,7 +726,7 @@ bool fast_prepare(cudaStream_t st, const Plan &P, Job &J, FastInfo &fi, std::str
 {
 	Cache &C = cache();
 	std::lock_guard<std::mutex> lk(C.mu);
-	FastState *FS = fast_build(P, J, false, err);
+	FastState *FS = fast_build(P, J, false, fi.tc_mode, err);
 	if(!FS) return false;
 	const size_t flag_off = (FS->blob.size() + 255) & ~(size_t)255;
 	const size_t need = flag_off + 256 + FS->flag_entries * 16;
@@ -681,6 +750,7 @@ bool fast_prepare(cudaStream_t st, const Plan &P, Job &J, FastInfo &fi, std::str
 	fi.launch_fn = fast_launch_impl;
 	fi.streaming = FS->streaming;
 	fi.slots = FS->F.ns;
+	fi.tc = FS->tc ? 1 : 0;
 	fi.flag_count_dev = FS->F.flag_count;
 	return true;
 }
@@ -691,7 +761,7 @@ void *fast_batch_item(const Plan &P, const Job &J, std::string &err)
 {
 	Cache &C = cache();
 	std::lock_guard<std::mutex> lk(C.mu);
-	return fast_build(P, J, true, err);
+	return fast_build(P, J, true, 0, err);
 }
 
 size_t fast_item_blob_bytes(const void *item) { return static_cast<const FastState *>(item)->blob.size(); }
@@ -730,6 +800,8 @@ void preload_fast_kernels()
 #undef IWG_PRE_PX
 #undef IWG_PRE_ST
 #undef IWG_PRE_GA
+	cudaFuncGetAttributes(&a, tc::tc_kernel(true));
+	cudaFuncGetAttributes(&a, tc::tc_kernel(false));
 	cudaFuncGetAttributes(&a, (const void *)k_hpass_fast<1>);
 	cudaFuncGetAttributes(&a, (const void *)k_hpass_fast<2>);
 	cudaFuncGetAttributes(&a, (const void *)k_hpass_fast<3>);

@@ -13,6 +13,8 @@ struct Plan;
 struct FastInfo {
 	int streaming = 0;   // vertical pass streams input rows into register slots
 	int slots = 0;       // register slots per column (streaming)
+	int tc_mode = 1;     // in: vertical pass on the tensor cores: 0 never, 1 wide windows, 2 whenever eligible
+	int tc = 0;          // out: the vertical pass runs on the tensor cores
 	int *flag_count_dev = nullptr;   // device counter of pixels re-evaluated exactly
 	void *state = nullptr;            // prepared launch state (fastpath.cu)
 	int launches = 0;

@@ -174,6 +174,7 @@ struct Stats {   // per call, readable through the iwg_* extension API
 	int form = 0;                // 0 = plain FP64, 1 = FP32 + guard band
 	int kernels = 0;             // kernel launches issued
 	int zero_copy = 0;           // kernels read/wrote the host image buffers directly
+	int vertical_tensor = 0;     // the vertical pass ran on the tensor cores
 };
 
 }  // namespace iwg

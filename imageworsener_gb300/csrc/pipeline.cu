@@ -903,6 +903,8 @@ __device__ __forceinline__ void prefetch_window(const Job &J, int i, int j, int 
 	}
 }
 
+__device__ __forceinline__ bool fix_df_finish(const Job &J, int i, int j, unsigned int mask, const float *my, int maxt, int lane);
+
 // Re-evaluates flagged pixel (i, j) in double-float (whole warp); returns
 // true (warp-uniform) with the codes stored if every decision was certain.
 __device__ bool fix_pixel_df(const Job &J, int i, int j, unsigned int mask, float *my, int maxt, int lane)
@@ -921,6 +923,15 @@ __device__ bool fix_pixel_df(const Job &J, int i, int j, unsigned int mask, floa
 	}
 	if(__any_sync(0xffffffffu, bad)) return false;
 	__syncwarp();
+	return fix_df_finish(J, i, j, mask, my, maxt, lane);
+}
+
+// Second half of the double-float re-evaluation of pixel (i, j), one warp:
+// lane m sums channel m's horizontal taps from the certified intermediate
+// values in 'my' (maxt per channel), unassociates and quantises; true
+// (warp-uniform) with the codes stored if every decision was certain.
+__device__ __forceinline__ bool fix_df_finish(const Job &J, int i, int j, unsigned int mask, const float *my, int maxt, int lane)
+{
 	const bool mine = lane < J.mid_n && ((mask >> lane) & 1u);
 	dfl s = {0.0f, 0.0f};
 	float A = 0.0f;
@@ -1068,72 +1079,128 @@ __global__ void __launch_bounds__(128, 8) k_fix_flagged_warp(Job J1, const Job *
 	}
 }
 
-// The FP64 path for the pixels k_fix_flagged_warp listed at the tail, one
-// block per pixel: the block's threads recompute the intermediate values of
-// every (channel, horizontal tap) at once, then warp 0 finishes each channel
-// as k_fix_flagged_warp does (lane m: channel m).
+// The FP64 path of one flagged pixel, by a whole block: the block's threads
+// recompute the intermediate values of every (channel, horizontal tap) at
+// once, then warp 0 finishes each channel as k_fix_flagged_warp does (lane m:
+// channel m).  Every thread of the block calls it with the same entry.
+__device__ void fix_pixel_fp64_block(const Job &J, int4 e, float *my, int maxt)
+{
+	const int lane = threadIdx.x & 31;
+	const int p = e.x;
+	const unsigned int mask = (unsigned int)e.y & ((1u << J.mid_n) - 1u);
+	const int i = p % J.out_w, j = p / J.out_w;
+	const int ntask = __popc(mask) * maxt;
+	for(int k = threadIdx.x; k < ntask; k += blockDim.x) {
+		const int r = k / maxt, t = k - r * maxt;
+		const int m = nth_bit(mask, r);
+		const DWeights &W = J.wh[J.mid[m].wh];
+		const int t0 = W.kind == 1 ? i : W.off[i];
+		const int nt = W.kind == 1 ? 1 : W.off[i + 1] - t0;
+		if(t < nt) {
+			const int src = W.src[t0 + t];
+			if(src >= 0) my[m * maxt + t] = (float)interm_exact<true>(J, m, src, j);
+		}
+	}
+	__syncthreads();
+	if(threadIdx.x < 32) {
+		const bool mine = lane < J.mid_n && ((mask >> lane) & 1u);
+		double s = 0.0;
+		if(mine) s = hsum_exact(J, lane, i, j, [&](int m, int k, int) { return (double)my[m * maxt + k]; });
+		const int al = J.mid_alpha >= 0 ? J.mid_alpha : 0;
+		const double a = (double)__double2float_rn(__shfl_sync(0xffffffffu, s, al));
+		int code = -1, oc = -1;
+		bool is_alpha = false;
+		if(mine) {
+			const DMid &mc = J.mid[lane];
+			is_alpha = mc.ctype == IW_CHANNELTYPE_ALPHA;
+			oc = mc.out_ch;
+			if(oc >= 0) {
+				const DOut &o = J.outc[oc];
+				const double v = unassoc_and_bkgd(J, mc, o, s, a, checker_alt(J, i, j), is_alpha);
+				if(J.out_float) {
+					float fv = __double2float_rn(v);
+					if(J.negate && !is_alpha) fv = __fsub_rn(1.0f, fv);
+					store_float(J, oc, i, j, fv);
+				}
+				else if(o.scan) J.scanbuf[((unsigned long long)oc * J.out_h + j) * J.out_w + i] = v;
+				else code = quantize_exact(o.q, v, i, j);
+			}
+		}
+		const int ac = __shfl_sync(0xffffffffu, code, al);
+		const int alpha_code = (J.mid_alpha >= 0 && J.mid[al].out_ch >= 0) ? ac : -1;
+		if(code >= 0) {
+			if(!is_alpha) {
+				if(J.negate) code = J.outc[oc].maxcc - code;
+				if(J.blacken && alpha_code == 0) code = 0;
+			}
+			store_code(J, oc, i, j, (unsigned int)code);
+		}
+	}
+	__syncthreads();   // 'my' is reused by the next pixel
+}
+
+// The FP64 path for the pixels listed at the tail of the flag list, one
+// block per pixel.
 template<bool BATCH>
 __global__ void __launch_bounds__(256) k_fix_leftover(Job J1, const Job *jobs, const int *count, const int *list, int maxt,
 	int cap)
 {
 	extern __shared__ float fix_cache[];
-	float *my = fix_cache;
 	const int n = *count, left = min(count[1], cap - n);
-	const int lane = threadIdx.x & 31;
 	for(int L = blockIdx.x; L < left; L += gridDim.x) {
 		const int4 e = reinterpret_cast<const int4 *>(list)[cap - 1 - L];
+		fix_pixel_fp64_block(BATCH ? jobs[e.z] : J1, e, fix_cache, maxt);
+	}
+}
+
+// Re-evaluation of flagged pixels with wide horizontal windows (48 taps or
+// more), one block per pixel: the block's threads (one per horizontal tap)
+// compute the certified double-float intermediate values the pixel reads --
+// each a vertical sum over the pixel's rows, its loads in flight together
+// with those of the other taps -- then warp 0 finishes as fix_pixel_df does.
+// A pixel the double-float tier cannot decide is listed at the tail of the
+// flag list for k_fix_leftover while there is room, else its FP64 path runs
+// here.  Scratch: kMaxCh * maxt floats of shared memory.
+template<bool BATCH>
+__global__ void __launch_bounds__(256, 1) k_fix_wide_df(Job J1, const Job *jobs, int *count, int *list, int maxt, int cap)
+{
+	extern __shared__ float fix_cache[];
+	float *my = fix_cache;
+	__shared__ int s_ok, s_slot;
+	const int n = *count;
+	const int lane = threadIdx.x & 31;
+	for(int f = blockIdx.x; f < n; f += gridDim.x) {
+		const int4 e = reinterpret_cast<const int4 *>(list)[f];
 		const Job &J = BATCH ? jobs[e.z] : J1;
 		const int p = e.x;
 		const unsigned int mask = (unsigned int)e.y & ((1u << J.mid_n) - 1u);
 		const int i = p % J.out_w, j = p / J.out_w;
-		const int ntask = __popc(mask) * maxt;
-		for(int k = threadIdx.x; k < ntask; k += blockDim.x) {
-			const int r = k / maxt, t = k - r * maxt;
-			const int m = nth_bit(mask, r);
-			const DWeights &W = J.wh[J.mid[m].wh];
+		bool bad = J.df_wv == nullptr;
+		if(!bad) {
+			const DWeights &W = J.wh[J.mid[0].wh];
 			const int t0 = W.kind == 1 ? i : W.off[i];
 			const int nt = W.kind == 1 ? 1 : W.off[i + 1] - t0;
-			if(t < nt) {
+			for(int t = threadIdx.x; t < nt; t += blockDim.x) {
 				const int src = W.src[t0 + t];
-				if(src >= 0) my[m * maxt + t] = (float)interm_exact<true>(J, m, src, j);
+				if(src >= 0 && !interm_df_all(J, mask, src, j, my + t, maxt)) bad = true;
 			}
+		}
+		bad = __syncthreads_or(bad) != 0;
+		if(threadIdx.x < 32) {
+			const bool ok = !bad && fix_df_finish(J, i, j, mask, my, maxt, lane);
+			if(lane == 0) s_ok = ok ? 1 : 0;
 		}
 		__syncthreads();
-		if(threadIdx.x < 32) {
-			const bool mine = lane < J.mid_n && ((mask >> lane) & 1u);
-			double s = 0.0;
-			if(mine) s = hsum_exact(J, lane, i, j, [&](int m, int k, int) { return (double)my[m * maxt + k]; });
-			const int al = J.mid_alpha >= 0 ? J.mid_alpha : 0;
-			const double a = (double)__double2float_rn(__shfl_sync(0xffffffffu, s, al));
-			int code = -1, oc = -1;
-			bool is_alpha = false;
-			if(mine) {
-				const DMid &mc = J.mid[lane];
-				is_alpha = mc.ctype == IW_CHANNELTYPE_ALPHA;
-				oc = mc.out_ch;
-				if(oc >= 0) {
-					const DOut &o = J.outc[oc];
-					const double v = unassoc_and_bkgd(J, mc, o, s, a, checker_alt(J, i, j), is_alpha);
-					if(J.out_float) {
-						float fv = __double2float_rn(v);
-						if(J.negate && !is_alpha) fv = __fsub_rn(1.0f, fv);
-						store_float(J, oc, i, j, fv);
-					}
-					else if(o.scan) J.scanbuf[((unsigned long long)oc * J.out_h + j) * J.out_w + i] = v;
-					else code = quantize_exact(o.q, v, i, j);
-				}
+		if(!s_ok) {
+			if(threadIdx.x == 0) s_slot = cap - 1 - atomicAdd(count + 1, 1);   // pixels that needed the FP64 path
+			__syncthreads();
+			const int slot = s_slot;
+			if(slot >= n) {
+				if(threadIdx.x == 0) reinterpret_cast<int4 *>(list)[slot] = e;
 			}
-			const int ac = __shfl_sync(0xffffffffu, code, al);
-			const int alpha_code = (J.mid_alpha >= 0 && J.mid[al].out_ch >= 0) ? ac : -1;
-			if(code >= 0) {
-				if(!is_alpha) {
-					if(J.negate) code = J.outc[oc].maxcc - code;
-					if(J.blacken && alpha_code == 0) code = 0;
-				}
-				store_code(J, oc, i, j, (unsigned int)code);
-			}
+			else fix_pixel_fp64_block(J, e, my, maxt);
 		}
-		__syncthreads();   // 'my' is reused by the next pixel
+		__syncthreads();   // s_ok, s_slot and 'my' are reused by the next pixel
 	}
 }
 
@@ -1167,6 +1234,13 @@ static int launch_fix(cudaStream_t st, const Job &J, const Job *jobs, int maxt, 
 	// launch enough warps to take them all at once (idle warps exit at once).
 	// With narrow windows a pixel's FP64 path is short and runs in place,
 	// hidden behind the other warps; from 48 taps on it goes to a block.
+	if(maxt >= 48 && per_warp <= 48 * 1024) {
+		// wide windows: a block per pixel, one thread per horizontal tap
+		const int tpb = std::min(256, (maxt + 31) / 32 * 32);
+		k_fix_wide_df<BATCH><<<8 * sms, tpb, per_warp, st>>>(J, jobs, count, list, maxt, cap);
+		k_fix_leftover<BATCH><<<4 * sms, 256, per_warp, st>>>(J, jobs, count, list, maxt, cap);
+		return 2;
+	}
 	if(per_warp * wpb <= 48 * 1024) {
 		const bool tail = maxt >= 48;
 		k_fix_flagged_warp<BATCH><<<24 * sms, 32 * wpb, per_warp * wpb, st>>>(J, jobs, count, list, maxt, tail ? cap : 0);
@@ -1499,6 +1573,7 @@ void preload_kernels()
 		for(const void *k : {(const void *)k_vpass_exact, (const void *)k_hpass_exact, (const void *)k_scan,
 			(const void *)k_finalize, (const void *)kb_vpass_exact, (const void *)kb_hpass_exact, (const void *)kb_scan,
 			(const void *)kb_finalize, (const void *)k_fix_flagged_warp<true>, (const void *)k_fix_flagged_warp<false>,
+			(const void *)k_fix_wide_df<true>, (const void *)k_fix_wide_df<false>,
 			(const void *)k_fix_leftover<true>, (const void *)k_fix_leftover<false>,
 			(const void *)k_fix_flagged_thread<true>, (const void *)k_fix_flagged_thread<false>})
 			cudaFuncGetAttributes(&a, k);
@@ -1798,12 +1873,18 @@ bool run_pipeline(iw_context *ctx, Plan &P, int warmup, int iters, int lane)
 	const char *prec = get_option(ctx, "gpu:precision");
 	bool want_plain = prec && !strcmp(prec, "fp64");
 	FastInfo fi;
+	{
+		const char *vt = get_option(ctx, "gpu:vertical");
+		fi.tc_mode = (vt && !strcmp(vt, "cuda")) ? 0 : ((vt && !strcmp(vt, "tensor")) ? 2 : 1);
+	}
 	bool fast = !want_plain && fast_eligible(P, J, fi);
 	ctx->stats.form = fast ? 1 : 0;
+	ctx->stats.vertical_tensor = 0;
 	if(fast && !fast_prepare(st, P, J, fi, err)) {
 		iw_set_error(ctx, err.c_str());
 		return false;
 	}
+	ctx->stats.vertical_tensor = fast ? fi.tc : 0;
 
 	// The device passes, launched warmup+iters times; the input stays resident.
 	// Events bracket every launch group of the timed iterations.
@@ -2396,6 +2477,7 @@ extern "C" int iwg_get_stats(struct iw_context *ctx, struct iwg_stats *out)
 	out->kernels = ctx->stats.kernels;
 	out->zero_copy = ctx->stats.zero_copy;
 	out->flagged_exact = ctx->stats.flagged_exact;
+	out->vertical_tensor = ctx->stats.vertical_tensor;
 	return 1;
 }
 

@@ -12,6 +12,14 @@
  *     Integer output is identical to the reference's.
  *   - "fp64": the reference's double-precision arithmetic throughout.
  * Select one per context with iw_set_option(ctx, "gpu:precision", "fp64").
+ *
+ * Vertical pass of the fp32 form.  For 8-bit inputs decoded through a table
+ * (no alpha) the vertical pass can run on the tensor cores as exact integer
+ * products of 8-bit digits of the fixed-point sample and weight; its error
+ * bound is far tighter than an FP32 sum's, so fewer samples are re-evaluated.
+ * iw_set_option(ctx, "gpu:vertical", v) with v = "auto" (default: tensor
+ * cores for windows of 48 rows or more), "tensor" (whenever eligible) or
+ * "cuda" (never).  The output is the same in every case.
  */
 #ifndef IMAGEW_GB300_H
 #define IMAGEW_GB300_H
@@ -36,6 +44,9 @@ struct iwg_stats {
 	                          host memory directly (no staging copies) */
 	long long flagged_exact; /* of the flagged pixels, those the double-float
 	                          tier could not decide and FP64 recomputed */
+	int vertical_tensor;   /* 1: the vertical pass ran on the tensor cores
+	                          (exact integer digit products; see the
+	                          "gpu:vertical" option) */
 };
 
 /* Copies the statistics of the context's last run into *out.  Returns 1. */
