@@ -801,6 +801,9 @@ __device__ __forceinline__ void store_code_f(const FJob &F, int ch, int x, int y
 	}
 }
 
+template<int NPL>
+__device__ __forceinline__ void hpass_tail(const FJob &F, int i, int j, const float (&v)[NPL], const float (&T)[NPL]);
+
 // Horizontal pass + tail for output pixel (i, j).
 template<int NPL>
 __device__ __forceinline__ void hpass_pixel(const FJob &F, int i, int j)
@@ -865,6 +868,52 @@ __device__ __forceinline__ void hpass_pixel(const FJob &F, int i, int j)
 #pragma unroll
 		for(int c = 0; c < NPL; c++) v[c] = __fadd_rn(v[c], p[c]);
 	}
+	hpass_tail<NPL>(F, i, j, v, T);
+}
+
+// Horizontal pass for wide windows, a warp per output pixel (i, j): lane l
+// accumulates taps l, l+32, ... (fused multiply-adds from 0), then a butterfly
+// of five additions gives every lane the same total, so a product passes
+// through at most ceil(n / 32) + 5 roundings (the host's bound uses that
+// count).  Lane 0 decides the codes.
+template<int NPL>
+__device__ __forceinline__ void hpass_pixel_warp(const FJob &F, int i, int j, int lane)
+{
+	if(i >= F.out_w || j >= F.out_h) return;
+	float v[NPL], T[NPL];
+#pragma unroll
+	for(int c = 0; c < NPL; c++) { v[c] = 0.0f; T[c] = 0.0f; }
+	const int t0 = F.hoff[i], t1 = F.hoff[i + 1];
+	const float *rowp[NPL];
+#pragma unroll
+	for(int c = 0; c < NPL; c++) rowp[c] = F.interm + (unsigned long long)c * F.plane + (unsigned long long)j * F.mid_w;
+	for(int t = t0 + lane; t < t1; t += 32) {
+		const int src = __ldg(F.hsrc + t);
+		const float w = __ldg(F.hw + t), aw = fabsf(w);
+		if(src < 0) continue;   // transparent edge: value 0
+#pragma unroll
+		for(int c = 0; c < NPL; c++) {
+			const float I = __ldg(rowp[c] + src);
+			v[c] = __fmaf_rn(I, w, v[c]);
+			T[c] = __fmaf_rn(fabsf(I), aw, T[c]);
+		}
+	}
+#pragma unroll
+	for(int off = 16; off > 0; off >>= 1) {
+#pragma unroll
+		for(int c = 0; c < NPL; c++) {
+			v[c] = __fadd_rn(v[c], __shfl_xor_sync(0xffffffffu, v[c], off));
+			T[c] = __fadd_rn(T[c], __shfl_xor_sync(0xffffffffu, T[c], off));
+		}
+	}
+	if(lane == 0) hpass_tail<NPL>(F, i, j, v, T);
+}
+
+// Quantisation tail of output pixel (i, j) from its horizontal sums v and
+// their magnitude sums T (error bound E = K0 + K1 * T per plane).
+template<int NPL>
+__device__ __forceinline__ void hpass_tail(const FJob &F, int i, int j, const float (&v)[NPL], const float (&T)[NPL])
+{
 	float E[NPL];
 #pragma unroll
 	for(int c = 0; c < NPL; c++) E[c] = __fmaf_rn(F.K1[c], T[c], F.K0[c]);

@@ -74,6 +74,15 @@ __global__ void __launch_bounds__(kHThreads) k_hpass_fast(FJob F)
 	hpass_pixel<NPL>(F, blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y);
 }
 
+// wide windows: a warp per output pixel, kHThreads / 32 pixels per block
+template<int NPL>
+__global__ void __launch_bounds__(kHThreads) k_hpass_warp(FJob F)
+{
+	hpass_pixel_warp<NPL>(F, blockIdx.x * (kHThreads / 32) + (threadIdx.x >> 5), blockIdx.y, threadIdx.x & 31);
+}
+
+constexpr int kHWarpTaps = 64;   // horizontal windows from this many taps: a warp per pixel
+
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
@@ -383,10 +392,14 @@ static FastState *fast_build(const Plan &P, const Job &J, bool batch, int tc_mod
 	const int nv = std::max(1, WV.max_taps), nh = std::max(1, WH.max_taps);
 	const double W1v = WV.kind == RowKind::Copy ? 1.0 : WV.wsum_abs_max, W1h = WH.kind == RowKind::Copy ? 1.0 : WH.wsum_abs_max;
 	const double Wnv = WV.kind == RowKind::Copy ? 0.0 : WV.wsum_neg_max;
+	// roundings a horizontal product passes through: blocked sums per thread,
+	// or a lane's strided sum plus a five-step butterfly (a warp per pixel)
+	const bool hwarp = !batch && nh >= kHWarpTaps;
+	const int h_rounds = hwarp ? (nh + 31) / 32 + 5 : std::min(nh, kHBlock) + (nh + kHBlock - 1) / kHBlock;
 	for(int q = 0; q < nplanes; q++) {
 		double r_dec = keys[q].premul ? 3.0 * u : 0.0;
 		double c1 = (r_dec + 2.0 * u + gamma_n(nv + 1, u) + gamma_n(nv + 1, ud)) * 1.01;
-		double c2 = (u + gamma_n(std::min(nh, kHBlock) + (nh + kHBlock - 1) / kHBlock + 1, u) + gamma_n(nh + 1, ud)) * 1.01;
+		double c2 = (u + gamma_n(h_rounds + 1, u) + gamma_n(nh + 1, ud)) * 1.01;
 		double ed = e_dec * (keys[q].premul ? 1.0 : 1.0);
 		double K0 = (ed * W1v * W1h + 2.02 * c1 * Wnv * W1h) * 1.05;
 		double K1 = (1.01 * c1 + c2) * 1.05;
@@ -652,7 +665,7 @@ static FastState *fast_build(const Plan &P, const Job &J, bool batch, int tc_mod
 				const double ed_tc = TB.e_abs * 1.01 / std::max(W1v, 1e-300);
 				for(int q = 0; q < nplanes; q++) {
 					double c1 = (2.0 * u + gamma_n(nv + 1, ud)) * 1.01;
-					double c2 = (u + gamma_n(std::min(nh, kHBlock) + (nh + kHBlock - 1) / kHBlock + 1, u) + gamma_n(nh + 1, ud)) * 1.01;
+					double c2 = (u + gamma_n(h_rounds + 1, u) + gamma_n(nh + 1, ud)) * 1.01;
 					F.K0[q] = (float)((ed_tc * W1v * W1h + 2.02 * c1 * Wnv * W1h) * 1.05);
 					F.K1[q] = (float)((1.01 * c1 + c2) * 1.05);
 				}
@@ -661,13 +674,24 @@ static FastState *fast_build(const Plan &P, const Job &J, bool batch, int tc_mod
 		}
 	}
 	if(!FS->vkernel) { delete FS; err = "fast form: no kernel for this layout"; return nullptr; }
-	switch(nplanes) {
-	case 1: FS->hkernel = (const void *)k_hpass_fast<1>; break;
-	case 2: FS->hkernel = (const void *)k_hpass_fast<2>; break;
-	case 3: FS->hkernel = (const void *)k_hpass_fast<3>; break;
-	default: FS->hkernel = (const void *)k_hpass_fast<4>; break;
+	if(hwarp) {
+		switch(nplanes) {
+		case 1: FS->hkernel = (const void *)k_hpass_warp<1>; break;
+		case 2: FS->hkernel = (const void *)k_hpass_warp<2>; break;
+		case 3: FS->hkernel = (const void *)k_hpass_warp<3>; break;
+		default: FS->hkernel = (const void *)k_hpass_warp<4>; break;
+		}
+		FS->hgrid = dim3((F.out_w + kHThreads / 32 - 1) / (kHThreads / 32), F.out_h);
 	}
-	FS->hgrid = dim3((F.out_w + kHThreads - 1) / kHThreads, F.out_h);
+	else {
+		switch(nplanes) {
+		case 1: FS->hkernel = (const void *)k_hpass_fast<1>; break;
+		case 2: FS->hkernel = (const void *)k_hpass_fast<2>; break;
+		case 3: FS->hkernel = (const void *)k_hpass_fast<3>; break;
+		default: FS->hkernel = (const void *)k_hpass_fast<4>; break;
+		}
+		FS->hgrid = dim3((F.out_w + kHThreads - 1) / kHThreads, F.out_h);
+	}
 	F.vgx = (int)FS->vgrid.x;
 	F.vgy = (int)FS->vgrid.y;
 	F.hgx = (int)FS->hgrid.x;
@@ -806,6 +830,10 @@ void preload_fast_kernels()
 	cudaFuncGetAttributes(&a, (const void *)k_hpass_fast<2>);
 	cudaFuncGetAttributes(&a, (const void *)k_hpass_fast<3>);
 	cudaFuncGetAttributes(&a, (const void *)k_hpass_fast<4>);
+	cudaFuncGetAttributes(&a, (const void *)k_hpass_warp<1>);
+	cudaFuncGetAttributes(&a, (const void *)k_hpass_warp<2>);
+	cudaFuncGetAttributes(&a, (const void *)k_hpass_warp<3>);
+	cudaFuncGetAttributes(&a, (const void *)k_hpass_warp<4>);
 	cudaGetLastError();
 }
 

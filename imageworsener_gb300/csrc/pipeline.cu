@@ -753,7 +753,9 @@ __device__ __forceinline__ bool rounds_to_hi(dfl x, float delta)
 // The reference's float intermediates of every channel in 'mask' at (column
 // x, row j), if all are certain.  The channels share the vertical weights
 // (the fast form has one weight set per dimension), so each tap's pixel is
-// read and its alpha decoded once for all of them.
+// read and its alpha decoded once for all of them.  UNROLL: taps whose loads
+// are in flight together (register budget of the caller).
+template<int UNROLL = 4>
 __device__ __forceinline__ bool interm_df_all(const Job &J, unsigned int mask, int x, int j, float *out, int stride)
 {
 	const DWeights &W = J.wv[J.mid[0].wv];
@@ -798,7 +800,7 @@ __device__ __forceinline__ bool interm_df_all(const Job &J, unsigned int mask, i
 	else {
 		const int tb = W.off[j], te = W.off[j + 1];
 		n = te - tb;
-#pragma unroll 4
+#pragma unroll UNROLL
 		for(int t = tb; t < te; t++) {   // unrolled so that the taps' loads are in flight together
 			const int src = W.src[t];
 			if(src >= 0) add_tap(src, df_of(J.df_wv[t]), false);   // edge taps add 0
@@ -1182,7 +1184,7 @@ __global__ void __launch_bounds__(256, 1) k_fix_wide_df(Job J1, const Job *jobs,
 			const int nt = W.kind == 1 ? 1 : W.off[i + 1] - t0;
 			for(int t = threadIdx.x; t < nt; t += blockDim.x) {
 				const int src = W.src[t0 + t];
-				if(src >= 0 && !interm_df_all(J, mask, src, j, my + t, maxt)) bad = true;
+				if(src >= 0 && !interm_df_all<8>(J, mask, src, j, my + t, maxt)) bad = true;
 			}
 		}
 		bad = __syncthreads_or(bad) != 0;

@@ -222,11 +222,15 @@ __global__ void __launch_bounds__(kThreads, 2) k_vtc(const __grid_constant__ TcJ
 		}
 		// per column: the 8 rows' digits as one 16-byte core-matrix row per digit
 		unsigned char *A = sA + s * 3 * kPieceBytes;
+		// all 32 table lookups of the stage first (they are independent)
+		uint2 LL[4][8];
+#pragma unroll
+		for(int c = 0; c < 4; c++)
+#pragma unroll
+			for(int q = 0; q < 8; q++) LL[c][q] = lutq[c][__byte_perm(raw[q], 0u, 0x4440u + c)];
 #pragma unroll
 		for(int c = 0; c < 4; c++) {
-			uint2 L[8];
-#pragma unroll
-			for(int q = 0; q < 8; q++) L[q] = lutq[c][__byte_perm(raw[q], 0u, 0x4440u + c)];
+			const uint2 (&L)[8] = LL[c];
 			uint4 d2, d1, d0;
 			d2.x = __byte_perm(L[0].x, L[1].x, 0x5410); d2.y = __byte_perm(L[2].x, L[3].x, 0x5410);
 			d2.z = __byte_perm(L[4].x, L[5].x, 0x5410); d2.w = __byte_perm(L[6].x, L[7].x, 0x5410);
