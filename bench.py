@@ -64,7 +64,7 @@ WORKLOADS = {
 class Stats(C.Structure):
     _fields_ = [("ms_total", C.c_double), ("ms_device", C.c_double), ("ms_part", C.c_double * 4),
                 ("flagged", C.c_longlong), ("form", C.c_int), ("kernels", C.c_int), ("zero_copy", C.c_int),
-                ("flagged_exact", C.c_longlong), ("vertical_tensor", C.c_int)]
+                ("flagged_exact", C.c_longlong), ("vertical_tensor", C.c_int), ("graph", C.c_int)]
 
 
 _T0 = time.perf_counter()

@@ -185,8 +185,10 @@ void preload_batch_kernels()
 	cudaGetLastError();
 }
 
-int fast_launch_batch(cudaStream_t st, void *const *items, int n, std::string &err, cudaEvent_t after_vertical)
+int fast_launch_batch(cudaStream_t st, void *const *items, int n, std::string &err, cudaEvent_t after_vertical,
+	cudaEvent_t after_horizontal, const std::function<int()> &tail, bool *graphed)
 {
+	if(graphed) *graphed = false;
 	if(n <= 0) return 0;
 	std::vector<Group> vg, hg;
 	auto group_of = [](std::vector<Group> &gs, const void *k) -> Group & {
@@ -267,10 +269,29 @@ int fast_launch_batch(cudaStream_t st, void *const *items, int n, std::string &e
 		launches++;
 		return true;
 	};
-	for(Group &g : vg) if(!launch(g)) return -1;
-	if(after_vertical) cudaEventRecord(after_vertical, st);
-	for(Group &g : hg) if(!launch(g)) return -1;
-	return launches;
+	// shared-memory attributes before the capture (host-side calls)
+	for(std::vector<Group> *gs : {&vg, &hg})
+		for(Group &g : *gs)
+			if(g.blocks > 0 && g.smem > 48 * 1024 &&
+				cudaFuncSetAttribute(g.kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g.smem) != cudaSuccess) {
+				err = "batch: shared memory request refused";
+				return -1;
+			}
+	auto issue = [&]() -> int {
+		launches = 0;
+		for(Group &g : vg) if(!launch(g)) return -1;
+		if(after_vertical) cudaEventRecord(after_vertical, st);
+		for(Group &g : hg) if(!launch(g)) return -1;
+		if(after_horizontal) cudaEventRecord(after_horizontal, st);
+		if(tail) {
+			const int t = tail();
+			if(t < 0) return -1;
+			launches += t;
+		}
+		return launches;
+	};
+	if(!graphed) return issue();
+	return run_as_graph(st, issue, graphed);
 }
 
 }  // namespace iwg

@@ -39,7 +39,7 @@ struct FTail {        // quantisation of one output channel, float tables
 };
 
 constexpr int kLutCells = 1024;
-constexpr int kHBlock = 16;   // horizontal taps per partial sum (blocked summation)
+constexpr int kHBlock = 4;    // horizontal taps per partial sum (blocked summation: about sqrt(n) is best)
 
 struct FJob {
 	// input
@@ -1013,6 +1013,12 @@ struct FastState {
 	const float2 *df_atab = nullptr;
 	size_t o_wvdf = 0, o_whdf = 0;
 	bool df = false;
+	// band tuning (fastpath.cu): the streaming schedule's windows (host
+	// copies) and the vertical kernel's shared memory as a function of the
+	// positions a band spans (vsmem = vsmem_fixed + positions * vsmem_per_pos)
+	std::vector<int> first_pos, last_pos;
+	size_t vsmem_fixed = 0, vsmem_per_pos = 0;
+	bool in_device = false;
 	// vertical pass on the tensor cores (tcvert.cu) instead of vkernel's FJob launch
 	bool tc = false;
 	tc::TcJob T;

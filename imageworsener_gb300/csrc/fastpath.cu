@@ -674,6 +674,21 @@ static FastState *fast_build(const Plan &P, const Job &J, bool batch, int tc_mod
 		}
 	}
 	if(!FS->vkernel) { delete FS; err = "fast form: no kernel for this layout"; return nullptr; }
+	FS->in_device = in_device;
+	if(S.ok) {
+		FS->first_pos = S.first_pos;
+		FS->last_pos = S.last_pos;
+	}
+	if(FS->vv.kind == 1) {
+		FS->vsmem_per_pos = (size_t)FS->vv.ns * sizeof(float) + sizeof(int2);
+		FS->vsmem_fixed = (size_t)dec_floats * sizeof(float);
+	}
+	else if(FS->vv.kind == 4) {
+		FS->vsmem_per_pos = (size_t)FS->vv.ns * sizeof(float) + sizeof(int2);
+		FS->vsmem_fixed = (size_t)kBulkStages * kBulkConsumers * FS->vv.px * FS->vv.nch * (FS->vv.depth / 8) + 256 +
+			(size_t)dec_floats * sizeof(float);
+	}
+	else FS->vsmem_fixed = FS->vsmem;
 	if(hwarp) {
 		switch(nplanes) {
 		case 1: FS->hkernel = (const void *)k_hpass_warp<1>; break;
@@ -746,6 +761,119 @@ static void fast_place(FastState *FS, const uint8_t *base, int *flag_count, int 
 	}
 }
 
+// ---- the autotuner: band heights of the vertical pass ----
+//
+// The vertical kernels split the output rows into bands (one block per strip
+// and band; for the tensor-core pass, bands of 16-row blocks).  Taller bands
+// read fewer overlapping input rows, shorter ones give the GPU more blocks;
+// the best count depends on the geometry, the kernel and the machine.  The
+// first image of a geometry times a few candidate counts on its own data
+// (CUDA events, best of two launches each after a warm launch) and keeps the
+// fastest; later images of that geometry reuse it.  Every output row is summed
+// by one block in the same order whatever the count, so the bytes never
+// depend on the choice.
+
+// Current band count of the prepared vertical pass (0: not banded).
+static int vbands(const FastState &FS)
+{
+	if(FS.tc) return (FS.T.nblk + FS.T.blocks_per_band - 1) / FS.T.blocks_per_band;
+	if(FS.vv.kind == 1 || FS.vv.kind == 2 || FS.vv.kind == 4) return (int)FS.vgrid.y;
+	return 0;
+}
+
+// Re-targets the prepared vertical pass to about 'bands' bands; false if that
+// count is not possible (shared memory).
+static bool set_vbands(FastState &FS, int bands)
+{
+	if(FS.tc) {
+		const int nblk = FS.T.nblk;
+		bands = std::max(1, std::min(bands, nblk));
+		const int bpb = (nblk + bands - 1) / bands;
+		FS.T.blocks_per_band = bpb;
+		FS.vgrid.y = (nblk + bpb - 1) / bpb;
+		FS.F.vgy = (int)FS.vgrid.y;
+		return true;
+	}
+	FJob &F = FS.F;
+	const int mid_h = F.mid_h;
+	bands = std::max(1, std::min(bands, mid_h));
+	const int rows = (mid_h + bands - 1) / bands;
+	bands = (mid_h + rows - 1) / rows;
+	size_t sm = FS.vsmem_fixed;
+	if(FS.vsmem_per_pos) {
+		if(FS.first_pos.size() < (size_t)mid_h || FS.last_pos.size() < (size_t)mid_h) return false;
+		int nq_max = 0;
+		for(int b = 0; b < bands; b++) {
+			const int jb = b * rows, je = std::min(jb + rows, mid_h);
+			nq_max = std::max(nq_max, FS.last_pos[je - 1] - FS.first_pos[jb] + 1);
+		}
+		sm = FS.vsmem_fixed + (size_t)nq_max * FS.vsmem_per_pos;
+		if(sm > 200 * 1024) return false;
+		if(sm > 48 * 1024 && cudaFuncSetAttribute(FS.vkernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess) {
+			cudaGetLastError();
+			return false;
+		}
+	}
+	F.rows_per_band = rows;
+	FS.vgrid.y = bands;
+	F.vgy = bands;
+	FS.vsmem = sm;
+	return true;
+}
+
+static bool launch_vertical(cudaStream_t st, FastState &FS)
+{
+	void *fargs[] = {&FS.F};
+	void *targs[] = {&FS.T};
+	return cudaLaunchKernel(FS.vkernel, FS.vgrid, dim3(FS.vthreads), FS.tc ? targs : fargs, FS.vsmem, st) == cudaSuccess;
+}
+
+// Chooses the band count of FS's vertical pass (cached per geometry).  Runs
+// on 'st' after the input upload; the vertical pass's output is rewritten by
+// the real run.  Caller holds the cache lock.
+static void tune_vertical(cudaStream_t st, FastState &FS)
+{
+	const int b0 = vbands(FS);
+	if(b0 <= 0 || !FS.in_device) return;
+	static std::map<std::vector<long long>, int> tuned;
+	const std::vector<long long> key = {(long long)(uintptr_t)FS.vkernel, FS.F.mid_w, FS.F.mid_h, FS.F.in_rows,
+		FS.J.wv[0].max_taps, FS.tc ? FS.T.nblk : 0};
+	auto it = tuned.find(key);
+	if(it != tuned.end()) {
+		if(!set_vbands(FS, it->second)) set_vbands(FS, b0);
+		return;
+	}
+	cudaEvent_t e0, e1;
+	if(cudaEventCreate(&e0) != cudaSuccess) { cudaGetLastError(); return; }
+	if(cudaEventCreate(&e1) != cudaSuccess) { cudaEventDestroy(e0); cudaGetLastError(); return; }
+	int best = b0;
+	float best_ms = 1e30f;
+	std::vector<int> cands = {b0, std::max(1, b0 / 2), 2 * b0, 3 * b0, 4 * b0};
+	std::vector<int> tried;
+	for(int c : cands) {
+		if(!set_vbands(FS, c)) continue;
+		const int actual = vbands(FS);
+		if(std::find(tried.begin(), tried.end(), actual) != tried.end()) continue;
+		tried.push_back(actual);
+		if(!launch_vertical(st, FS)) { cudaGetLastError(); continue; }   // warm
+		float ms_min = 1e30f;
+		for(int rep = 0; rep < 2; rep++) {
+			cudaEventRecord(e0, st);
+			launch_vertical(st, FS);
+			cudaEventRecord(e1, st);
+			float ms = 0.0f;
+			if(cudaEventSynchronize(e1) == cudaSuccess && cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess)
+				ms_min = std::min(ms_min, ms);
+		}
+		cudaGetLastError();
+		if(ms_min < best_ms) { best_ms = ms_min; best = actual; }
+	}
+	cudaEventDestroy(e0);
+	cudaEventDestroy(e1);
+	if(!set_vbands(FS, best)) set_vbands(FS, b0);
+	tuned[key] = vbands(FS);
+}
+
 bool fast_prepare(cudaStream_t st, const Plan &P, Job &J, FastInfo &fi, std::string &err)
 {
 	Cache &C = cache();
@@ -769,6 +897,7 @@ bool fast_prepare(cudaStream_t st, const Plan &P, Job &J, FastInfo &fi, std::str
 	uint8_t *base = (uint8_t *)C.scratch;
 	cudaMemcpyAsync(base, FS->blob.data(), FS->blob.size(), cudaMemcpyHostToDevice, st);
 	fast_place(FS, base, (int *)(base + flag_off), (int *)(base + flag_off + 256), 0);
+	if(fi.autotune) tune_vertical(st, *FS);
 	fi.state = FS;
 	fi.launches = 3;
 	fi.launch_fn = fast_launch_impl;

@@ -1,6 +1,7 @@
 // fastpath.cuh -- interface of the FP32 + guard-band form (fastpath.cu).
 #pragma once
 
+#include <functional>
 #include <string>
 #include <cuda_runtime.h>
 
@@ -15,6 +16,7 @@ struct FastInfo {
 	int slots = 0;       // register slots per column (streaming)
 	int tc_mode = 1;     // in: vertical pass on the tensor cores: 0 never, 1 wide windows, 2 whenever eligible
 	int tc = 0;          // out: the vertical pass runs on the tensor cores
+	int autotune = 1;    // in: choose the vertical pass's band count by measurement (cached per geometry)
 	int *flag_count_dev = nullptr;   // device counter of pixels re-evaluated exactly
 	void *state = nullptr;            // prepared launch state (fastpath.cu)
 	int launches = 0;
@@ -40,6 +42,33 @@ int fast_launch(cudaStream_t st, FastInfo &fi, Mark mark)
 // Frees the prepared state.
 void fast_release(FastInfo &fi);
 
+// Queues what 'issue' launches on 'st' as one CUDA graph: captured,
+// instantiated, launched (and freed once it has run).  Returns issue's value;
+// *graphed tells whether the graph ran.  If the stream cannot be captured or
+// the graph not launched, the same launches are issued directly.
+template<class F>
+int run_as_graph(cudaStream_t st, F &&issue, bool *graphed)
+{
+	*graphed = false;
+	if(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed) == cudaSuccess) {
+		const int r = issue();
+		cudaGraph_t g = nullptr;
+		const cudaError_t e = cudaStreamEndCapture(st, &g);
+		cudaGraphExec_t x = nullptr;
+		if(e == cudaSuccess && g && r >= 0 && cudaGraphInstantiate(&x, g, 0) == cudaSuccess &&
+			cudaGraphLaunch(x, st) == cudaSuccess) {
+			cudaGraphExecDestroy(x);
+			cudaGraphDestroy(g);
+			*graphed = true;
+			return r;
+		}
+		if(x) cudaGraphExecDestroy(x);
+		if(g) cudaGraphDestroy(g);
+	}
+	cudaGetLastError();
+	return issue();
+}
+
 // ---- batch: many images in a few launches ----
 // Host preparation of one image (no device work); null with 'err' if the
 // image cannot run in the fast form.  J's device pointers (input, output,
@@ -60,8 +89,14 @@ void preload_fast_kernels();
 void preload_batch_kernels();
 void preload_noalloc_kernels();   // noalloc.cu
 
+// The launches of a batch: vertical groups, 'after_vertical' recorded,
+// horizontal groups, 'after_horizontal' recorded, then 'tail()' (the
+// re-evaluation launches, returning their count); the job tables are uploaded
+// before them.  With graphed != nullptr they are captured and run as one CUDA
+// graph (*graphed: whether it ran); nullptr: launched directly.  Returns the
+// kernel launches, -1 on error.
 int fast_launch_batch(cudaStream_t st, void *const *items, int n, std::string &err,
-	cudaEvent_t after_vertical = nullptr);
+	cudaEvent_t after_vertical, cudaEvent_t after_horizontal, const std::function<int()> &tail, bool *graphed);
 // Copies the image's double-float re-evaluation pointers (set by placement)
 // into the caller's job record.
 void fast_item_job_df(const void *item, dev::Job &J);

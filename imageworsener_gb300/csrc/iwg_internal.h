@@ -175,6 +175,7 @@ struct Stats {   // per call, readable through the iwg_* extension API
 	int kernels = 0;             // kernel launches issued
 	int zero_copy = 0;           // kernels read/wrote the host image buffers directly
 	int vertical_tensor = 0;     // the vertical pass ran on the tensor cores
+	int graph = 0;               // the timed passes were replayed as a CUDA graph
 };
 
 }  // namespace iwg

@@ -1878,6 +1878,8 @@ bool run_pipeline(iw_context *ctx, Plan &P, int warmup, int iters, int lane)
 	{
 		const char *vt = get_option(ctx, "gpu:vertical");
 		fi.tc_mode = (vt && !strcmp(vt, "cuda")) ? 0 : ((vt && !strcmp(vt, "tensor")) ? 2 : 1);
+		const char *at = get_option(ctx, "gpu:autotune");
+		fi.autotune = !(at && !strcmp(at, "off"));
 	}
 	bool fast = !want_plain && fast_eligible(P, J, fi);
 	ctx->stats.form = fast ? 1 : 0;
@@ -1910,6 +1912,41 @@ bool run_pipeline(iw_context *ctx, Plan &P, int warmup, int iters, int lane)
 		else l = plain_launch(st, P, J, [&]() { mark(timed); });
 		if(timed) marks_per_it = (int)(ev.size() - before);
 		launches = l;
+	}
+	// Repeated passes of a resident image (the timed entry point): the fast
+	// form's launches captured once as a CUDA graph and replayed nt times
+	// between two events; that mean is the device time per pass.  The
+	// per-launch breakdown comes from the directly launched passes above.
+	float graph_ms = -1.0f;
+	ctx->stats.graph = 0;
+	if(fast && nt > 1) {
+		cudaGraph_t g = nullptr;
+		cudaGraphExec_t gx = nullptr;
+		if(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed) == cudaSuccess) {
+			fast_launch(st, fi, []() {});
+			if(cudaStreamEndCapture(st, &g) != cudaSuccess || !g || cudaGraphInstantiate(&gx, g, 0) != cudaSuccess) gx = nullptr;
+		}
+		cudaGetLastError();
+		if(gx) {
+			cudaEvent_t ga, gb;
+			cudaEventCreate(&ga);
+			cudaEventCreate(&gb);
+			cudaGraphLaunch(gx, st);   // warm-up replay
+			cudaEventRecord(ga, st);
+			bool ok = true;
+			for(int it = 0; it < nt && ok; it++) ok = cudaGraphLaunch(gx, st) == cudaSuccess;
+			cudaEventRecord(gb, st);
+			if(ok && cudaEventSynchronize(gb) == cudaSuccess && cudaEventElapsedTime(&graph_ms, ga, gb) == cudaSuccess) {
+				graph_ms /= (float)nt;
+				ctx->stats.graph = 1;
+			}
+			else graph_ms = -1.0f;
+			cudaEventDestroy(ga);
+			cudaEventDestroy(gb);
+			cudaGraphExecDestroy(gx);
+		}
+		if(g) cudaGraphDestroy(g);
+		cudaGetLastError();
 	}
 	if(S.lane != 0) wait_stream(st, true);   // downloads queued once the kernels are done (as for batches)
 	if(upmode == UP_COPY) cudaMemcpyAsync(ctx->img2.pixels, S.out.p, out_bytes, cudaMemcpyDeviceToHost, st);
@@ -1950,7 +1987,7 @@ bool run_pipeline(iw_context *ctx, Plan &P, int warmup, int iters, int lane)
 		iw_set_errorf(ctx, "CUDA error: %s", cudaGetErrorString(ce));
 		return false;
 	}
-	ctx->stats.ms_device = total_ms / nt;
+	ctx->stats.ms_device = graph_ms > 0.0f ? (double)graph_ms : total_ms / nt;
 	for(int k = 0; k < 4; k++) ctx->stats.ms_part[k] = part[k] / nt;
 	ctx->stats.kernels = launches;
 	return true;
@@ -2143,13 +2180,17 @@ bool run_batch(const std::vector<iw_context *> &ctxs, const std::vector<Plan *> 
 	cudaEventCreate(&ev_f);
 	cudaEventRecord(e0, st);
 	pt.mark(1);
-	int launches = fast_launch_batch(st, items.data(), m, err, ev_h);
-	cudaEventRecord(ev_f, st);
-	pt.mark(2);
-	if(launches >= 0) {
-		launches += launch_fix_flagged_batch(st, (const Job *)(tbase + o_jobs), maxt, flag_count, flag_list,
+	// vertical and horizontal groups, then the re-evaluation, launched
+	// directly.  (Captured as one CUDA graph, the same launches gave correct
+	// output for this batch but wrong output for the plain-form batch run on
+	// the lane right after it; the cause was not found, so batches do not use
+	// graphs.)
+	const bool graphed = false;
+	int launches = fast_launch_batch(st, items.data(), m, err, ev_h, ev_f, [&]() {
+		return launch_fix_flagged_batch(st, (const Job *)(tbase + o_jobs), maxt, flag_count, flag_list,
 			(int)std::min<size_t>(nflag, 0x7fffffff));
-	}
+	}, nullptr);
+	pt.mark(2);
 	cudaEventRecord(e1, st);
 	pt.mark(3);
 	if(upmode == UP_COPY)
@@ -2195,6 +2236,7 @@ bool run_batch(const std::vector<iw_context *> &ctxs, const std::vector<Plan *> 
 	for(int k = 0; k < m; k++) {
 		iw_context *ctx = ctxs[item_img[k]];
 		ctx->stats.form = 1;
+		ctx->stats.graph = graphed ? 1 : 0;
 		ctx->stats.zero_copy = zc;
 		ctx->stats.kernels = launches;
 		ctx->stats.ms_device = ms;
@@ -2480,6 +2522,7 @@ extern "C" int iwg_get_stats(struct iw_context *ctx, struct iwg_stats *out)
 	out->zero_copy = ctx->stats.zero_copy;
 	out->flagged_exact = ctx->stats.flagged_exact;
 	out->vertical_tensor = ctx->stats.vertical_tensor;
+	out->graph = ctx->stats.graph;
 	return 1;
 }
 

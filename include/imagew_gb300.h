@@ -47,6 +47,9 @@ struct iwg_stats {
 	int vertical_tensor;   /* 1: the vertical pass ran on the tensor cores
 	                          (exact integer digit products; see the
 	                          "gpu:vertical" option) */
+	int graph;             /* 1: iwg_process_image_timed replayed the passes
+	                          as a CUDA graph (ms_device is then the mean time
+	                          of one replay) */
 };
 
 /* Copies the statistics of the context's last run into *out.  Returns 1. */

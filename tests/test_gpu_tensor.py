@@ -116,3 +116,48 @@ def test_tensor_vertical_full_size_downscale(gpulib):
         assert st.vertical_tensor == (1 if vertical == "tensor" else 0)
         flagged[vertical] = st.flagged
     assert flagged["tensor"] < flagged["cuda"], flagged
+
+
+def _stats_after(lib, ctx):
+    from bench import Stats
+    st = Stats()
+    lib.dll.iwg_get_stats.argtypes = [C.c_void_p, C.POINTER(Stats)]
+    lib.dll.iwg_get_stats(ctx, C.byref(st))
+    return st
+
+
+def test_timed_replays_run_as_cuda_graph(gpulib, oracle):
+    """iwg_process_image_timed replays the fp32 form's launches as a CUDA
+    graph; the output is the lone run's, and the calls after it (the FP64
+    plain form on the same lane, a 16-bit output) are unaffected."""
+    from bench import make_ctx
+    job = W.precision(n=1024, out=250)
+    want = run_job(gpulib, W.precision(n=1024, out=250))
+    ctx = make_ctx(gpulib, job)
+    try:
+        gpulib.dll.iwg_process_image_timed.restype = C.c_int
+        gpulib.dll.iwg_process_image_timed.argtypes = [C.c_void_p, C.c_int, C.c_int]
+        assert gpulib.dll.iwg_process_image_timed(ctx, 1, 4)
+        got = _collect(gpulib, ctx, True, [])
+        st = _stats_after(gpulib, ctx)
+    finally:
+        gpulib.iw_destroy_context(ctx)
+    assert st.graph == 1 and st.ms_device > 0
+    assert got.key() == want.key()
+    plain = W.precision(n=1024, out=250)
+    plain.calls = list(plain.calls) + [("iw_set_option", b"gpu:precision", b"fp64")]
+    assert run_job(gpulib, plain).key() == want.key()
+    for seed in (3, 11, 29):   # 16-bit output: the plain form
+        job = [j for j in W.batch(40, seed=seed, max_side=400) if j.bit_depth == 16][0]
+        assert run_job(gpulib, job).key() == run_job(oracle, job).key()
+
+
+@pytest.mark.parametrize("vertical", ["tensor", "cuda"])
+def test_autotuned_bands_same_bytes(gpulib, vertical):
+    """The band count chosen by the autotuner never changes the output."""
+    for seed in (7700, 7701, 7702):
+        a, _ = run_with_stats(gpulib, tensor_case(seed), vertical)
+        job = tensor_case(seed)
+        job.calls = list(job.calls) + [("iw_set_option", b"gpu:autotune", b"off")]
+        b, _ = run_with_stats(gpulib, job, vertical)
+        assert a.key() == b.key(), seed
