@@ -636,7 +636,7 @@ static FastState *fast_build(const Plan &P, const Job &J, bool batch, int tc_mod
 				sms = 152;
 			cudaGetLastError();
 			const size_t tsm = tc::tc_smem_bytes(nplanes);
-			const bool tvec = v_base % 4 == 0 && P.in_bpr % 4 == 0;
+			const bool tvec = v_base % 2 == 0 && P.in_bpr % 2 == 0;
 			const void *tk = tc::tc_kernel(tvec);
 			int strips = 0, bands = 0, bpb = 0;
 			tc::tc_geometry(TB, J.mid_w * nplanes, sms, strips, bands, bpb);

@@ -1182,6 +1182,24 @@ __global__ void __launch_bounds__(256, 1) k_fix_wide_df(Job J1, const Job *jobs,
 			const DWeights &W = J.wh[J.mid[0].wh];
 			const int t0 = W.kind == 1 ? i : W.off[i];
 			const int nt = W.kind == 1 ? 1 : W.off[i + 1] - t0;
+			// start the pixel's input window towards L2 (the walk below is a
+			// chain of dependent loads: sample -> decode table): each thread
+			// its column of every vertical tap's row (identity orientation,
+			// byte samples; a hint only)
+			if(J.orient == 0 && J.in_depth >= 8) {
+				const DWeights &V = J.wv[J.mid[0].wv];
+				const int vb = V.kind == 1 ? j : V.off[j], vn = V.kind == 1 ? 1 : V.off[j + 1] - vb;
+				const unsigned long long bpp = (unsigned long long)J.in_nphys * (J.in_depth / 8);
+				for(int t = threadIdx.x; t < nt; t += blockDim.x) {
+					const int src = W.src[t0 + t];
+					if(src < 0) continue;
+					const uint8_t *colp = J.in + (unsigned long long)(J.crop_x + src) * bpp;
+					for(int r = 0; r < vn; r++) {
+						const int sv = V.src[vb + r];
+						if(sv >= 0) asm volatile("prefetch.global.L2 [%0];" ::"l"(colp + (unsigned long long)(J.crop_y + sv) * J.in_bpr));
+					}
+				}
+			}
 			for(int t = threadIdx.x; t < nt; t += blockDim.x) {
 				const int src = W.src[t0 + t];
 				if(src >= 0 && !interm_df_all<8>(J, mask, src, j, my + t, maxt)) bad = true;

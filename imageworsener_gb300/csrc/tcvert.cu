@@ -96,14 +96,25 @@ __device__ __forceinline__ void tmem_ld16(unsigned taddr, uint32_t (&v)[16])
 		:: "memory");
 }
 
+__device__ __forceinline__ void tmem_ld8(unsigned taddr, uint32_t (&v)[8])
+{
+	asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+		: "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7])
+		: "r"(taddr) : "memory");
+	asm volatile("tcgen05.wait::ld.sync.aligned;"
+		: "+r"(v[0]), "+r"(v[1]), "+r"(v[2]), "+r"(v[3]), "+r"(v[4]), "+r"(v[5]), "+r"(v[6]), "+r"(v[7])
+		:: "memory");
+}
+
 // ---------------------------------------------------------------------------
 // kernel
 // ---------------------------------------------------------------------------
 
-// This thread's input words for one stage: its 4 byte columns (from cbase)
-// in the 8 input rows from row0 (rows past the crop repeat the last row;
-// their weights are zero).  Columns past the image read as code 0 (their
-// results are never stored).  VEC: the columns' 4 bytes are one aligned word.
+// This thread's codes for one stage: its 2 byte columns (from cbase) in the
+// 8 input rows from row0, one row per element (column cbase in bits 0-7,
+// cbase + 1 in bits 8-15; rows past the crop repeat the last row, their
+// weights are zero).  Columns past the image read as code 0 (their results
+// are never stored).  VEC: the two bytes are one aligned 16-bit word.
 template<bool VEC>
 __device__ __forceinline__ void load_words(uint32_t (&raw)[8], const TcJob &T, int cbase, bool full, int row0)
 {
@@ -112,48 +123,52 @@ __device__ __forceinline__ void load_words(uint32_t (&raw)[8], const TcJob &T, i
 #pragma unroll
 	for(int r = 0; r < 8; r++) {
 		const uint8_t *p = base + (unsigned long long)min(row0 + r, last) * T.in_bpr;
-		if(VEC && full) raw[r] = __ldg(reinterpret_cast<const uint32_t *>(p));
+		if(VEC && full) raw[r] = __ldg(reinterpret_cast<const unsigned short *>(p));
 		else {
 			uint32_t w = 0;
 #pragma unroll
-			for(int c = 0; c < 4; c++)
+			for(int c = 0; c < 2; c++)
 				if(cbase + c < T.cols) w |= (uint32_t)__ldg(p + c) << (8 * c);
 			raw[r] = w;
 		}
 	}
 }
 
-// This thread's share of a stage's two weight tiles (2 * 3072 bytes = 384 x 16 bytes).
-__device__ __forceinline__ void load_tiles(uint4 (&bt)[3], const uint4 *tiles, int stage, int tid)
+// This thread's share of a stage's two weight tiles (2 * 3072 bytes = 384 x
+// 16 bytes): pieces tid and tid + 256 (the second for tid < 128 only).
+constexpr int kTilePieces = 2 * kTileBytes / 16;
+__device__ __forceinline__ void load_tiles(uint4 (&bt)[2], const uint4 *tiles, int stage, int tid)
 {
-	const uint4 *g = tiles + (size_t)stage * (2 * kTileBytes / 16);
-#pragma unroll
-	for(int q = 0; q < 3; q++) bt[q] = __ldg(g + tid + q * kThreads);
+	const uint4 *g = tiles + (size_t)stage * kTilePieces;
+	bt[0] = __ldg(g + tid);
+	bt[1] = tid + kThreads < kTilePieces ? __ldg(g + tid + kThreads) : make_uint4(0, 0, 0, 0);
 }
 
-// Digit-product sums of block b -> float intermediate (16 output rows of this
-// thread's column).  Columns 0..127 of the block's TMEM region hold
-// X2*(W2,W1,W0), X1*(W2,W1,W0), X0*(W2,W1), 16 rows each; the weights of the
-// digit products are 2^(8*(i+j)) with the digits' positions i, j.
+// Digit-product sums of block b -> float intermediate: this thread's byte
+// column (TMEM lane) and output rows 8h..8h+7 of the block (h = warp / 4;
+// warps w and w + 4 share lanes 32(w % 4)..).  Columns 0..127 of the block's
+// TMEM region hold X2*(W2,W1,W0), X1*(W2,W1,W0), X0*(W2,W1), 16 rows each;
+// the weights of the digit products are 2^(8*(i+j)) with the digits' positions i, j.
 __device__ __forceinline__ void write_block(const TcJob &T, unsigned tmem, int b, int warp, int col, bool colok, int ch)
 {
-	const unsigned base = tmem + ((unsigned)(warp * 32) << 16) + (unsigned)(b & 1) * 128u;
-	long long acc[kR];
+	const int h = warp >> 2;
+	const unsigned base = tmem + ((unsigned)((warp & 3) * 32) << 16) + (unsigned)(b & 1) * 128u + (unsigned)h * 8u;
+	long long acc[8];
 #pragma unroll
-	for(int r = 0; r < kR; r++) acc[r] = 0;
+	for(int r = 0; r < 8; r++) acc[r] = 0;
 #pragma unroll
 	for(int q = 0; q < 8; q++) {
-		uint32_t v[16];
-		tmem_ld16(base + q * 16, v);
+		uint32_t v[8];
+		tmem_ld8(base + q * 16, v);
 		const int sh = q == 0 ? 32 : ((q == 1 || q == 3) ? 24 : ((q == 5 || q == 7) ? 8 : 16));
 #pragma unroll
-		for(int r = 0; r < kR; r++) acc[r] += (long long)__float2int_rz(__uint_as_float(v[r])) * (1LL << sh);
+		for(int r = 0; r < 8; r++) acc[r] += (long long)__float2int_rz(__uint_as_float(v[r])) * (1LL << sh);
 	}
 	if(!colok) return;
 	float *o = T.interm + (unsigned long long)ch * T.plane + col / T.nphys;
 #pragma unroll
-	for(int r = 0; r < kR; r++) {
-		const int j = b * kR + r;
+	for(int r = 0; r < 8; r++) {
+		const int j = b * kR + h * 8 + r;
 		if(j < T.mid_h) o[(unsigned long long)j * T.mid_w] = __fmul_rn(__ll2float_rn(acc[r]), T.scale);
 	}
 }
@@ -164,8 +179,11 @@ __global__ void __launch_bounds__(kThreads, 2) k_vtc(const __grid_constant__ TcJ
 	extern __shared__ __align__(128) unsigned char smem[];
 	unsigned char *sA = smem;                                   // kStages x 3 digits x kPieceBytes
 	unsigned char *sB = sA + kStages * 3 * kPieceBytes;         // kStages x 2 tiles x kTileBytes
-	uint2 *sLut = reinterpret_cast<uint2 *>(sB + kStages * 2 * kTileBytes);
-	unsigned long long *bar = reinterpret_cast<unsigned long long *>(sLut + T.nphys * 256);
+	// digit table split in two so that nearby codes fall on different banks
+	// (or share a word): X2 | X1 << 16 (4 bytes), X0 (2 bytes)
+	uint32_t *sLutHi = reinterpret_cast<uint32_t *>(sB + kStages * 2 * kTileBytes);
+	unsigned short *sLutLo = reinterpret_cast<unsigned short *>(sLutHi + T.nphys * 256);
+	unsigned long long *bar = reinterpret_cast<unsigned long long *>(sLutLo + T.nphys * 256);
 	unsigned *s_tmem = reinterpret_cast<unsigned *>(bar + kStages);
 	int *s_abort = reinterpret_cast<int *>(s_tmem + 1);
 
@@ -174,7 +192,11 @@ __global__ void __launch_bounds__(kThreads, 2) k_vtc(const __grid_constant__ TcJ
 	const int b1 = min(b0 + T.blocks_per_band, T.nblk);
 	if(b0 >= b1) return;                                        // whole block, before any allocation
 
-	for(int k = tid; k < T.nphys * 256; k += kThreads) sLut[k] = T.lut[k];
+	for(int k = tid; k < T.nphys * 256; k += kThreads) {
+		const uint2 e = T.lut[k];
+		sLutHi[k] = e.x;
+		sLutLo[k] = (unsigned short)e.y;
+	}
 	if(tid == 0) {
 		for(int s = 0; s < kStages; s++) bar_init(bar + s, 1);
 		*s_abort = 0;
@@ -186,23 +208,27 @@ __global__ void __launch_bounds__(kThreads, 2) k_vtc(const __grid_constant__ TcJ
 	tc_fence_after();
 	const unsigned tmem = *s_tmem;
 
-	// epilogue: thread tid owns TMEM lane tid = byte column col
-	const int col = blockIdx.x * kM + tid;
+	// epilogue: thread tid owns TMEM lane 32 (warp % 4) + lane = byte column col
+	const int col = blockIdx.x * kM + (warp & 3) * 32 + (tid & 31);
 	const bool colok = col < T.cols;
 	const int ch = colok ? col % T.nphys : 0;
-	// decode: warp w takes rows 8w..8w+7 of each stage, lane l the 4 byte
-	// columns 4l..4l+3 of the strip (one 128-byte line per row and warp)
+	// decode: warp w takes rows 8(w / 2)..+7 of each stage and the 64 byte
+	// columns (w % 2) * 64.. of the strip, lane l two of them (one 64-byte
+	// segment per row and warp); each (column, 8 rows) is one 16-byte
+	// core-matrix row per digit
 	const int lane = tid & 31;
-	const int cbase = blockIdx.x * kM + lane * 4;
-	const bool full = cbase + 3 < T.cols;
-	const uint2 *lutq[4];
+	const int rg = warp >> 1;
+	const int m0 = (warp & 1) * 64 + lane * 2;          // first of the thread's columns in the strip
+	const int cbase = blockIdx.x * kM + m0;
+	const bool full = cbase + 1 < T.cols;
+	int lofs[2];
 #pragma unroll
-	for(int c = 0; c < 4; c++) lutq[c] = sLut + ((cbase + c) % T.nphys) * 256;
+	for(int c = 0; c < 2; c++) lofs[c] = ((cbase + c) % T.nphys) * 256;
 	const int t0 = T.blk[b0].x, t1 = T.blk[b1 - 1].y;
 
 	uint32_t raw[8];
-	uint4 bt[3];
-	load_words<VEC>(raw, T, cbase, full, t0 * kRows + warp * 8);
+	uint4 bt[2];
+	load_words<VEC>(raw, T, cbase, full, t0 * kRows + rg * 8);
 	load_tiles(bt, T.tiles, t0, tid);
 	int done_b = b0;       // first block of the band not yet written out
 	int issued = -1;       // last stage whose operations were committed
@@ -210,9 +236,9 @@ __global__ void __launch_bounds__(kThreads, 2) k_vtc(const __grid_constant__ TcJ
 	for(int t = t0; t < t1; t++) {
 		const int i = t - t0, s = i % kStages, use = i / kStages;
 		uint32_t nraw[8];
-		uint4 nbt[3];
+		uint4 nbt[2];
 		if(t + 1 < t1) {
-			load_words<VEC>(nraw, T, cbase, full, (t + 1) * kRows + warp * 8);
+			load_words<VEC>(nraw, T, cbase, full, (t + 1) * kRows + rg * 8);
 			load_tiles(nbt, T.tiles, t + 1, tid);
 		}
 		// the stage buffer is free once the MMAs that read it (kStages stages ago) are done
@@ -220,33 +246,35 @@ __global__ void __launch_bounds__(kThreads, 2) k_vtc(const __grid_constant__ TcJ
 			atomicExch(T.err_flag, 1);
 			*(volatile int *)s_abort = 1;
 		}
-		// per column: the 8 rows' digits as one 16-byte core-matrix row per digit
+		// per column: the 8 rows' digits as one core-matrix row (16 bytes) per digit
 		unsigned char *A = sA + s * 3 * kPieceBytes;
-		// all 32 table lookups of the stage first (they are independent)
-		uint2 LL[4][8];
+		uint32_t hi[2][8], lo[2][8];   // all 32 table lookups of the stage first (independent)
 #pragma unroll
-		for(int c = 0; c < 4; c++)
+		for(int c = 0; c < 2; c++)
 #pragma unroll
-			for(int q = 0; q < 8; q++) LL[c][q] = lutq[c][__byte_perm(raw[q], 0u, 0x4440u + c)];
+			for(int q = 0; q < 8; q++) {
+				const int code = lofs[c] + (int)__byte_perm(raw[q], 0u, 0x4440u + c);
+				hi[c][q] = sLutHi[code];
+				lo[c][q] = sLutLo[code];
+			}
 #pragma unroll
-		for(int c = 0; c < 4; c++) {
-			const uint2 (&L)[8] = LL[c];
+		for(int c = 0; c < 2; c++) {
 			uint4 d2, d1, d0;
-			d2.x = __byte_perm(L[0].x, L[1].x, 0x5410); d2.y = __byte_perm(L[2].x, L[3].x, 0x5410);
-			d2.z = __byte_perm(L[4].x, L[5].x, 0x5410); d2.w = __byte_perm(L[6].x, L[7].x, 0x5410);
-			d1.x = __byte_perm(L[0].x, L[1].x, 0x7632); d1.y = __byte_perm(L[2].x, L[3].x, 0x7632);
-			d1.z = __byte_perm(L[4].x, L[5].x, 0x7632); d1.w = __byte_perm(L[6].x, L[7].x, 0x7632);
-			d0.x = __byte_perm(L[0].y, L[1].y, 0x5410); d0.y = __byte_perm(L[2].y, L[3].y, 0x5410);
-			d0.z = __byte_perm(L[4].y, L[5].y, 0x5410); d0.w = __byte_perm(L[6].y, L[7].y, 0x5410);
-			const int m = lane * 4 + c;
-			const int off = (m >> 3) * kSboA + warp * 128 + (m & 7) * 16;
+			d2.x = __byte_perm(hi[c][0], hi[c][1], 0x5410); d2.y = __byte_perm(hi[c][2], hi[c][3], 0x5410);
+			d2.z = __byte_perm(hi[c][4], hi[c][5], 0x5410); d2.w = __byte_perm(hi[c][6], hi[c][7], 0x5410);
+			d1.x = __byte_perm(hi[c][0], hi[c][1], 0x7632); d1.y = __byte_perm(hi[c][2], hi[c][3], 0x7632);
+			d1.z = __byte_perm(hi[c][4], hi[c][5], 0x7632); d1.w = __byte_perm(hi[c][6], hi[c][7], 0x7632);
+			d0.x = __byte_perm(lo[c][0], lo[c][1], 0x5410); d0.y = __byte_perm(lo[c][2], lo[c][3], 0x5410);
+			d0.z = __byte_perm(lo[c][4], lo[c][5], 0x5410); d0.w = __byte_perm(lo[c][6], lo[c][7], 0x5410);
+			const int m = m0 + c;
+			const int off = (m >> 3) * kSboA + rg * 128 + (m & 7) * 16;
 			*reinterpret_cast<uint4 *>(A + off) = d2;
 			*reinterpret_cast<uint4 *>(A + kPieceBytes + off) = d1;
 			*reinterpret_cast<uint4 *>(A + 2 * kPieceBytes + off) = d0;
 		}
 		uint4 *Bs = reinterpret_cast<uint4 *>(sB + s * 2 * kTileBytes);
-#pragma unroll
-		for(int q = 0; q < 3; q++) Bs[tid + q * kThreads] = bt[q];
+		Bs[tid] = bt[0];
+		if(tid + kThreads < kTilePieces) Bs[tid + kThreads] = bt[1];
 		proxy_fence();
 		__syncthreads();
 		if(*(volatile int *)s_abort) break;
@@ -290,8 +318,8 @@ __global__ void __launch_bounds__(kThreads, 2) k_vtc(const __grid_constant__ TcJ
 		if(waited) tc_fence_before();    // TMEM reads ordered before the next barrier and the MMAs after it
 #pragma unroll
 		for(int k = 0; k < 8; k++) raw[k] = nraw[k];
-#pragma unroll
-		for(int q = 0; q < 3; q++) bt[q] = nbt[q];
+		bt[0] = nbt[0];
+		bt[1] = nbt[1];
 	}
 	// A stop on a timed-out wait can leave committed operations running: wait
 	// (bounded) for the last commit before the tensor memory is released.
@@ -317,7 +345,7 @@ uint16_t bf16_of_int(int v)
 
 size_t tc_smem_bytes(int nphys)
 {
-	return (size_t)kStages * 3 * kPieceBytes + (size_t)kStages * 2 * kTileBytes + (size_t)nphys * 256 * 8 +
+	return (size_t)kStages * 3 * kPieceBytes + (size_t)kStages * 2 * kTileBytes + (size_t)nphys * 256 * 6 +
 		kStages * 8 + 16;
 }
 

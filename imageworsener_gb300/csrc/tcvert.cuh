@@ -24,7 +24,10 @@
 //
 // MMA layout (cta_group::1, kind::f16 with bf16 operands, FP32 accumulators):
 //   A = decoded input, M = 128 byte columns of a strip, K = 32 input rows per
-//       stage; three A operands per stage, one per X digit.
+//       stage; three A operands per stage, one per X digit, written by 8
+//       decoding warps (2 columns x 8 rows per thread, one 16-byte core-matrix
+//       row per column and digit) from a digit table split into a 4-byte
+//       (X2, X1) and a 2-byte (X0) part, whose lookups rarely collide on a bank.
 //   B = weights, N = 48 rows: the W2, W1, W0 digits of 16 output rows (a
 //       block).  The X0 operand uses the first 32 (W2, W1) only.
 //   D = TMEM, 128 lanes (columns) x 128 FP32 columns per block: the sums
@@ -54,7 +57,7 @@ constexpr int kSboA = 528;                 // A: bytes between 8-row groups (512
 constexpr int kPieceBytes = (kM / 8) * kSboA;  // one X digit of a stage: 8448
 constexpr int kTileBytes = 48 * kRows * 2;      // one block's W digits of a stage: 3072
 constexpr int kTmemCols = 256;             // two live blocks of 128 columns
-constexpr int kThreads = 128;
+constexpr int kThreads = 256;             // 8 warps: warp w decodes rows 8(w/2).. of 64 columns of a stage
 
 struct TcJob {
 	const uint8_t *in;            // input at the crop origin
@@ -96,7 +99,7 @@ void tc_geometry(const TcBuild &B, int cols, int sms, int &strips, int &bands, i
 
 size_t tc_smem_bytes(int nphys);
 // k_vtc, for cudaLaunchKernel with a TcJob argument; 'vec': the input at the
-// crop origin and its row stride are 4-byte aligned (word loads)
+// crop origin and its row stride are 2-byte aligned (16-bit loads)
 const void *tc_kernel(bool vec);
 
 }  // namespace tc
