@@ -5,7 +5,8 @@ for sm_103a, linked with nvcc into one shared library.
     python -m imageworsener_gb300.build --force  # rebuild everything
 
 Objects go to imageworsener_gb300/_build/, the library to
-imageworsener_gb300/libimagew_gb300.so (both git-ignored).  Sources compile
+imageworsener_gb300/libimagew_gb300.so and the command-line tool to
+imageworsener_gb300/imagew_gb300 (all git-ignored).  Sources compile
 in parallel; a file is recompiled only when it, or a header, changed.
 """
 from __future__ import annotations
@@ -88,7 +89,27 @@ def build(force: bool = False, verbose: bool = False) -> str:
             sys.stderr.write(" ".join(cmd) + "\n" + r.stdout + r.stderr)
         if r.returncode:
             raise RuntimeError("link failed")
+    build_cli(force)
     return LIB
+
+
+CLI_DIR = os.path.join(PKG, "cli")
+CLI = os.path.join(PKG, "imagew_gb300")
+
+
+def build_cli(force: bool = False) -> str:
+    """The imagew_gb300 command-line tool (cli/*.c), linked against the
+    library next to it."""
+    srcs = [os.path.join(CLI_DIR, f) for f in ("imagew_cli.c", "pnm.c")]
+    deps = srcs + [os.path.join(CLI_DIR, "pnm.h"), os.path.join(INCLUDE, "imagew.h"), LIB]
+    if force or not os.path.exists(CLI) or any(os.path.getmtime(d) > os.path.getmtime(CLI) for d in deps):
+        cmd = ["gcc", "-std=gnu99", "-O2", "-Wall", f"-I{INCLUDE}", f"-I{CLI_DIR}", "-o", CLI, *srcs,
+               f"-L{PKG}", "-limagew_gb300", "-Wl,-rpath,$ORIGIN", "-lm"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode:
+            sys.stderr.write(" ".join(cmd) + "\n" + r.stdout + r.stderr)
+            raise RuntimeError("CLI build failed")
+    return CLI
 
 
 if __name__ == "__main__":

@@ -1,0 +1,31 @@
+"""Generates tests/golden/cli_cases.json: for each case of tests/iwcli.py,
+the exit code of the reference's own imagew (built from its sources by
+`make -C oracle refcli`) and the SHA-256 of the file it wrote.
+
+    python tests/golden/make_cli_golden.py
+"""
+import json
+import os
+import sys
+import tempfile
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(HERE))
+import iwcli  # noqa: E402
+
+ROOT = os.path.dirname(os.path.dirname(HERE))
+REF_CLI = os.path.join(ROOT, "oracle", "_ref", "imagew_ref")
+N = 200
+
+if __name__ == "__main__":
+    if not os.path.exists(REF_CLI):
+        sys.exit("build the reference CLI first: make -C oracle refcli")
+    out = []
+    with tempfile.TemporaryDirectory() as d:
+        for seed in range(N):
+            c = iwcli.case(seed)
+            rc, digest = iwcli.run_case(REF_CLI, c, d)
+            out.append({**c, "rc": rc, "sha256": digest})
+    with open(os.path.join(HERE, "cli_cases.json"), "w") as f:
+        json.dump(out, f, indent=0)
+    print(len(out), "cases;", sum(1 for c in out if c["rc"] == 0), "written")
