@@ -226,6 +226,10 @@ struct iw_context {
 	int no_gamma = 0, intclamp = 0, pref_units = 0;
 	int randomize = 0, seed = 0;
 	iw_byte opt_gray = 1, opt_pal = 1, opt_16to8 = 1, opt_strip = 1, opt_bintrns = 1;
+	// the post-pass's property scan done on the device (pipeline.cu
+	// k_out_props): bits 0-3 as OptState's has_16bit, has_trns,
+	// has_partial_trns, has_color; 0x100 = valid
+	int opt_dev_props = 0;
 	iwg::DimRequest dim[2];
 	int compression = 0, page = 0, include_screen = 1, interlaced = 0, bmp_nofh = 0, out_fmt = 0;
 	struct Option { char *name; char *val; };

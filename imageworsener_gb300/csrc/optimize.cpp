@@ -356,7 +356,17 @@ void optimize(iw_context *ctx)
 		if(o.label[0] != o.label[1] || o.label[0] != o.label[2]) o.has_color = 1;
 		if(o.bit_depth == 16 && (o.label[0] % 257 || o.label[1] % 257 || o.label[2] % 257)) o.has_16bit = 1;
 	}
-	if(scan_pixels(o)) {
+	bool scanned;
+	if(ctx->opt_dev_props & 0x100) {   // the same scan, done on the device over the whole image
+		const int f = ctx->opt_dev_props;
+		if(f & 1) o.has_16bit = 1;
+		if(f & 2) o.has_trns = 1;
+		if(f & 4) o.has_partial_trns = 1;
+		if(f & 8) o.has_color = 1;
+		scanned = true;
+	}
+	else scanned = scan_pixels(o);
+	if(scanned) {
 		if(o.bit_depth == 16 && !o.has_16bit) to_8bit(ctx, o, nch_of(o.imgtype));
 		if(!o.has_trns && ctx->opt_strip) {
 			if(o.imgtype == IW_IMGTYPE_RGBA) pick(ctx, o, IW_IMGTYPE_RGB, 0, 1, 2);

@@ -1288,6 +1288,40 @@ int launch_fix_flagged_batch(cudaStream_t st, const Job *jobs, int maxt, int *co
 	return launch_fix<true>(st, none, jobs, maxt, count, list, cap);
 }
 
+// Device form of the output post-pass's property scan (optimize.cpp
+// scan_pixels; src/imagew-opt.c:18-386) over the output image while it is in
+// device memory: bit 0 a 16-bit sample whose two bytes differ (16 bits
+// needed), bit 1 an alpha below full (transparency), bit 2 an alpha strictly
+// between 0 and full (partial transparency), bit 3 a pixel whose R, G and B
+// differ (colour).  Warp-level OR, one atomic per warp with a bit set.
+__global__ void k_out_props(const uint8_t *out, int w, int h, unsigned long long bpr, int nch, int wide, int has_a,
+	int rgb, unsigned int *flags)
+{
+	unsigned int f = 0;
+	const unsigned int full = wide ? 65535u : 255u;
+	const long long total = (long long)w * h;
+	const long long step = (long long)gridDim.x * blockDim.x;
+	for(long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < total; p += step) {
+		const int y = (int)(p / w), x = (int)(p - (long long)y * w);
+		const uint8_t *q = out + (unsigned long long)y * bpr + (unsigned long long)x * nch * (wide ? 2 : 1);
+		unsigned int v[4] = {0, 0, 0, 0};
+		for(int k = 0; k < nch && k < 4; k++) {
+			if(wide) {
+				v[k] = ((unsigned int)q[2 * k] << 8) | q[2 * k + 1];
+				if(q[2 * k] != q[2 * k + 1]) f |= 1u;
+			}
+			else v[k] = q[k];
+		}
+		if(has_a && v[nch - 1] < full) {
+			f |= 2u;
+			if(v[nch - 1] > 0) f |= 4u;
+		}
+		if(rgb && (v[0] != v[1] || v[0] != v[2])) f |= 8u;
+	}
+	f = __reduce_or_sync(0xffffffffu, f);
+	if((threadIdx.x & 31) == 0 && f) atomicOr(flags, f);
+}
+
 // ===========================================================================
 // Host side: device memory, tables, launches
 // ===========================================================================
@@ -1593,7 +1627,7 @@ void preload_kernels()
 		for(const void *k : {(const void *)k_vpass_exact, (const void *)k_hpass_exact, (const void *)k_scan,
 			(const void *)k_finalize, (const void *)kb_vpass_exact, (const void *)kb_hpass_exact, (const void *)kb_scan,
 			(const void *)kb_finalize, (const void *)k_fix_flagged_warp<true>, (const void *)k_fix_flagged_warp<false>,
-			(const void *)k_fix_wide_df<true>, (const void *)k_fix_wide_df<false>,
+			(const void *)k_fix_wide_df<true>, (const void *)k_fix_wide_df<false>, (const void *)k_out_props,
 			(const void *)k_fix_leftover<true>, (const void *)k_fix_leftover<false>,
 			(const void *)k_fix_flagged_thread<true>, (const void *)k_fix_flagged_thread<false>})
 			cudaFuncGetAttributes(&a, k);
@@ -1966,11 +2000,33 @@ bool run_pipeline(iw_context *ctx, Plan &P, int warmup, int iters, int lane)
 		if(g) cudaGraphDestroy(g);
 		cudaGetLastError();
 	}
+	// The post-pass's property scan as a device reduction over the output,
+	// where the host would scan it (16-bit, or 8-bit with more than one
+	// channel; integer output at a full max code) and the output is in device
+	// memory; the flags come back with the image.
+	unsigned int prop_flags = 0;
+	bool props = false;
+	{
+		const int ot = ctx->img2.imgtype, od = ctx->img2.bit_depth;
+		const bool wide = od == 16;
+		if(!zero_copy && ctx->img2.sampletype == IW_SAMPLETYPE_UINT && !ctx->reduced_out && (od == 8 || od == 16) &&
+			!(ot == IW_IMGTYPE_GRAY && !wide) && P.out_w > 0 && P.out_h > 0 && S.flags.ensure(16)) {
+			const int nch = iw_imgtype_num_channels(ot);
+			cudaMemsetAsync(S.flags.p, 0, sizeof(unsigned int), st);
+			const long long px = (long long)P.out_w * P.out_h;
+			const unsigned blocks = (unsigned)std::min<long long>((px + 255) / 256, 4096);
+			k_out_props<<<blocks, 256, 0, st>>>((const uint8_t *)S.out.p, P.out_w, P.out_h, (unsigned long long)P.out_bpr,
+				nch, wide ? 1 : 0, IW_IMGTYPE_HAS_ALPHA(ot) ? 1 : 0, IW_IMGTYPE_IS_GRAY(ot) ? 0 : 1, (unsigned int *)S.flags.p);
+			props = true;
+		}
+	}
 	if(S.lane != 0) wait_stream(st, true);   // downloads queued once the kernels are done (as for batches)
+	if(props) cudaMemcpyAsync(&prop_flags, S.flags.p, sizeof(unsigned int), cudaMemcpyDeviceToHost, st);
 	if(upmode == UP_COPY) cudaMemcpyAsync(ctx->img2.pixels, S.out.p, out_bytes, cudaMemcpyDeviceToHost, st);
 	if(upmode == UP_STAGE) stage_d2h(S.stager, st, {Xfer{(uint8_t *)S.out.p, (uint8_t *)ctx->img2.pixels, out_bytes}});
 	cudaError_t ce = wait_stream(st, S.lane != 0);
 	if(ce == cudaSuccess) ce = cudaGetLastError();
+	ctx->opt_dev_props = (ce == cudaSuccess && props) ? (int)(prop_flags | 0x100u) : 0;
 	ctx->stats.flagged = 0;
 	ctx->stats.flagged_exact = 0;
 	if(ce == cudaSuccess && fast && fi.flag_count_dev) {

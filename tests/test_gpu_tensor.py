@@ -161,3 +161,40 @@ def test_autotuned_bands_same_bytes(gpulib, vertical):
         job.calls = list(job.calls) + [("iw_set_option", b"gpu:autotune", b"off")]
         b, _ = run_with_stats(gpulib, job, vertical)
         assert a.key() == b.key(), seed
+
+
+def _props_job(kind: str, seed: int) -> Job:
+    """Inputs whose output post-pass has to scan the whole image: opaque,
+    gray-valued, 8-bit-representable 16-bit samples, or a single partial
+    alpha value / coloured pixel far from the start."""
+    from imageworsener_gb300.iwapi import IMGTYPE_RGBA, IMGTYPE_GRAYA
+    rng = np.random.default_rng(seed)
+    w, h = int(rng.integers(40, 200)), int(rng.integers(40, 200))
+    g = rng.integers(0, 256, (h, w)).astype(np.uint16)
+    if kind == "rgba16_opaque_gray":
+        px = np.stack([g * 257, g * 257, g * 257, np.full_like(g, 65535)], -1).astype(">u2").tobytes()
+        return Job(IMGTYPE_RGBA, 16, w, h, px, calls=[("iw_set_output_profile", iwcases.PNG),
+                                                       ("iw_set_output_canvas_size", w, h),
+                                                       ("iw_set_output_depth", 16)] + iwcases._resize_calls("null", 0, 0))
+    if kind == "rgb8_late_colour":
+        a = np.stack([g, g, g], -1).astype(np.uint8)
+        a[h - 1, w - 1, 0] ^= 1
+        return Job(IMGTYPE_RGB, 8, w, h, a.tobytes(), calls=[("iw_set_output_profile", iwcases.PNG),
+                                                            ("iw_set_output_canvas_size", w, h)] + iwcases._resize_calls("null", 0, 0))
+    a = np.stack([g, np.full_like(g, 255)], -1).astype(np.uint8)   # graya8, one partial alpha at the end
+    a[h - 1, w - 1, 1] = 128
+    return Job(IMGTYPE_GRAYA, 8, w, h, a.tobytes(), calls=[("iw_set_output_profile", iwcases.PNG),
+                                                          ("iw_set_output_canvas_size", w // 2 + 1, h // 2 + 1)])
+
+
+@pytest.mark.parametrize("kind", ["rgba16_opaque_gray", "rgb8_late_colour", "graya8_late_partial"])
+def test_post_pass_properties_from_device(gpulib, oracle, kind):
+    """The post-pass's property scan (16-bit need, transparency, colour) runs
+    as a device reduction over the output; the repacked image equals the
+    oracle's."""
+    for seed in range(3):
+        want = run_job(oracle, _props_job(kind, seed))
+        got = run_job(gpulib, _props_job(kind, seed))
+        assert got.key() == want.key(), (kind, seed)
+    if kind == "rgba16_opaque_gray":
+        assert got.imgtype == 1 and got.bit_depth == 8   # alpha stripped, gray, 8-bit
