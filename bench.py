@@ -536,7 +536,7 @@ def main():
         st64, dig_plain = device_timed(lib, job, 1, max(2, min(args.steps, 5)), "fp64")
         barrier()
         progress("end to end")
-        e2e_times, dig_e2e, e2e_zc = e2e_timed(lib, job, 2, max(3, min(args.steps, 10)))
+        e2e_times, dig_e2e, e2e_zc = e2e_timed(lib, job, max(3, args.warmup), max(3, min(args.steps, 20)))
         e2e_modes = {}
         for mode in ("zero", "stage", "copy"):
             progress(f"end to end, transfer {mode}")
@@ -604,7 +604,9 @@ def main():
         "e2e": {"value": world * out_px / 1e6 / (e2e_ms / 1000.0), "unit": "Mpix/s", "h2d_bytes_per_step": in_bytes,
                 "d2h_bytes_per_step": out_bytes, "ms_per_step": e2e_ms, "p50_ms": 1000 * statistics.median(e2e_times),
                 "host_buffers": "pageable (caller-malloc'd, as the libimagew ownership model requires)",
-                "transfer": "zero-copy (GPU reads/writes host memory over NVLink-C2C)" if e2e_zc.get("zero_copy") else "pinned staging (host copy threads + DMA)",
+                "transfer": "zero-copy (GPU reads/writes host memory over NVLink-C2C)" if e2e_zc.get("zero_copy") else
+                            "cudaMemcpyAsync from / to the caller's pageable buffers (default for one image)",
+                "step_ms": [round(1000 * t, 3) for t in e2e_times],
                 "last_call": e2e_zc, "by_transfer_mode": e2e_modes},
         "roofline": {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None, "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)",
