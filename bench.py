@@ -348,8 +348,20 @@ def batch_leg(lib: IWLib, n_images: int, pool_size: int, cpu_threads: int, cpu_i
     ctxs, _, _, _ = run(jobs[:64], modes[0])     # warm-up: device tables, kernel modules
     free(ctxs)
     per_mode = {}
+    phases = (C.c_double * 14)()
+    lib.dll.iwg_batch_phase_ms.restype = C.c_int
+    lib.dll.iwg_batch_phase_ms.argtypes = [C.POINTER(C.c_double), C.c_int]
+    host_phase = None
     for mode in modes:
+        lib.dll.iwg_batch_phase_ms(phases, 14)
+        before = list(phases)
         ctxs, ok_m, wall_m, st_m = run(jobs, mode)
+        lib.dll.iwg_batch_phase_ms(phases, 14)
+        if host_phase is None:   # the first (default) mode's breakdown
+            names = ("plan", "fast_batches", "plain_batches", "post_pass", "prepare", "upload", "launch_passes",
+                     "launch_fixup", "wait_download", "rest", "of_which_tables", "of_which_attributes",
+                     "of_which_d2h_wait", "of_which_d2h_copy")
+            host_phase = {k: round(a - b, 3) for k, a, b in zip(names, phases, before)}
         dig_m = [output_digest(lib, ctxs[k]) for k in range(min(pool_size, n_images))]
         free(ctxs)
         per_mode[mode] = {"wall_ms": 1000 * wall_m, "e2e_mpix_s": out_px / 1e6 / wall_m, "device_ms": st_m.ms_device}
@@ -371,7 +383,8 @@ def batch_leg(lib: IWLib, n_images: int, pool_size: int, cpu_threads: int, cpu_i
            "last_chunk_ms": {"vertical": st.ms_part[0], "horizontal": st.ms_part[1], "fixup": st.ms_part[2]},
            "last_chunk_flagged": st.flagged, "last_chunk_left_to_fp64": st.flagged_exact,
            "lone_mpix_s": pool_px / 1e6 / lone_dt,
-           "identical_to_lone": digests == lone[:len(digests)], "transfer": modes[0], "by_transfer_mode": per_mode}
+           "identical_to_lone": digests == lone[:len(digests)], "transfer": modes[0], "by_transfer_mode": per_mode,
+           "host_phase_ms": host_phase}
     if cpu_images > 0:
         import concurrent.futures as cf
         oracle = IWLib(os.path.join(ROOT, "oracle", "_build", "liboracle_iw.so"))

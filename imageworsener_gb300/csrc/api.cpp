@@ -14,6 +14,7 @@
 #include <algorithm>
 #include <atomic>
 #include <chrono>
+#include <mutex>
 #include <ctime>
 #include <thread>
 #include <vector>
@@ -965,10 +966,37 @@ size_t iwg::batch_device_bytes(const iwg::Plan &P)
 	return in + mid + out + scan + (size_t)P.out_w * P.out_h * 16 + 4096;
 }
 
+// Host wall time of iwg_process_batch's stages, process-wide sums (ms):
+// planning, fast-form batches, plain-form batches, output post-pass.
+static std::mutex g_bstage_mu;
+static double g_bstage_ms[4] = {0, 0, 0, 0};
+
+static void bstage_add(int k, std::chrono::steady_clock::time_point &t)
+{
+	const auto n = std::chrono::steady_clock::now();
+	std::lock_guard<std::mutex> lk(g_bstage_mu);
+	g_bstage_ms[k] += std::chrono::duration<double, std::milli>(n - t).count();
+	t = n;
+}
+
+extern "C" int iwg_batch_phase_ms(double *out, int n)
+{
+	double v[4 + iwg::kBatchPhases];
+	{
+		std::lock_guard<std::mutex> lk(g_bstage_mu);
+		for(int k = 0; k < 4; k++) v[k] = g_bstage_ms[k];
+	}
+	iwg::batch_phase_ms(v + 4);
+	int m = 0;
+	for(; out && m < n && m < 4 + iwg::kBatchPhases; m++) out[m] = v[m];
+	return m;
+}
+
 extern "C" int iwg_process_batch(struct iw_context **ctxs, int n)
 {
 	if(!ctxs || n <= 0) return 0;
 	auto t0 = std::chrono::steady_clock::now();
+	auto ts = t0;
 	std::vector<iwg::Plan> plans(n);
 	std::vector<char> planned(n, 0);
 	parallel_for(n, [&](int i) {
@@ -981,6 +1009,7 @@ extern "C" int iwg_process_batch(struct iw_context **ctxs, int n)
 		ctx->use_count++;
 		planned[i] = iwg::build_plan(ctx, plans[i]) ? 1 : 0;
 	});
+	bstage_add(0, ts);
 	// chunks of at most kBudget device bytes, in the callers' order
 	const size_t kBudget = (size_t)8 << 30;
 	std::vector<char> done(n, 0);
@@ -1006,7 +1035,9 @@ extern "C" int iwg_process_batch(struct iw_context **ctxs, int n)
 		}
 		std::vector<int> status;
 		double dev_ms = 0;
+		ts = std::chrono::steady_clock::now();
 		iwg::run_batch(cc, pp, status, dev_ms);
+		bstage_add(1, ts);
 		dev_total += dev_ms;
 		// what the fast form did not take: one batch in the plain form
 		std::vector<iw_context *> cc2;
@@ -1024,6 +1055,7 @@ extern "C" int iwg_process_batch(struct iw_context **ctxs, int n)
 		if(!cc2.empty()) {
 			std::vector<int> status2;
 			iwg::run_batch_plain(cc2, pp2, status2, dev_ms);
+			bstage_add(2, ts);
 			dev_total += dev_ms;
 			for(size_t j = 0; j < idx2.size(); j++) {
 				const int i = idx2[j];
@@ -1032,11 +1064,13 @@ extern "C" int iwg_process_batch(struct iw_context **ctxs, int n)
 			}
 		}
 	}
+	ts = std::chrono::steady_clock::now();
 	parallel_for(n, [&](int i) {
 		if(!done[i]) return;
 		iwg::bkgd_label(ctxs[i], plans[i]);
 		iwg::optimize(ctxs[i]);
 	});
+	bstage_add(3, ts);
 	const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
 	int ok = 0;
 	for(int i = 0; i < n; i++)

@@ -67,6 +67,13 @@ IW_EXPORT(int) iwg_process_image_timed(struct iw_context *ctx, int warmup, int i
  * buf (NUL-terminated, at most buflen bytes).  Returns 0 if no device. */
 IW_EXPORT(int) iwg_device_info(char *buf, int buflen);
 
+/* Host time of iwg_process_batch() calls, process-wide sums in ms: [0]
+ * planning (on all host threads, wall time), [1] the fast-form batches, [2]
+ * the plain-form batches, [3] the output post-pass (all host threads, wall),
+ * [4..13] the batched calls' phases as in iwg_server_info.batch_phase_ms.
+ * Writes at most n values; returns how many. */
+IW_EXPORT(int) iwg_batch_phase_ms(double *out, int n);
+
 /* Processes n contexts as one batch.  Each context must be set up as for
  * iw_process_image() and not yet processed; afterwards each holds exactly the
  * output iw_process_image() would have given it alone (and counts as
