@@ -92,7 +92,8 @@ constexpr int kHWarpTaps = 64;   // horizontal windows from this many taps: a wa
 // are cached under (address, kind) together with a reference that keeps the
 // source alive.
 struct Cache {
-	std::mutex mu;
+	std::mutex mu;        // the per-image scratch and the band tuner
+	std::mutex tab_mu;    // the device table cache 'dev' (and the decode-error record)
 	struct Entry { std::shared_ptr<const void> keep; std::shared_ptr<const void> derived; void *dev; };
 	std::map<std::pair<const void *, int>, Entry> dev;
 	void *scratch = nullptr;
@@ -119,6 +120,7 @@ template<class T>
 const T *dev_table(const std::shared_ptr<const std::vector<T>> &v)
 {
 	Cache &C = cache();
+	std::lock_guard<std::mutex> lk(C.tab_mu);
 	auto key = std::make_pair((const void *)v.get(), 0);
 	auto it = C.dev.find(key);
 	if(it != C.dev.end()) return (const T *)it->second.dev;
@@ -132,6 +134,7 @@ template<class Fn>
 const float *dev_derived(const std::shared_ptr<const std::vector<double>> &v, int kind, Fn make)
 {
 	Cache &C = cache();
+	std::lock_guard<std::mutex> lk(C.tab_mu);
 	auto key = std::make_pair((const void *)v.get(), kind);
 	auto it = C.dev.find(key);
 	if(it != C.dev.end()) return (const float *)it->second.dev;
@@ -380,7 +383,10 @@ static FastState *fast_build(const Plan &P, const Job &J, bool batch, int tc_mod
 			dec_err[std::make_pair((const void *)coltab.get(), P.in_depth)] = dt.err;
 			return dt.f;
 		});
-		e_dec = dec_err[std::make_pair((const void *)coltab.get(), P.in_depth)];
+		{
+			std::lock_guard<std::mutex> lk(cache().tab_mu);
+			e_dec = dec_err[std::make_pair((const void *)coltab.get(), P.in_depth)];
+		}
 		dec_floats = P.in_depth == 8 ? 256 : 8192;
 		if(!dec_tab) { err = "Out of GPU memory (fast tables)"; return nullptr; }
 	}
@@ -910,10 +916,10 @@ bool fast_prepare(cudaStream_t st, const Plan &P, Job &J, FastInfo &fi, std::str
 
 // ---- batch support (see fastpath.cuh) ----
 
+// Safe to call from several host threads at once: fast_build's shared state
+// (the device table cache) is guarded by its own lock.
 void *fast_batch_item(const Plan &P, const Job &J, std::string &err)
 {
-	Cache &C = cache();
-	std::lock_guard<std::mutex> lk(C.mu);
 	return fast_build(P, J, true, 0, err);
 }
 

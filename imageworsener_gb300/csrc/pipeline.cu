@@ -2134,9 +2134,12 @@ bool run_batch(const std::vector<iw_context *> &ctxs, const std::vector<Plan *> 
 		const Plan &P = *plans[i];
 		const char *prec = get_option(ctx, "gpu:precision");
 		if(prec && !strcmp(prec, "fp64")) continue;
-		if(!make_job(ctx, P, S, pk, fixes[i], jobs[i])) { status[i] = -1; continue; }
+		// images the fast form cannot take are left to the plain-form batch
+		// (which builds their jobs): decided from the plan, before packing
 		FastInfo fi;
-		if(jobs[i].any_scan || !fast_eligible(P, jobs[i], fi)) continue;
+		if(!fast_eligible(P, jobs[i], fi)) continue;
+		if(!make_job(ctx, P, S, pk, fixes[i], jobs[i])) { status[i] = -1; continue; }
+		if(jobs[i].any_scan) continue;
 		sel.push_back(i);
 	}
 	if(sel.empty()) return true;
@@ -2169,9 +2172,11 @@ bool run_batch(const std::vector<iw_context *> &ctxs, const std::vector<Plan *> 
 	int *flag_count = (int *)(base + o_cnt);
 	int *flag_list = (int *)(base + o_flags);
 
-	// final device addresses, then the fast form's host preparation
+	// final device addresses, then the fast form's host preparation of every
+	// image on the host threads (fast_batch_item is safe to call concurrently)
 	std::vector<void *> items;
 	std::vector<int> item_img;
+	std::vector<int> ready;
 	for(int i : sel) {
 		iw_context *ctx = ctxs[i];
 		const Plan &P = *plans[i];
@@ -2183,14 +2188,22 @@ bool run_batch(const std::vector<iw_context *> &ctxs, const std::vector<Plan *> 
 		J.in = zc ? (const uint8_t *)ctx->img1.pixels : base + o_in[i];
 		J.interm = (float *)(base + o_mid[i]);
 		J.out = zc ? (uint8_t *)ctx->img2.pixels : base + o_out[i];
+		ready.push_back(i);
+	}
+	std::vector<void *> prepared(ready.size(), nullptr);
+	host_pool().run((int)ready.size(), [&](int k) {
+		cudaSetDevice(S.device);   // pool threads: the lane's device for the table uploads
 		std::string e2;
-		void *it = fast_batch_item(P, J, e2);
-		if(!it) {   // leave it to the caller's lone run
-			iw_free(ctx, ctx->img2.pixels);
-			ctx->img2.pixels = nullptr;
+		prepared[k] = fast_batch_item(*plans[ready[k]], jobs[ready[k]], e2);
+	});
+	for(size_t k = 0; k < ready.size(); k++) {
+		const int i = ready[k];
+		if(!prepared[k]) {   // leave it to the caller's lone run
+			iw_free(ctxs[i], ctxs[i]->img2.pixels);
+			ctxs[i]->img2.pixels = nullptr;
 			continue;
 		}
-		items.push_back(it);
+		items.push_back(prepared[k]);
 		item_img.push_back(i);
 	}
 	if(items.empty()) return true;
