@@ -1581,6 +1581,7 @@ struct DeviceState {
 	int *done_d = nullptr;
 	int done_cap = 0;
 	std::map<const void *, std::pair<std::shared_ptr<const void>, void *>> table_cache;
+	std::mutex table_mu;   // table_cache: batches build jobs on several host threads
 	std::vector<uint8_t> staging;
 	Stager stager;
 };
@@ -1687,6 +1688,7 @@ template<class T>
 const T *cached_table(DeviceState &S, const std::shared_ptr<const std::vector<T>> &v)
 {
 	if(!v) return nullptr;
+	std::lock_guard<std::mutex> lk(S.table_mu);
 	auto it = S.table_cache.find(v.get());
 	if(it != S.table_cache.end()) return (const T *)it->second.second;
 	void *d = nullptr;
@@ -2067,6 +2069,44 @@ bool run_pipeline(iw_context *ctx, Plan &P, int warmup, int iters, int lane)
 	return true;
 }
 
+// Batches of at least this many images prepare their jobs on the host pool
+// (shared by all lanes, so a small serving batch would wait for it).
+constexpr int kPoolMin = 16;
+
+// make_job for the images 'which' on the host threads.  Each image packs its
+// arrays into a buffer of its own; the buffers are then appended to
+// S.staging in image order, each at a 256-byte boundary (as the packer aligns
+// its arrays), and the image's fix-up offsets moved by its buffer's position,
+// so the result equals packing them one after the other.  ok[k]: make_job's
+// result for which[k].
+static void make_jobs(const std::vector<iw_context *> &ctxs, const std::vector<Plan *> &plans, const std::vector<int> &which,
+	DeviceState &S, std::vector<std::vector<Fixup>> &fixes, std::vector<Job> &jobs, std::vector<char> &ok)
+{
+	const int m = (int)which.size();
+	std::vector<std::vector<uint8_t>> bufs(m);
+	ok.assign(m, 0);
+	auto one = [&](int k) {
+		const int i = which[k];
+		Packer pk(bufs[k]);
+		ok[k] = make_job(ctxs[i], *plans[i], S, pk, fixes[i], jobs[i]) ? 1 : 0;
+	};
+	if(m < kPoolMin)   // small batches (serving): no wait for the shared pool
+		for(int k = 0; k < m; k++) one(k);
+	else
+		host_pool().run(m, [&](int k) {
+			cudaSetDevice(S.device);   // pool threads: the lane's device for the table uploads
+			one(k);
+		});
+	S.staging.clear();
+	for(int k = 0; k < m; k++) {
+		if(!ok[k]) continue;
+		const size_t base = (S.staging.size() + 255) & ~(size_t)255;
+		S.staging.resize(base + bufs[k].size());
+		if(!bufs[k].empty()) memcpy(S.staging.data() + base, bufs[k].data(), bufs[k].size());
+		for(Fixup &f : fixes[which[k]]) f.off += base;
+	}
+}
+
 // A batch of planned images.  The images the fast form takes run together:
 // one launch per kernel variant for the vertical and horizontal passes, one
 // exact re-evaluation launch for the flagged pixels of all of them.  Each
@@ -2127,20 +2167,25 @@ bool run_batch(const std::vector<iw_context *> &ctxs, const std::vector<Plan *> 
 	}
 	std::vector<Job> jobs(n);                 // sized once: fix-ups point into it
 	std::vector<std::vector<Fixup>> fixes(n);
-	Packer pk(S.staging);
-	std::vector<int> sel;
+	std::vector<int> cand, sel;
 	for(int i = 0; i < n; i++) {
-		iw_context *ctx = ctxs[i];
-		const Plan &P = *plans[i];
-		const char *prec = get_option(ctx, "gpu:precision");
+		const char *prec = get_option(ctxs[i], "gpu:precision");
 		if(prec && !strcmp(prec, "fp64")) continue;
 		// images the fast form cannot take are left to the plain-form batch
 		// (which builds their jobs): decided from the plan, before packing
 		FastInfo fi;
-		if(!fast_eligible(P, jobs[i], fi)) continue;
-		if(!make_job(ctx, P, S, pk, fixes[i], jobs[i])) { status[i] = -1; continue; }
-		if(jobs[i].any_scan) continue;
-		sel.push_back(i);
+		if(!fast_eligible(*plans[i], jobs[i], fi)) continue;
+		cand.push_back(i);
+	}
+	{
+		std::vector<char> ok;
+		make_jobs(ctxs, plans, cand, S, fixes, jobs, ok);
+		for(size_t k = 0; k < cand.size(); k++) {
+			const int i = cand[k];
+			if(!ok[k]) { status[i] = -1; continue; }
+			if(jobs[i].any_scan) continue;
+			sel.push_back(i);
+		}
 	}
 	if(sel.empty()) return true;
 
@@ -2191,11 +2236,17 @@ bool run_batch(const std::vector<iw_context *> &ctxs, const std::vector<Plan *> 
 		ready.push_back(i);
 	}
 	std::vector<void *> prepared(ready.size(), nullptr);
-	host_pool().run((int)ready.size(), [&](int k) {
-		cudaSetDevice(S.device);   // pool threads: the lane's device for the table uploads
+	auto prep = [&](int k) {
 		std::string e2;
 		prepared[k] = fast_batch_item(*plans[ready[k]], jobs[ready[k]], e2);
-	});
+	};
+	if((int)ready.size() < kPoolMin)   // small batches (serving): no wait for the shared pool
+		for(int k = 0; k < (int)ready.size(); k++) prep(k);
+	else
+		host_pool().run((int)ready.size(), [&](int k) {
+			cudaSetDevice(S.device);   // pool threads: the lane's device for the table uploads
+			prep(k);
+		});
 	for(size_t k = 0; k < ready.size(); k++) {
 		const int i = ready[k];
 		if(!prepared[k]) {   // leave it to the caller's lone run
@@ -2379,11 +2430,15 @@ bool run_batch_plain(const std::vector<iw_context *> &ctxs, const std::vector<Pl
 	}
 	std::vector<Job> jobs(n);
 	std::vector<std::vector<Fixup>> fixes(n);
-	Packer pk(S.staging);
-	std::vector<int> sel;
-	for(int i = 0; i < n; i++) {
-		if(!make_job(ctxs[i], *plans[i], S, pk, fixes[i], jobs[i])) { status[i] = -1; continue; }
-		sel.push_back(i);
+	std::vector<int> all(n), sel;
+	for(int i = 0; i < n; i++) all[i] = i;
+	{
+		std::vector<char> ok;
+		make_jobs(ctxs, plans, all, S, fixes, jobs, ok);
+		for(int i = 0; i < n; i++) {
+			if(!ok[i]) { status[i] = -1; continue; }
+			sel.push_back(i);
+		}
 	}
 	if(sel.empty()) return true;
 	const int upmode = upload_mode(ctxs[sel[0]], S, false, true);
