@@ -301,6 +301,7 @@ int pnm_write(struct iw_context *ctx, FILE *f, int fmt)
 	switch(fmt) {
 	case IW_FORMAT_PPM: return write_rgb(ctx, f, &img, 0);
 	case IW_FORMAT_PGM: return write_gray(ctx, f, &img, 0);
+	case IW_FORMAT_PBM: return write_pbm(ctx, f, &img);
 	case IW_FORMAT_PAM:
 		if(img.imgtype == IW_IMGTYPE_RGBA) return write_alpha(ctx, f, &img, 4);
 		if(img.imgtype == IW_IMGTYPE_GRAYA) return write_alpha(ctx, f, &img, 2);

@@ -90,6 +90,83 @@ def case(seed: int) -> dict:
     return {"seed": seed, "kind": kind, "w": w, "h": h, "out": out, "args": args}
 
 
+HEX = ["ff0000", "0f0", "12345678", "0000ffff0000", "808080", "fff", "c0ffee80", "zz"]
+REORIENT = ["fliph", "flipv", "rotate90", "rotate180", "rotate270", "transpose", "transverse", "3", "6"]
+CSPACES = ["linear", "gamma1.8", "gamma2.4", "srgb", "srgbp", "srgbr", "rec709"]
+
+
+def _extra_options(rng) -> list[str]:
+    """One of the options beyond size / filter / depth / dither / crop:
+    relative and fitted sizes, interpolating blur, translation, image size,
+    channel offsets, per-channel depths / colour counts / dithers, grayscale
+    formulas, colour spaces, gamma and clamping switches, optimisation
+    switches, random seeds, backgrounds, reorientation, PBM output."""
+    i = int(rng.integers(22))
+    num = lambda lo, hi: "%g" % round(float(rng.uniform(lo, hi)), 2)  # noqa: E731
+    if i == 0:
+        return [str(rng.choice(["-w", "-h"])), "x" + num(0.2, 2.5)]
+    if i == 1:
+        return [str(rng.choice(["-s", "-S"])), "%d,%d" % (int(rng.integers(1, 200)), int(rng.integers(1, 200)))]
+    if i == 2:
+        return [str(rng.choice(["-blur", "-blurx", "-blury"])), str(rng.choice(["x", "x" + num(0.5, 1.5)]))]
+    if i == 3:
+        return ["-translate", ("s" if rng.random() < 0.4 else "") + num(-3, 3) + "," + num(-3, 3)] + \
+            (["-edge", "t"] if rng.random() < 0.5 else [])
+    if i == 4:
+        return ["-imagesize", "%s,%s" % (num(5, 120), num(5, 120)), "-edge", str(rng.choice(["s", "t"]))]
+    if i == 5:
+        return ["-offset" + str(rng.choice(["red", "green", "blue", "rb", "vred", "vgreen", "vblue", "vrb"])), num(-2, 2)]
+    if i == 6:
+        return ["-depth", ",".join(str(int(rng.integers(1, 17))) for _ in range(int(rng.integers(3, 5))))]
+    if i == 7:
+        return [str(rng.choice(["-depthgray", "-depthalpha"])), str(int(rng.integers(1, 16)))]
+    if i == 8:
+        return ["-depthcc", str(int(rng.choice([2, 3, 6, 100, 300])))]
+    if i == 9:
+        return ["-cc", ",".join(str(int(rng.integers(2, 40))) for _ in range(4))]
+    if i == 10:
+        return ["-cc" + str(rng.choice(["color", "alpha", "red", "green", "blue", "gray"])), str(int(rng.integers(2, 20)))]
+    if i == 11:
+        return ["-dither" + str(rng.choice(["color", "alpha", "red", "green", "blue", "gray"])),
+                str(rng.choice(DITHERS)), "-cc", str(int(rng.integers(2, 12)))]
+    if i == 12:
+        return [str(rng.choice(["-gsf", "-grayscaleformula"])),
+                str(rng.choice(["s", "c", "w0.2,0.5,0.3", "v1,0.4,0.1", "v1", "w2,1,1"]))]
+    if i == 13:
+        return ["-condgrayscale"]
+    if i == 14:
+        return [str(rng.choice(["-cs", "-inputcs"])), str(rng.choice(CSPACES))] + \
+            (["-intent", str(rng.choice(["p", "r", "s", "a", "default", "none", "d"]))] if rng.random() < 0.3 else [])
+    if i == 15:
+        return [str(rng.choice(["-nogamma", "-intclamp", "-negate", "-nocslabel"]))]
+    if i == 16:
+        return ["-noopt", str(rng.choice(["all", "grayscale", "palette", "reduceto8", "stripalpha", "binarytrns"]))]
+    if i == 17:
+        return ["-randseed", str(int(rng.integers(1, 1000))), "-dither", str(rng.choice(["r", "r2"])),
+                "-cc", str(int(rng.integers(2, 8)))]
+    if i == 18:
+        if rng.random() < 0.5:
+            return ["-bkgd", str(rng.choice(HEX))]
+        return ["-bkgd", "%s,%s" % (rng.choice(HEX[:6]), rng.choice(HEX[:6])), "-checkersize", str(int(rng.integers(1, 9))),
+                "-checkerorigin", "%d,%d" % (int(rng.integers(0, 5)), int(rng.integers(0, 5)))]
+    if i == 19:
+        return ["-reorient", str(rng.choice(REORIENT))]
+    if i == 20:
+        return ["-outfmt", "pbm"] + (["-dither", str(rng.choice(["f", "o", "halftone"]))] if rng.random() < 0.5 else [])
+    return ["-nobestfit", "-w", str(int(rng.integers(1, 200))), "-h", str(int(rng.integers(1, 200))), "-bestfit"]
+
+
+def case_ext(seed: int) -> dict:
+    """A case of case(seed)'s kind, size and output with one to three of the
+    further options added."""
+    c = case(seed)
+    rng = np.random.default_rng(20_000 + seed)
+    args = list(c["args"])
+    for _ in range(int(rng.integers(1, 4))):
+        args += _extra_options(rng)
+    return {**c, "args": args}
+
+
 def run_case(exe: str, c: dict, tmpdir: str) -> tuple[int, str | None]:
     """(exit code, SHA-256 of the written file or None) of one case."""
     import hashlib
