@@ -255,8 +255,8 @@ static int write_alpha(struct iw_context *ctx, FILE *f, const struct iw_image *i
 	int m, j;
 	size_t rowsize;
 	if(img->bit_depth != 8 && img->bit_depth != 16) return 0;
-	m = nch == 4 ? written_maxval(ctx, img, rgba, 4, "PNM/PPM/PAM format requires equal bit depths") :
-	    written_maxval(ctx, img, ga, 2, "PNM/PPM/PAM format requires equal bit depths");
+	m = nch == 4 ? written_maxval(ctx, img, rgba, 4, "PAM format requires equal bit depths") :
+	    written_maxval(ctx, img, ga, 2, "PAM format requires equal bit depths");
 	if(m < 0) return 0;
 	rowsize = (size_t)nch * (img->bit_depth / 8) * img->width;
 	if(nch == 4) header_pam(f, img, 4, m, "RGB_ALPHA");
