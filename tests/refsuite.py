@@ -8,10 +8,12 @@ writes PNM/PAM files only.
   reader hands it to the library (src/imagew-png.c:296-401): palettes
   expanded to RGB(A), tRNS colour keys expanded to an alpha channel (low-bit
   gray to 8 bits first), sBIT applied as a shift plus maximum codes, other
-  images at their own bit depth.  It is written as PGM/PPM/PAM.  Inputs that
-  PNM cannot carry (per-channel sBIT, non-square pixel density when the size
-  is fitted, a background label that -usebkgdlabel asks for) and inputs in
-  other formats (GIF, BMP, JPEG, WebP) are skipped with the reason.
+  images at their own bit depth.  It is written as PGM/PPM/PAM.  For
+  non-square pixel densities the size the front end would fit is computed
+  here and passed as an exact size.  The four lines a PNM/PAM file cannot
+  carry (per-channel sBIT in or out, the input's background label used as
+  the background) run through the library API instead (api_jobs); lines
+  with other formats (GIF, BMP, JPEG, WebP, TIFF, MIFF) are skipped.
 * A PNG output is compared as sample values: the tool writes PAM instead (the
   PNG and PAM output profiles differ only in what the output optimizer may
   pack -- palettes, colour keys, 1/2/4-bit gray -- so the pixel values are
@@ -287,21 +289,57 @@ def cases(tdir: str) -> list[Case]:
     return out
 
 
-def prepare_input(c: Case, tdir: str, tmpdir: str) -> str:
-    """The case's input as a file the PNM/PAM tool reads (raises Unsupported)."""
+def _density_size(opts: list[str], sw: int, sh: int, dx: float, dy: float) -> list[str]:
+    """The options with the size the front end computes for an input of
+    non-square pixels (src/imagew-cmd.c:805-900, do_bestfit :427-454): the
+    source is stretched to square pixels before fitting.  Only -w/-width,
+    -h/-height (pixels or x<factor>) and -density are expected here."""
+    aw, ah = sw, sh
+    if dx > dy:
+        ah = int(0.5 + (dx / dy) * sh)
+    else:
+        aw = int(0.5 + (dy / dx) * sw)
+    req = {0: -1, 1: -1}
+    rest: list[str] = []
+    it = iter(opts)
+    for o in it:
+        if o in ("-w", "-width", "-h", "-height"):
+            k, v = (0 if o in ("-w", "-width") else 1), next(it)
+            req[k] = max(1, int(0.5 + float(v[1:]) * (aw if k == 0 else ah))) if v.startswith("x") else int(v)
+        elif o == "-density":
+            rest += [o, next(it)]
+        elif o.startswith("-") and o not in ("-zipcmprlevel",):
+            raise Unsupported("non-square pixel density with option %s" % o)
+        else:
+            rest.append(o)
+    w, h = req[0], req[1]
+    if w == -1 and h == -1:
+        w, h = aw, ah
+    elif w == -1 or h == -1:   # fit the one given
+        if h == -1:
+            h = int(0.5 + ah * (w / aw))
+        else:
+            w = int(0.5 + aw * (h / ah))
+    return rest + ["-S", "%d,%d" % (max(w, 1), max(h, 1))]
+
+
+def prepare_input(c: Case, tdir: str, tmpdir: str) -> tuple[str, list[str]]:
+    """The case's input as a file the PNM/PAM tool reads, and the options to
+    give it (raises Unsupported)."""
     src = os.path.join(tdir, c.source)
     if not src.endswith(".png"):
-        return src
+        return src, c.options
     s, maxval, info = png_as_read(src)
+    opts = c.options
     d = info["density"]
     if d is not None and d[0] != d[1] and _fits_size(c.options):
-        raise Unsupported("non-square pixel density with a fitted size")
+        opts = _density_size(c.options, s.shape[1], s.shape[0], float(d[0]), float(d[1]))
     if info["bkgd"] and "-usebkgdlabel" in c.options:
         raise Unsupported("input background label used as the background")
     ext = {1: "pgm", 3: "ppm"}.get(s.shape[-1], "pam")
     path = os.path.join(tmpdir, "in_" + c.name.rsplit(".", 1)[0].replace("/", "_") + "." + ext)
     _write_pnm(path, s, maxval)
-    return path
+    return path, opts
 
 
 def expected_values(c: Case, tdir: str) -> np.ndarray:
@@ -315,7 +353,7 @@ def run_case(exe: str, c: Case, tdir: str, tmpdir: str) -> tuple[str, str | None
     if c.skip:
         return "skipped", c.skip
     try:
-        inp = prepare_input(c, tdir, tmpdir)
+        inp, opts = prepare_input(c, tdir, tmpdir)
     except Unsupported as e:
         return "skipped", str(e)
     out_ext = "pam" if c.ext == "png" else c.ext
@@ -323,7 +361,7 @@ def run_case(exe: str, c: Case, tdir: str, tmpdir: str) -> tuple[str, str | None
     if os.path.exists(out):
         os.remove(out)
     extra = ["-outfmt", "pam"] if c.ext == "png" else []
-    r = subprocess.run([exe, "-noinfo", "-nowarn", *c.options, *extra, inp, out], capture_output=True, timeout=120)
+    r = subprocess.run([exe, "-noinfo", "-nowarn", *opts, *extra, inp, out], capture_output=True, timeout=120)
     if r.returncode or not os.path.exists(out):
         msg = r.stderr.decode(errors="replace").strip()
         if c.ext == "png" and "requires equal bit depths" in msg:
@@ -341,3 +379,100 @@ def run_case(exe: str, c: Case, tdir: str, tmpdir: str) -> tuple[str, str | None
         n = int(np.count_nonzero(np.any(want != got, axis=-1)))
         return "differ", "%d of %d pixels" % (n, want.shape[0] * want.shape[1])
     return "match", None
+
+
+# --------------------------------------------------------------------------
+# lines replayed through the library API instead of the PNM/PAM tool
+
+def result_values(r) -> np.ndarray:
+    """Exact sample fractions (h, w, 4) of an output image from
+    imageworsener_gb300.iwapi.run_job: palette, colour key and per-channel
+    maximum codes resolved."""
+    from imageworsener_gb300 import iwapi
+    ch = iwapi.num_channels(r.imgtype)
+    row_bytes = r.bpr
+    raw = np.frombuffer(r.pixels, np.uint8).reshape(r.height, row_bytes)
+    n = r.width * ch
+    if r.bit_depth == 16:
+        s = raw[:, :2 * n].copy().view(">u2").astype(np.int64)
+    elif r.bit_depth == 8:
+        s = raw[:, :n].astype(np.int64)
+    else:
+        bits = np.unpackbits(raw, axis=1)[:, :n * r.bit_depth].reshape(r.height, n, r.bit_depth)
+        s = (bits.astype(np.int64) * (1 << np.arange(r.bit_depth - 1, -1, -1))).sum(axis=-1)
+    s = s.reshape(r.height, r.width, ch)
+    if r.imgtype == iwapi.IMGTYPE_PALETTE:
+        pal = np.array(r.palette, np.float64) / 255.0
+        return _rgba(pal[s[..., 0]])
+    types = {iwapi.IMGTYPE_GRAY: [iwapi.CT_GRAY], iwapi.IMGTYPE_GRAYA: [iwapi.CT_GRAY, iwapi.CT_ALPHA],
+             iwapi.IMGTYPE_RGB: [iwapi.CT_RED, iwapi.CT_GREEN, iwapi.CT_BLUE],
+             iwapi.IMGTYPE_RGBA: [iwapi.CT_RED, iwapi.CT_GREEN, iwapi.CT_BLUE, iwapi.CT_ALPHA]}[r.imgtype]
+    top = (1 << r.bit_depth) - 1
+    maxv = np.array([r.reduced_maxcolors[t] if r.reduced_maxcolors else top for t in types], np.float64)
+    v = s / maxv
+    if r.colorkey is not None:
+        key = np.array(r.colorkey[:ch], np.int64)
+        v = np.concatenate([v, np.where(np.all(s == key, axis=-1), 0.0, 1.0)[..., None]], axis=-1)
+    return _rgba(v)
+
+
+def api_jobs(tdir: str, lib) -> dict:
+    """The regression lines whose inputs need library calls that a PNM/PAM
+    file cannot express, as iwapi jobs for ``lib``: input maximum codes per
+    channel from sBIT (src/imagew-png.c:182-226), the input's background label
+    used as the background (src/imagew-png.c:228-250, src/imagew-cmd.c:1302),
+    and output depths per channel (src/imagew-cmd.c:984-1044).  Each follows
+    the front end's order of calls for the line's options; background colours
+    are given in sRGB and linearised by ``lib`` as the front end does
+    (src/imagew-cmd.c:1280-1291)."""
+    import ctypes as C
+    from imageworsener_gb300 import iwapi
+    from pngread import read_png
+    png = PNG_PROFILE
+    srgb = iwapi.Csdescr(iwapi.CS_SRGB, 0, 0.0)
+    lin = lambda x: lib.iw_convert_sample_to_linear(float(x), C.byref(srgb))   # noqa: E731
+
+    def rgba8(name):
+        g = read_png(os.path.join(tdir, "srcimg", name))
+        if g.color_type != 3:
+            return g.samples.astype(np.int64), g
+        rgb = g.palette[g.samples[..., 0]].astype(np.int64)
+        if g.trns is None:
+            return rgb, g
+        a = np.full(len(g.palette), 255, np.int64)
+        a[:len(g.trns)] = np.frombuffer(g.trns, np.uint8)
+        return np.concatenate([rgb, a[g.samples[..., 0]][..., None]], axis=-1), g
+
+    def job(s, calls):
+        h, w, ch = s.shape
+        imgtype = {3: iwapi.IMGTYPE_RGB, 4: iwapi.IMGTYPE_RGBA}[ch]
+        return iwapi.Job(imgtype, 8, w, h, s.astype(np.uint8).tobytes(), calls=calls)
+
+    jobs = {}
+    s, g = rgba8("rgb8a-sbit.png")   # sBIT on RGBA8, no options
+    bits = np.array(g.sbit[:4], np.int64)
+    jobs["sbit1.png"] = job(s >> (8 - bits), [("iw_set_input_max_color_code", k, (1 << int(bits[k])) - 1) for k in range(4)]
+                            + [("iw_set_output_profile", png), ("iw_set_output_canvas_size", g.width, g.height)])
+    s, g = rgba8("p8-sbit.png")      # palette with sBIT: shifted after the expansion
+    bits = np.array(g.sbit[:3], np.int64)
+    jobs["sbit2.png"] = job(s >> (8 - bits), [("iw_set_input_max_color_code", k, (1 << int(bits[k])) - 1) for k in range(3)]
+                            + [("iw_set_output_profile", png), ("iw_set_output_canvas_size", g.width, g.height)])
+    s, g = rgba8("rgb8a.png")        # -width 24 -height 24 -depth 6,8,5,7
+    jobs["sbitw.png"] = job(s, [("iw_set_output_profile", png), ("iw_set_output_depth", 8),
+                                ("iw_set_output_max_color_code", 0, 63), ("iw_set_output_max_color_code", 2, 31),
+                                ("iw_set_output_max_color_code", 3, 127), ("iw_set_output_canvas_size", 24, 24)])
+    s, g = rgba8("p8tbg.png")        # -bkgd 080,008 -checkersize 2 -usebkgdlabel; bKGD = a palette entry
+    label = g.palette[g.bkgd[0]] / 255.0
+    jobs["rbkgd2.png"] = job(s, [("iw_set_input_bkgd_label", *(float(x) for x in label)),
+                                 ("iw_set_output_profile", png),
+                                 ("iw_set_apply_bkgd_2", (lin(0), lin(8 / 15), lin(0), 1.0)),
+                                 ("iw_set_bkgd_checkerboard_2", 2, (lin(0), lin(0), lin(8 / 15), 1.0)),
+                                 ("iw_set_bkgd_checkerboard_origin", 0, 0),
+                                 ("iw_set_value", iwapi.VAL["USE_BKGD_LABEL"], 1),
+                                 ("iw_set_output_canvas_size", g.width, g.height)])
+    return jobs
+
+
+# the reference's PNG output profile (src/imagew-util.c:562-567)
+PNG_PROFILE = 0x0001 | 0x0002 | 0x0004 | 0x0008 | 0x0010 | 0x0020 | 0x0040 | 0x0100 | 0x0200 | 0x0400 | 0x0800 | \
+    0x1000 | 0x8000 | 0x10000

@@ -25,7 +25,7 @@ pytestmark = pytest.mark.skipif(TDIR is None, reason="the reference's regression
 
 REF_CLI = os.path.join(ROOT, "oracle", "_ref", "imagew_ref")
 ORACLE_CLI = os.path.join(ROOT, "oracle", "_build", "imagew_cli_oracle")
-MIN_MATCHED = 150   # of the 196 lines: the rest are other formats or inputs PNM cannot carry
+MIN_MATCHED = 156   # of the 196 lines: 4 more run through the library API below, 36 are other formats
 
 
 def _make(target: str, path: str) -> str:
@@ -90,3 +90,27 @@ def test_oracle_cli_reproduces_reference_expected_files(tmp_path):
     counts, bad = _replay(exe, tmp_path)
     assert not bad, f"{len(bad)} lines differ: {bad[:5]}"
     assert counts["match"] >= MIN_MATCHED, counts
+
+
+def _api_lines(lib) -> list:
+    import numpy as np
+    from imageworsener_gb300.iwapi import run_job
+    bad = []
+    for name, job in refsuite.api_jobs(TDIR, lib).items():
+        r = run_job(lib, job)
+        want = refsuite.png_values(os.path.join(TDIR, "expected", name))
+        if not r.ok or not np.array_equal(want, refsuite.result_values(r)):
+            bad.append((name, r.error))
+    return bad
+
+
+def test_reference_core_reproduces_library_api_lines(reference):
+    """The lines a PNM/PAM file cannot carry (per-channel sBIT in and out, the
+    input's background label as the background), through the library API:
+    the reference core built here reproduces its files, so the jobs are
+    faithful."""
+    assert not _api_lines(reference)
+
+
+def test_oracle_reproduces_library_api_lines(oracle):
+    assert not _api_lines(oracle)
