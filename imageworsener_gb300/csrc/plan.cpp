@@ -191,6 +191,25 @@ static void prepare_bkgd(iw_context *ctx, Plan &P)
 	}
 }
 
+// Whether the reference's allocators would give a buffer of n bytes
+// (iw_malloc) or of n1 x n2 bytes (iw_malloc_large) under the context's
+// allocation limit; sets their error when not.
+static bool ref_fits(iw_context *ctx, size_t n)
+{
+	if(n <= ctx->max_malloc) return true;
+	iw_set_error(ctx, "Out of memory");
+	return false;
+}
+
+static bool ref_fits_large(iw_context *ctx, size_t n1, size_t n2)
+{
+	if(n2 && n1 > ctx->max_malloc / n2) {
+		iw_set_error(ctx, "Image too large to process");
+		return false;
+	}
+	return ref_fits(ctx, n1 * n2);
+}
+
 bool build_plan(iw_context *ctx, Plan &P)
 {
 	int w = ctx->canvas_w, h = ctx->canvas_h;
@@ -430,11 +449,36 @@ bool build_plan(iw_context *ctx, Plan &P)
 		return false;
 	}
 
+	// The reference's buffers and their size limits, checked without
+	// allocating, in its order, before any device work
+	// (src/imagew-main.c:1385-1417, :851-858, :979-985).  This library keeps
+	// its images on the device, but a job the reference refuses is refused
+	// here with the same message: an image whose output or intermediate
+	// exceeds the allocation limit ("Image too large to process"), and a crop
+	// that the reference's clamp leaves with a negative size (a negative
+	// width fails at the intermediate image, a negative height at the
+	// vertical pass's column buffer, "Out of memory").
+	{
+		const size_t mid_px = (size_t)(long long)((long long)P.crop_w * h);   // an int product there
+		if(!ref_fits_large(ctx, P.out_bpr, (size_t)h)) return false;
+		if(!ref_fits_large(ctx, mid_px, sizeof(float))) return false;
+		if(P.errdiff)
+			for(int k = 0; k < 3; k++)
+				if(!ref_fits(ctx, (size_t)w * sizeof(double))) return false;
+		if(IW_IMGTYPE_HAS_ALPHA(P.mid_type)) {
+			if(!ref_fits_large(ctx, mid_px, sizeof(float))) return false;
+			if(!ref_fits_large(ctx, (size_t)(long long)((long long)w * h), sizeof(float))) return false;
+		}
+	}
+
 	// Weight sets.  One per dimension unless a channel offset or an early
 	// background on a transparent edge makes them differ per channel
-	// (src/imagew-main.c:2031-2045).
-	for(int d = 0; d < 2; d++) {
+	// (src/imagew-main.c:2031-2045).  Vertical first, each after its pass's
+	// column buffers, as the reference builds them.
+	for(int d = 1; d >= 0; d--) {
 		int n_in = d == 0 ? P.crop_w : P.crop_h, n_out = d == 0 ? w : h;
+		if(!ref_fits(ctx, (size_t)(long long)n_in * sizeof(double))) return false;
+		if(!ref_fits(ctx, (size_t)n_out * sizeof(double))) return false;
 		P.wsets[d].clear();
 		for(int m = 0; m < P.mid_n; m++) {
 			const MidChannel &mc = P.mid[m];

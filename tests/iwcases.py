@@ -235,3 +235,39 @@ def baseline_small_case(seed: int = 1, w: int = 1024, h: int = 768, ow: int = 51
     calls = [("iw_set_output_profile", PPM), ("iw_set_output_canvas_size", ow, oh)]
     calls += _resize_calls("lanczos", 3, 0)
     return Job(IMGTYPE_RGB, 8, w, h, px, calls=calls)
+
+
+def crop_case(i: int) -> Job:
+    """A small image with a crop drawn to land outside it as often as inside:
+    the reference's clamp then leaves zero or negative sizes (it limits the y
+    origin by moving the x origin), which it refuses at its first buffer of
+    that size or processes as an empty crop."""
+    rng = np.random.default_rng(80_000 + i)
+    w, h = int(rng.integers(1, 12)), int(rng.integers(1, 12))
+    imgtype = [IMGTYPE_RGB, IMGTYPE_GRAY, IMGTYPE_RGBA][i % 3]
+    calls = [("iw_set_output_profile", 0x41),
+             ("iw_set_input_crop", int(rng.integers(-3, 20)), int(rng.integers(-3, 20)),
+              int(rng.integers(-2, 15)), int(rng.integers(-2, 15))),
+             ("iw_set_output_canvas_size", int(rng.integers(1, 15)), int(rng.integers(1, 15)))]
+    fam = str(rng.choice(["auto", "null", "nearest", "mix", "cubic", "lanczos", "box"]))
+    if fam != "auto":
+        for d in (0, 1):
+            calls.append(("iw_set_resize_alg", d, RT[fam], 1.0, 3.0 if fam == "lanczos" else 0.0, 0.5))
+    if i % 5 == 0:
+        calls.append(("iw_set_dither_type", CT_ALL, DITHER_ERRDIFF, 0))
+    px = rng.integers(0, 256, w * h * num_channels(imgtype), dtype=np.uint8).tobytes()
+    return Job(imgtype, 8, w, h, px, calls=calls)
+
+
+def over_limit_cases() -> list[tuple[str, Job]]:
+    """Jobs whose output or intermediate image exceeds the allocation limit
+    (2e9 bytes by default, or a smaller one set by the caller)."""
+    prof = ("iw_set_output_profile", 0x41)
+    return [
+        ("output 30000x30000 RGB", Job(IMGTYPE_RGB, 8, 1, 1, bytes(3), calls=[prof, ("iw_set_output_canvas_size", 30000, 30000)])),
+        ("intermediate 23000x23000", Job(IMGTYPE_GRAY, 8, 23000, 1, bytes(23000),
+                                         calls=[prof, ("iw_set_output_canvas_size", 1, 23000)])),
+        ("alpha intermediate", Job(IMGTYPE_RGBA, 8, 23000, 1, bytes(92000), calls=[prof, ("iw_set_output_canvas_size", 1, 23000)])),
+        ("limit 1e6", Job(IMGTYPE_GRAY, 8, 600, 1, bytes(600),
+                          calls=[prof, ("iw_set_max_malloc", 1000000), ("iw_set_output_canvas_size", 1, 600)])),
+    ]

@@ -87,3 +87,60 @@ def test_planning_errors_match_oracle_without_gpu(gpulib, oracle):
         job = Job(IMGTYPE_RGB, 8, 4, 4, px, calls=calls)
         a, b = run_job(gpulib, job), run_job(oracle, job)
         assert (a.ok, a.error) == (b.ok, b.error)
+
+
+FLOAT_NONLINEAR = "Floating-point input must use a linear input colorspace"
+
+
+@pytest.mark.parametrize("block", range(4))
+def test_planning_warnings_match_oracle_on_random_grid(gpulib, oracle, block):
+    """The library's planning (output type, depth, colour space, background
+    and offset decisions) raises the same warnings as the oracle, in the same
+    order, on the random settings grid.  Without a GPU the run stops after
+    planning with a CUDA error; with one it completes.  The one documented
+    refusal is 32-bit float input in a non-linear colour space."""
+    import iwcases
+    bad = []
+    for seed in range(block * 600, block * 600 + 600):
+        a = run_job(gpulib, iwcases.random_case(seed), keep_warnings=True)
+        b = run_job(oracle, iwcases.random_case(seed), keep_warnings=True)
+        if b.ok:
+            status_ok = a.ok or "CUDA" in (a.error or "") or a.error == FLOAT_NONLINEAR
+        else:
+            status_ok = not a.ok and a.error == b.error
+        if not status_ok or a.warnings != b.warnings:
+            bad.append((seed, a.error, b.error, a.warnings, b.warnings))
+    assert not bad, bad[:3]
+
+
+def _same_refusal(a, b) -> bool:
+    """The library refuses exactly what the oracle refuses, with its message;
+    what the oracle processes gets past planning (to the device, or to a
+    CUDA error where there is none)."""
+    if not b.ok:
+        return not a.ok and a.error == b.error
+    return a.ok or "CUDA" in (a.error or "")
+
+
+def test_crops_outside_the_image_refused_like_oracle(gpulib, oracle):
+    """Crops the reference's clamp leaves with zero or negative sizes: the
+    negative ones are refused while planning, before any device work, with
+    the reference's message; the empty ones are processed."""
+    import iwcases
+    bad, refused = [], 0
+    for i in range(1500):
+        a = run_job(gpulib, iwcases.crop_case(i), keep_warnings=True)
+        b = run_job(oracle, iwcases.crop_case(i), keep_warnings=True)
+        refused += not b.ok
+        if not _same_refusal(a, b) or a.warnings != b.warnings:
+            bad.append((i, a.error, b.error))
+    assert not bad, bad[:5]
+    assert refused > 500
+
+
+def test_images_over_the_allocation_limit_refused_like_oracle(gpulib, oracle):
+    import iwcases
+    for name, job in iwcases.over_limit_cases():
+        a, b = run_job(gpulib, job), run_job(oracle, job)
+        assert not b.ok and b.error == "Image too large to process", name
+        assert (a.ok, a.error) == (b.ok, b.error), name

@@ -80,3 +80,22 @@ def test_oracle_error_cases_match_reference(oracle, reference):
             continue
         assert a.key() == b.key(), (calls, a.error, b.error)
         assert not a.ok
+
+
+def test_oracle_matches_reference_on_crops_outside_the_image(oracle, reference):
+    """The reference's crop clamp can leave zero or negative sizes; it then
+    refuses the job at its first buffer of that size, or processes an empty
+    crop.  Same outcome, message and bytes."""
+    bad = []
+    for i in range(1500):
+        a = run_job(reference, iwcases.crop_case(i), keep_warnings=True)
+        b = run_job(oracle, iwcases.crop_case(i), keep_warnings=True)
+        if a.key() != b.key() or a.warnings != b.warnings:
+            bad.append(i)
+    assert not bad, bad[:10]
+
+
+def test_oracle_matches_reference_over_the_allocation_limit(oracle, reference):
+    for name, job in iwcases.over_limit_cases():
+        a, b = run_job(reference, job), run_job(oracle, job)
+        assert a.key() == b.key(), name
