@@ -221,7 +221,7 @@ def random_case(seed: int, max_dim: int = 48) -> Job:
     return Job(imgtype, depth, w, h, px, bpr=bpr, calls=calls, sampletype=sampletype, orient=orient)
 
 
-def baseline_small_case(seed: int = 1, w: int = 1024, h: int = 768, ow: int = 512, oh: int = 384) -> Job:
+def plain_small_case(seed: int = 1, w: int = 1024, h: int = 768, ow: int = 512, oh: int = 384) -> Job:
     """The plain small workload: 8-bit sRGB RGB, smooth gradients plus uniform
     noise in [-16, 16], Lanczos3 in linear light, 8-bit output, no dither."""
     rng = np.random.default_rng(seed)
