@@ -497,6 +497,14 @@ bool build_plan(iw_context *ctx, Plan &P)
 			else P.mid[m].wset_v = found;
 		}
 	}
+	if(P.crop_w < 1 || P.crop_h < 1) {
+		// A crop that the reference's clamp leaves without rows or columns
+		// (its y origin at the image's height): the reference carries on and
+		// resamples from empty column buffers, reading past their end.  No
+		// device pass is run on an empty source here.
+		iw_set_error(ctx, "Input crop is empty");
+		return false;
+	}
 
 	// decode transfer per intermediate channel: alpha and no-gamma use linear
 	for(int m = 0; m < P.mid_n; m++)

@@ -271,3 +271,22 @@ def over_limit_cases() -> list[tuple[str, Job]]:
         ("limit 1e6", Job(IMGTYPE_GRAY, 8, 600, 1, bytes(600),
                           calls=[prof, ("iw_set_max_malloc", 1000000), ("iw_set_output_canvas_size", 1, 600)])),
     ]
+
+
+def clamped_crop(job: Job) -> tuple[int, int, int, int]:
+    """The crop (x, y, w, h) the reference's clamp gives an upright job
+    (src/imagew-cmd.c:1311-1325 and the library's own clamp, which limits
+    the y origin by moving the x origin)."""
+    cx, cy, cw, ch = [c for c in job.calls if c[0] == "iw_set_input_crop"][0][1:]
+    w, h = job.width, job.height
+    x, y = max(cx, 0), max(cy, 0)
+    if x > w - 1:
+        x = w - 1
+    if y > h - 1:
+        x = h - 1
+    cw = w - x if cw < 0 else cw
+    ch = h - y if ch < 0 else ch
+    cw, ch = max(cw, 1), max(ch, 1)
+    cw = min(cw, w - x)
+    ch = min(ch, h - y)
+    return x, y, cw, ch

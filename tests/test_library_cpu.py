@@ -123,19 +123,27 @@ def _same_refusal(a, b) -> bool:
 
 
 def test_crops_outside_the_image_refused_like_oracle(gpulib, oracle):
-    """Crops the reference's clamp leaves with zero or negative sizes: the
-    negative ones are refused while planning, before any device work, with
-    the reference's message; the empty ones are processed."""
+    """Crops the reference's clamp leaves with zero or negative sizes, all
+    refused while planning, before any device work: the negative ones with
+    the reference's message; the empty ones (which the reference resamples
+    from empty buffers) with "Input crop is empty"."""
     import iwcases
-    bad, refused = [], 0
+    bad, refused, empty = [], 0, 0
     for i in range(1500):
-        a = run_job(gpulib, iwcases.crop_case(i), keep_warnings=True)
+        job = iwcases.crop_case(i)
+        a = run_job(gpulib, job, keep_warnings=True)
         b = run_job(oracle, iwcases.crop_case(i), keep_warnings=True)
         refused += not b.ok
-        if not _same_refusal(a, b) or a.warnings != b.warnings:
+        _, _, cw, ch = iwcases.clamped_crop(job)
+        if b.ok and min(cw, ch) == 0:
+            empty += 1
+            ok = not a.ok and a.error == "Input crop is empty"
+        else:
+            ok = _same_refusal(a, b)
+        if not ok or a.warnings != b.warnings:
             bad.append((i, a.error, b.error))
     assert not bad, bad[:5]
-    assert refused > 500
+    assert refused > 500 and empty > 20
 
 
 def test_images_over_the_allocation_limit_refused_like_oracle(gpulib, oracle):
