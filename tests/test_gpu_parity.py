@@ -113,3 +113,30 @@ def test_stats_report_form(gpulib):
         if form == "fp32":
             assert st.flagged < 0.05 * 250 * 250
             assert 0 <= st.flagged_exact <= st.flagged
+
+
+def test_crops_inside_and_outside_the_image(gpulib, oracle):
+    """Crops drawn to land outside the image as often as inside: the ones the
+    oracle processes give the oracle's bytes on the GPU; the ones the
+    reference refuses (negative clamped sizes) are refused with its message,
+    and crops that clamp to nothing with "Input crop is empty" -- all while
+    planning, before any device work."""
+    bad = []
+    for i in range(400):
+        job = iwcases.crop_case(i)
+        a = run_job(gpulib, job, keep_warnings=True)
+        b = run_job(oracle, iwcases.crop_case(i), keep_warnings=True)
+        _, _, cw, ch = iwcases.clamped_crop(job)
+        if b.ok and min(cw, ch) == 0:
+            ok = not a.ok and a.error == "Input crop is empty"
+        else:
+            ok = a.key() == b.key()
+        if not ok or a.warnings != b.warnings:
+            bad.append((i, a.error, b.error))
+    assert not bad, bad[:5]
+
+
+def test_images_over_the_allocation_limit_refused(gpulib, oracle):
+    for name, job in iwcases.over_limit_cases():
+        a, b = run_job(gpulib, job), run_job(oracle, job)
+        assert (a.ok, a.error) == (b.ok, b.error) == (False, "Image too large to process"), name
