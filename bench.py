@@ -26,8 +26,9 @@ gb300 arm (default):
 
 reference arm (--impl reference): the reference's CPU code on all host cores
   (the reference build when present, else the oracle port), one context per
-  thread, each step = every thread processing a 1/4-height strip of the
-  workload (same filter and scale factor, 250 output rows).
+  thread, each step = every thread processing one full image of the same
+  workload (the reference cannot split an image); same "config" object as
+  the gb300 arm.
 
 Multi-GPU: the pipeline does not shard within an image; N ranks run N
 independent replicas (weak scaling), value = all ranks' output pixels / the
@@ -264,24 +265,24 @@ def golden_digest(name):
         return None
 
 
-def strip_job(job, frac_rows: int = 4):
-    """The reference arm's sample: the top 1/frac of the image with the same
-    scale factor (same filter, output height / frac)."""
-    h = job.height // frac_rows
-    calls = []
-    for c in job.calls:
-        if c[0] == "iw_set_output_canvas_size":
-            c = (c[0], c[1], max(1, c[2] // frac_rows))
-        calls.append(c)
-    from imageworsener_gb300.iwapi import Job
-    return Job(job.imgtype, job.bit_depth, job.width, h, job.pixels[: job.bpr * h], bpr=job.bpr, calls=calls)
+def workload_config(name: str, job, world: int) -> dict:
+    """The "config" object of both arms' JSON lines: the workload by its
+    sizes.  The two arms print the same object, so the driver sees one
+    configuration; how each arm spreads it over its hardware (replicas on
+    GPUs, contexts on host threads) is reported beside it."""
+    return {"workload": name, "input": f"{job.width}x{job.height} x{len(job.pixels) // (job.width * job.height)}B/px",
+            "output_px": W.out_pixels(job), "parallelism": f"replicas x{world}",
+            "l2": "input (134 MB) larger than L2; passes back to back" if name == "precision" else "per workload"}
 
 
 def run_reference_arm(args, rank, world):
+    """The reference's CPU implementation on the full workload: every step,
+    each of the host's threads runs one whole image through its own context
+    (the reference cannot split one image), so a step produces threads x the
+    workload's output pixels.  Under torchrun only rank 0 runs."""
     if rank != 0:
         return 0
     job = WORKLOADS[args.workload]()
-    sample = strip_job(job, 4)
     ref_so = os.path.join(ROOT, "oracle", "_ref", "libimagew_ref.so")
     if os.path.exists(ref_so):
         lib, kind = IWLib(ref_so), "reference"
@@ -289,10 +290,16 @@ def run_reference_arm(args, rank, world):
         subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "port"], check=True)
         lib, kind = IWLib(os.path.join(ROOT, "oracle", "_build", "liboracle_iw.so")), "port"
     threads = os.cpu_count() or 1
-    out_px = W.out_pixels(sample)
-    times = []
+    out_px = W.out_pixels(job)
+    gold = golden_digest(args.workload)
+    times, digests = [], []
     for s in range(args.warmup + args.steps):
-        ths = [threading.Thread(target=run_job, args=(lib, sample)) for _ in range(threads)]
+        res = [None] * threads
+
+        def one(k):
+            res[k] = run_job(lib, job)
+
+        ths = [threading.Thread(target=one, args=(k,)) for k in range(threads)]
         t0 = time.perf_counter()
         for t in ths:
             t.start()
@@ -301,17 +308,21 @@ def run_reference_arm(args, rank, world):
         dt = time.perf_counter() - t0
         if s >= args.warmup:
             times.append(dt)
+        if s == 0:
+            digests = [r.digest() for r in res]
     ms = 1000.0 * statistics.mean(times)
     value = threads * out_px / 1e6 / (ms / 1000.0)
+    sample = (f"{threads} host threads, each one full {job.width}x{job.height} image of the workload "
+              f"({out_px} output px) through its own context, per step")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "Mpix/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": args.workload, "sample": f"{threads} threads x one {sample.width}x{sample.height} strip "
-                   f"-> {out_px} output px each", "threads": threads},
-        "cpu_baseline": {"value": value, "unit": "Mpix/s", "cores": threads, "kind": kind,
-                         "sample": f"{threads} concurrent contexts, each a 1/4-height strip of the workload"},
+        "config": workload_config(args.workload, job, world),
+        "threads": threads,
+        "cpu_baseline": {"value": value, "unit": "Mpix/s", "cores": threads, "kind": kind, "sample": sample},
         "e2e": {"value": value, "unit": "Mpix/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "bit_exact": {"reference": all(d == gold for d in digests), "golden": gold is not None},
     }
     print(json.dumps(line), flush=True)
     return 0
@@ -482,7 +493,22 @@ def serving_leg(lib: IWLib, rate: float, seconds: float, thumbs, ups):
                   "post": med([ph[k][3] - ph[k][2] for k in keys if k in ph])}
         return {"n": len(v), "p50_ms": v[len(v) // 2] if v else None,
                 "p99_ms": v[min(len(v) - 1, int(0.99 * len(v)))] if v else None, "stage_p50_ms": stages}
+    def windows(span=10.0):
+        """Latency by arrival window: a backlog that grows shows as a rising p99."""
+        out = []
+        nwin = int(seconds // span + (1 if seconds % span else 0))
+        for w in range(nwin):
+            keys = [k for k in snap if w * span <= sched[k][0] < (w + 1) * span]
+            v = sorted(snap[k][0] for k in keys)
+            ed = sorted(snap[k][0] for k in keys if sched[k][2] and sched[k][1] == "up")
+            q = lambda xs, f: xs[min(len(xs) - 1, int(f * len(xs)))] if xs else None
+            out.append({"from_s": w * span, "n": len(v), "p50_ms": q(v, 0.5), "p99_ms": q(v, 0.99),
+                        "errdiff_up_p50_ms": q(ed, 0.5), "errdiff_up_p99_ms": q(ed, 0.99)})
+        return out
+    last_submit = max((t for t, _, _ in sched), default=0.0)
+    done_at = [sched[k][0] + snap[k][0] / 1000.0 for k in snap]
     return {"rate_req_s": rate, "seconds": seconds, "requests": len(sched), "completed": len(snap),
+            "windows_10s": windows(), "drain_after_last_arrival_s": (max(done_at) - last_submit) if done_at else None,
             "failed": sum(1 for v in snap.values() if not v[1]),
             "errdiff_requests": sum(1 for x in sched if x[2]), "upscale_requests": sum(1 for x in sched if x[1] == "up"),
             "p50_ms": pct(0.50), "p90_ms": pct(0.90), "p99_ms": pct(0.99), "max_ms": ls[-1] if ls else None,
@@ -511,7 +537,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--batch-images", type=int, default=4096, help="batched leg: contexts per call (0: skip)")
     ap.add_argument("--batch-pool", type=int, default=256, help="batched leg: distinct generated images")
-    ap.add_argument("--serve-seconds", type=float, default=10.0, help="serving leg: length of the arrival stream (0: skip)")
+    ap.add_argument("--serve-seconds", type=float, default=60.0, help="serving leg: length of the arrival stream (0: skip)")
     ap.add_argument("--serve-rate", type=float, default=2000.0, help="serving leg: requests per second")
     ap.add_argument("--no-large", action="store_true", help="skip the large-downscale leg")
     args = ap.parse_args()
@@ -611,9 +637,7 @@ def main():
         "metric": METRIC, "value": value, "unit": "Mpix/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "fp32 (fp64 guard)", "data": "synthetic",
-        "config": {"workload": args.workload, "input": f"{job.width}x{job.height} x{len(job.pixels) // (job.width * job.height)}B/px",
-                   "output_px": out_px, "parallelism": f"replicas x{world}",
-                   "l2": "input (134 MB) larger than L2; passes back to back"},
+        "config": workload_config(args.workload, job, world),
         "e2e": {"value": world * out_px / 1e6 / (e2e_ms / 1000.0), "unit": "Mpix/s", "h2d_bytes_per_step": in_bytes,
                 "d2h_bytes_per_step": out_bytes, "ms_per_step": e2e_ms, "p50_ms": 1000 * statistics.median(e2e_times),
                 "host_buffers": "pageable (caller-malloc'd, as the libimagew ownership model requires)",

@@ -471,6 +471,25 @@ bool build_plan(iw_context *ctx, Plan &P)
 		}
 	}
 
+	// A crop that the reference's clamp leaves without rows or columns (its y
+	// origin at the image's height): the reference carries on and resamples
+	// from empty column buffers, reading past their end.  It is refused here,
+	// before any weight list is built on an empty source, whenever both
+	// passes' column buffers fit the allocation limit (when one does not, the
+	// loop below reports the reference's own error first).
+	{
+		auto fits = [&](size_t n) { return n <= ctx->max_malloc; };
+		bool cols_fit = true;
+		for(int d = 1; d >= 0; d--) {
+			int n_in = d == 0 ? P.crop_w : P.crop_h, n_out = d == 0 ? w : h;
+			cols_fit = cols_fit && fits((size_t)(long long)n_in * sizeof(double)) && fits((size_t)n_out * sizeof(double));
+		}
+		if(cols_fit && (P.crop_w < 1 || P.crop_h < 1)) {
+			iw_set_error(ctx, "Input crop is empty");
+			return false;
+		}
+	}
+
 	// Weight sets.  One per dimension unless a channel offset or an early
 	// background on a transparent edge makes them differ per channel
 	// (src/imagew-main.c:2031-2045).  Vertical first, each after its pass's
@@ -498,10 +517,8 @@ bool build_plan(iw_context *ctx, Plan &P)
 		}
 	}
 	if(P.crop_w < 1 || P.crop_h < 1) {
-		// A crop that the reference's clamp leaves without rows or columns
-		// (its y origin at the image's height): the reference carries on and
-		// resamples from empty column buffers, reading past their end.  No
-		// device pass is run on an empty source here.
+		// (the check before the weight lists refuses these first; this one
+		// stays so that no device pass can ever see an empty source)
 		iw_set_error(ctx, "Input crop is empty");
 		return false;
 	}

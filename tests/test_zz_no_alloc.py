@@ -2,8 +2,9 @@
 
 Each case runs the same image through iw_process_image() (the library's
 ordinary entry point, output post-pass options off so the image keeps its
-type, except the one that packs a gray result back to gray) and through iwg_resize_u8_noalloc() twice in a row, and requires
-identical bytes.  Integer output, so the tolerance is zero.  This file sorts
+type, except the one that packs a gray result back to gray), through the CPU
+oracle with the same settings, and through iwg_resize_u8_noalloc() twice in
+a row, and requires identical bytes.  Integer output, so the tolerance is zero.  This file sorts
 last so it also runs after every other GPU test in one session.
 """
 from __future__ import annotations
@@ -78,7 +79,7 @@ def _call(f, torch, case, src, src_bpr, dst, dst_bpr):
 
 
 @pytest.mark.parametrize("case", CASES, ids=lambda c: f"{c[0]:#x}-{c[1]}x{c[2]}-{c[3]}x{c[4]}-{c[5]}")
-def test_noalloc_matches_process_image(gpulib, torch_cuda, case):
+def test_noalloc_matches_process_image(gpulib, oracle, torch_cuda, case):
     torch = torch_cuda
     f = _bind(gpulib)
     imgtype, sw, sh, dw, dh = case[:5]
@@ -86,6 +87,9 @@ def test_noalloc_matches_process_image(gpulib, torch_cuda, case):
     rng = np.random.default_rng(sw * 7919 + sh * 31 + dw)
     pixels, bpr = make_pixels(rng, imgtype, 8, sw, sh)
     exp = _expected(gpulib, case, pixels, bpr)
+    # the same job through the CPU oracle: the comparison below is then with
+    # the reference's arithmetic directly, not only with this library
+    assert _expected(oracle, case, pixels, bpr).pixels == exp.pixels, "iw_process_image differs from the oracle"
     src = torch.from_numpy(np.frombuffer(pixels, dtype=np.uint8).copy()).cuda()
     dst_bpr = exp.bpr
     assert dst_bpr == dw * nch
@@ -155,3 +159,28 @@ def test_noalloc_rejects_oversize_and_bad_args(gpulib, torch_cuda):
     ok = f(src.data_ptr(), 20000, 1, 80000, dst.data_ptr(), 4, 4, 16, IMGTYPE_RGBA, RT["cubic"], 0.0, 0.5,
            CS_SRGB, 0.0, None, msg, 256)
     assert ok == 0 and b"dimensions" in msg.value
+
+
+def test_noalloc_allocates_nothing(gpulib, torch_cuda):
+    """After the first call on the device (which resolves the scratch
+    array), further calls leave the device's free memory unchanged: nothing
+    is allocated on the device (a cudaMalloc takes at least one 2 MiB page)."""
+    torch = torch_cuda
+    f = _bind(gpulib)
+    case = CASES[1]
+    imgtype, sw, sh, dw, dh = case[:5]
+    rng = np.random.default_rng(4242)
+    pixels, bpr = make_pixels(rng, imgtype, 8, sw, sh)
+    nch = num_channels(imgtype)
+    src = torch.from_numpy(np.frombuffer(pixels, dtype=np.uint8).copy()).cuda()
+    dst = torch.zeros((dw * nch * dh,), dtype=torch.uint8, device="cuda")
+    _call(f, torch, case, src.data_ptr(), bpr, dst.data_ptr(), dw * nch)
+    torch.cuda.synchronize()
+    first = dst.cpu().numpy().tobytes()
+    free0 = torch.cuda.mem_get_info()[0]
+    for _ in range(5):
+        _call(f, torch, case, src.data_ptr(), bpr, dst.data_ptr(), dw * nch)
+    torch.cuda.synchronize()
+    free1 = torch.cuda.mem_get_info()[0]
+    assert free1 == free0, f"device free memory changed by {free0 - free1} bytes across calls"
+    assert dst.cpu().numpy().tobytes() == first
