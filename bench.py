@@ -49,6 +49,9 @@ import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
+# the library's device lanes each want a hardware queue; this must be set
+# before the process creates its CUDA context (torch does so first here)
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 
 from imageworsener_gb300 import workloads as W  # noqa: E402
 from imageworsener_gb300.iwapi import IWLib, Image, run_job, _convert_arg, _libc  # noqa: E402
@@ -65,7 +68,8 @@ WORKLOADS = {
 class Stats(C.Structure):
     _fields_ = [("ms_total", C.c_double), ("ms_device", C.c_double), ("ms_part", C.c_double * 4),
                 ("flagged", C.c_longlong), ("form", C.c_int), ("kernels", C.c_int), ("zero_copy", C.c_int),
-                ("flagged_exact", C.c_longlong), ("vertical_tensor", C.c_int), ("graph", C.c_int)]
+                ("flagged_exact", C.c_longlong), ("vertical_tensor", C.c_int), ("graph", C.c_int),
+                ("fused", C.c_int), ("ms_phase", C.c_double * 6)]
 
 
 _T0 = time.perf_counter()
@@ -216,7 +220,7 @@ def e2e_timed(lib: IWLib, job, warmup: int, steps: int, extra_calls=()):
     timed region; contexts are destroyed after it."""
     lib.dll.iwg_get_stats.argtypes = [C.c_void_p, C.POINTER(Stats)]
     n = job.bpr * job.height
-    times, dig, zc = [], None, {}
+    times, dig, zc, phases = [], None, {}, []
     for s in range(warmup + steps):
         buf = _libc.malloc(n)
         C.memmove(buf, job.pixels, n)
@@ -234,16 +238,22 @@ def e2e_timed(lib: IWLib, job, warmup: int, steps: int, extra_calls=()):
         t1 = time.perf_counter()
         if not ok:
             raise RuntimeError("iw_process_image failed")
+        st = Stats()
+        lib.dll.iwg_get_stats(ctx, C.byref(st))
         if s == warmup + steps - 1:
             dig = output_digest(lib, ctx)
-            st = Stats()
-            lib.dll.iwg_get_stats(ctx, C.byref(st))
             zc = {"zero_copy": st.zero_copy, "device_ms": st.ms_device,
                   "kernel_ms": {"vertical": st.ms_part[0], "horizontal": st.ms_part[1], "fixup": st.ms_part[2]},
                   "host_ms_total": st.ms_total}
         lib.iw_destroy_context(ctx)
         if s >= warmup:
             times.append(t1 - t0)
+            phases.append(list(st.ms_phase))
+    if phases:
+        med = [statistics.median(p[k] for p in phases) for k in range(6)]
+        zc["phase_ms_median"] = {"plan": med[0], "h2d": med[1], "device": med[2], "d2h": med[3], "post_pass": med[4],
+                                 "device_part_wall": med[5]}
+        zc["h2d_GBps"] = n / 1e6 / med[1] if med[1] > 0 else None
     return times, dig, zc
 
 
@@ -527,6 +537,40 @@ def serving_leg(lib: IWLib, rate: float, seconds: float, thumbs, ups):
                                                  list(info.batch_phase_ms)))}}
 
 
+def fp_error_leg(lib: IWLib, job, name: str) -> dict:
+    """Max / RMS error of the fp32 form's linear-light values against the
+    fp64 form's (the reference's arithmetic), per configuration: the float
+    intermediate after the vertical pass and the value each output sample is
+    quantised from, with the flagged fraction and the count of samples
+    beyond the fp32 form's own bound (0 expected).  The batched entry pools
+    16 images of the batched configuration that the fp32 form takes."""
+    from imageworsener_gb300.iwapi import fp_error
+    out = {name: fp_error(lib, job)}
+    for other in ("small", "downscale"):
+        if other != name:
+            out[other] = fp_error(lib, WORKLOADS[other]())
+    agg = {"images": 0, "interm_max": 0.0, "final_max": 0.0, "bound_violations": 0, "samples": 0,
+           "final_sq": 0.0, "flagged_px": 0.0, "px": 0}
+    for j in W.batch(16, seed=4):
+        st = fp_error(lib, j)
+        if st.get("form") != 1 or "interm_max" not in st:
+            continue
+        agg["images"] += 1
+        for k in ("interm_max", "final_max"):
+            agg[k] = max(agg[k], st[k])
+        agg["bound_violations"] += st["bound_violations"]
+        agg["final_sq"] += st["final_rms"] ** 2 * st["samples"]
+        agg["samples"] += st["samples"]
+        px = W.out_pixels(j)
+        agg["flagged_px"] += st["flagged_fraction"] * px
+        agg["px"] += px
+    out["batched_sample"] = {"images": agg["images"], "interm_max": agg["interm_max"], "final_max": agg["final_max"],
+                             "final_rms": (agg["final_sq"] / agg["samples"]) ** 0.5 if agg["samples"] else None,
+                             "bound_violations": agg["bound_violations"],
+                             "flagged_fraction": agg["flagged_px"] / agg["px"] if agg["px"] else None}
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -577,11 +621,12 @@ def main():
         progress("end to end")
         e2e_times, dig_e2e, e2e_zc = e2e_timed(lib, job, max(3, args.warmup), max(3, min(args.steps, 20)))
         e2e_modes = {}
-        for mode in ("zero", "stage", "copy"):
+        for mode in ("zero", "stage", "copy", "pull"):
             progress(f"end to end, transfer {mode}")
             tm, dg, info = e2e_timed(lib, job, 2, 5, [("iw_set_option", b"gpu:upload", mode.encode())])
             e2e_modes[mode] = {"ms_per_step": 1000.0 * statistics.mean(tm), "bit_exact": dg == gold,
-                               "device_ms": info.get("device_ms")}
+                               "device_ms": info.get("device_ms"), "phase_ms_median": info.get("phase_ms_median"),
+                               "h2d_GBps": info.get("h2d_GBps")}
         barrier()
         batched = None
         if args.batch_images > 0:
@@ -602,6 +647,8 @@ def main():
                             "vertical_tensor": lst.vertical_tensor, "flagged": lst.flagged,
                             "left_to_fp64": lst.flagged_exact, "kernel_ms": list(lst.ms_part)[:3],
                             "bit_exact": ldig == golden_digest(name)}
+        progress("fp error of the fp32 form against fp64, per configuration")
+        fp_err = fp_error_leg(lib, job, args.workload)
         serving = None
         if args.serve_seconds > 0:
             progress("serving configuration")
@@ -642,7 +689,8 @@ def main():
                 "d2h_bytes_per_step": out_bytes, "ms_per_step": e2e_ms, "p50_ms": 1000 * statistics.median(e2e_times),
                 "host_buffers": "pageable (caller-malloc'd, as the libimagew ownership model requires)",
                 "transfer": "zero-copy (GPU reads/writes host memory over NVLink-C2C)" if e2e_zc.get("zero_copy") else
-                            "cudaMemcpyAsync from / to the caller's pageable buffers (default for one image)",
+                            "default: a copy kernel pulls the caller's pageable input over NVLink-C2C into device "
+                            "memory; the output comes back by cudaMemcpyAsync",
                 "step_ms": [round(1000 * t, 3) for t in e2e_times],
                 "last_call": e2e_zc, "by_transfer_mode": e2e_modes},
         "roofline": {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -660,6 +708,7 @@ def main():
                       "golden": gold is not None},
         "batched": batched,
         "serving": serving,
+        "fp_error": fp_err,
         "other_configs": large,
         "gpu_launches": st.kernels * args.steps,
         "clocks": clk.summary(),

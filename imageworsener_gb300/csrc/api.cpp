@@ -641,13 +641,21 @@ int iw_process_image(struct iw_context *ctx)
 		return 0;
 	}
 	ctx->use_count++;
-	auto t0 = std::chrono::steady_clock::now();
+	using Clk = std::chrono::steady_clock;
+	auto ms = [](Clk::time_point a, Clk::time_point b) { return std::chrono::duration<double, std::milli>(b - a).count(); };
+	const auto t0 = Clk::now();
 	iwg::Plan P;
 	if(!iwg::build_plan(ctx, P)) return 0;
+	const auto t1 = Clk::now();
 	if(!iwg::run_pipeline(ctx, P)) return 0;
+	const auto t2 = Clk::now();
 	iwg::bkgd_label(ctx, P);
 	iwg::optimize(ctx);
-	ctx->stats.ms_total = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+	const auto t3 = Clk::now();
+	ctx->stats.ms_phase[0] = ms(t0, t1);
+	ctx->stats.ms_phase[4] = ms(t2, t3);
+	ctx->stats.ms_phase[5] = ms(t1, t2);
+	ctx->stats.ms_total = ms(t0, t3);
 	return 1;
 }
 

@@ -95,6 +95,10 @@ struct Job {
 	const float2 *df_tab[kMaxCh];
 	const float2 *df_atab;
 	const float2 *df_wv, *df_wh;
+
+	// debug readback (null normally): the value each output sample is
+	// quantised from, [out_n][out_h][out_w] (plain form)
+	double *dbg;
 };
 
 // ---- double-float ("df") arithmetic ----

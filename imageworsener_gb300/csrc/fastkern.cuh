@@ -90,9 +90,16 @@ struct FJob {
 	// flags
 	int *flag_count;
 	int *flag_list;            // entries (pixel, mask, image, 0)
+	int flag_cap;              // entries the list holds
 	int img;                   // index of the image in a batch (0 alone)
 	int *err_flag;             // set by a kernel whose bounded wait ran out
+	int wait_polls;            // polls of a pipeline wait before it gives up (kWaitPolls; failure tests shorten it)
+	int starve;                // failure tests: the producer issues no copies, so every pipeline wait runs out
 	int vgx, vgy, hgx;         // blocks of the vertical pass (x, bands or rows), horizontal pass (x)
+	// debug readback (null normally): per output sample, the FP32 value the
+	// tail quantises and its error bound, [2][out_n][out_h][out_w]; NaN where
+	// the tail decided without a value (blackened, undecidable alpha)
+	float *dbg;
 };
 static_assert(sizeof(FJob) <= 4096, "FJob is passed by value as a kernel parameter");
 
@@ -337,10 +344,15 @@ __device__ __forceinline__ void mbar_arrive(unsigned long long *bar)
 }
 
 // Waits for the phase of 'parity' to complete; gives up (false) after a
-// bounded number of polls (each poll may suspend the thread briefly).
-__device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned parity)
+// bounded number of polls (each poll may suspend the thread briefly).  The
+// pipeline's waits take the job's limit (FJob::wait_polls: a failure test
+// shortens it); the final wait for a block's own copies in flight always
+// takes the full limit.
+constexpr int kWaitPolls = 1 << 21;
+
+__device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned parity, int polls = kWaitPolls)
 {
-	for(int it = 0; it < (1 << 21); it++) {
+	for(int it = 0; it < polls; it++) {
 		unsigned done;
 		asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
 			: "=r"(done) : "r"(smem_u32(bar)), "r"(parity) : "memory");
@@ -414,9 +426,9 @@ __device__ __forceinline__ void vbulk_tile(const FJob &F, unsigned char *s_raw, 
 		const int last_row = F.in_rows - 1;
 		int issued = 0;
 		bool ok = true;
-		for(int q = 0; q < nq && ok; q++) {
+		for(int q = 0; q < nq && ok && !F.starve; q++) {
 			const int st = q % kBulkStages, use = q / kBulkStages;
-			if(use > 0 && !mbar_wait(empty + st, (use - 1) & 1)) { ok = false; break; }
+			if(use > 0 && !mbar_wait(empty + st, (use - 1) & 1, F.wait_polls)) { ok = false; break; }
 			if(*(volatile int *)abort_flag) { ok = false; break; }
 			const int row = min(max(p0 + q, 0), last_row);
 			mbar_expect_tx(full + st, bytes);
@@ -450,7 +462,7 @@ __device__ __forceinline__ void vbulk_tile(const FJob &F, unsigned char *s_raw, 
 
 	for(int q = 0; q < nq; q++) {
 		const int st = q % kBulkStages, use = q / kBulkStages;
-		if(!mbar_wait(full + st, use & 1)) {
+		if(!mbar_wait(full + st, use & 1, F.wait_polls)) {
 			atomicExch(F.err_flag, 1);
 			*(volatile int *)abort_flag = 1;
 			return;
@@ -518,6 +530,234 @@ __device__ __forceinline__ void vbulk_tile(const FJob &F, unsigned char *s_raw, 
 				}
 			}
 		}
+	}
+}
+
+// ---------------------------------------------------------------------------
+// Fused vertical + horizontal pass (one launch, no intermediate image in
+// device memory).  A block owns a tile of output columns [i0, i1) and a band
+// of output rows.  Its producer warp streams the rows of the input columns
+// the tile's horizontal windows read ([xa, xa + nc)) into a shared-memory
+// ring with bulk copies (as vbulk_tile); the consumers decode and accumulate
+// the vertical sums exactly as vbulk_tile does (same operations, same order,
+// so the same float intermediates), but a finished intermediate row goes to
+// a small ring of rows in shared memory instead of device memory.  Every
+// second finished row, the consumers synchronise and run the horizontal sums
+// and the guarded quantisation tail of those rows' output pixels from shared
+// memory (same operations and order as hpass_pixel, so the same values,
+// bounds, codes and flags as the two-kernel form).
+// Requirements (checked by the host): at most one output row finishes per
+// input position (downscales), the tile's input columns fit one strip of
+// kBulkConsumers * PX pixels, every horizontal source of the tile lies in
+// [xa, xa + nc), rows 16-byte aligned, nc * bytes per pixel a multiple of 16.
+// ---------------------------------------------------------------------------
+template<int NPL>
+__device__ __forceinline__ void hpass_tail(const FJob &F, int i, int j, const float (&v)[NPL], const float (&T)[NPL]);
+
+struct FuseTile {
+	int xa, nc;       // first input column of the tile's strip, columns
+	int i0, i1;       // output columns
+};
+constexpr int kFuseRows = 4;   // intermediate rows in shared memory (two being summed, two filling)
+
+template<int NS, int NCH, bool ALPHA, int DEPTH, int PX>
+__device__ __forceinline__ void vhfuse_tile(const FJob &F, const FuseTile *tiles, unsigned char *s_raw, int tile, int band)
+{
+	constexpr int BPP = NCH * (DEPTH / 8);
+	constexpr int NW = PX * BPP / 4;
+	static_assert(NW == 4, "one 16-byte group per consumer and row");
+	static_assert(NCH == 4, "the row ring holds one float4 per column");
+	constexpr int STRIP = kBulkConsumers * PX * BPP;
+	constexpr int MIDW = kBulkConsumers * PX;              // columns of a ring row
+	unsigned char *ring = s_raw;                           // kBulkStages * STRIP
+	float4 *mid = reinterpret_cast<float4 *>(s_raw + kBulkStages * STRIP);   // kFuseRows * MIDW
+	unsigned char *after = s_raw + kBulkStages * STRIP + (size_t)kFuseRows * MIDW * sizeof(float4);
+	unsigned long long *full = reinterpret_cast<unsigned long long *>(after);
+	unsigned long long *empty = full + kBulkStages;
+	int *abort_flag = reinterpret_cast<int *>(empty + kBulkStages);
+	float *s_tab = reinterpret_cast<float *>(after + 256);
+	const FuseTile T = tiles[tile];
+	const int jb = band * F.rows_per_band;
+	const int je = min(jb + F.rows_per_band, F.mid_h);
+	if(jb >= je) return;
+	const int p0 = F.first_pos[jb], p1 = F.last_pos[je - 1];
+	const int nq = p1 - p0 + 1;
+	float *s_w = s_tab + F.dec_tab_floats;
+	int2 *s_fin = reinterpret_cast<int2 *>(s_w + (size_t)nq * NS);
+	for(int k = threadIdx.x; k < F.dec_tab_floats; k += blockDim.x) s_tab[k] = F.dec_tab[k];
+	for(int k = threadIdx.x; k < nq * NS; k += blockDim.x) {
+		const int q = k / NS, sl = k - q * NS;
+		s_w[k] = F.sw[(size_t)(p0 - F.pmin + q) * 8 + sl];
+	}
+	for(int k = threadIdx.x; k < nq; k += blockDim.x) s_fin[k] = F.pinfo[p0 - F.pmin + k];
+	if(threadIdx.x == 0) {
+		for(int k = 0; k < kBulkStages; k++) {
+			mbar_init(full + k, 1);
+			mbar_init(empty + k, kBulkConsumers / 32);
+		}
+		*abort_flag = 0;
+		asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+	}
+	__syncthreads();
+
+	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+	if(warp == kBulkConsumers / 32) {
+		// producer
+		if(lane != 0) return;
+		const uint8_t *base = F.in + (size_t)(F.crop_x + T.xa) * BPP + (unsigned long long)F.crop_y * F.in_bpr;
+		const unsigned bytes = (unsigned)(T.nc * BPP);
+		const int last_row = F.in_rows - 1;
+		int issued = 0;
+		bool ok = true;
+		for(int q = 0; q < nq && ok && !F.starve; q++) {
+			const int st = q % kBulkStages, use = q / kBulkStages;
+			if(use > 0 && !mbar_wait(empty + st, (use - 1) & 1, F.wait_polls)) { ok = false; break; }
+			if(*(volatile int *)abort_flag) { ok = false; break; }
+			const int row = min(max(p0 + q, 0), last_row);
+			mbar_expect_tx(full + st, bytes);
+			bulk_g2s(ring + (size_t)st * STRIP, base + (unsigned long long)row * F.in_bpr, bytes, full + st);
+			issued = q + 1;
+		}
+		if(!ok) {
+			atomicExch(F.err_flag, 1);
+			*(volatile int *)abort_flag = 1;
+		}
+		// every issued copy lands before the block's shared memory goes away
+		for(int q = max(0, issued - kBulkStages); q < issued; q++) mbar_wait(full + q % kBulkStages, (q / kBulkStages) & 1);
+		return;
+	}
+
+	// consumers
+	const int x0 = threadIdx.x * PX;                  // first column of this thread (tile-local)
+	const bool any = x0 < T.nc;
+	const float ainv = F.alpha_inv;
+	static_assert(PX == 2, "accumulators pair the thread's two pixels");
+	static_assert(NS == 4, "one 16-byte load of the slot weights per row");
+	unsigned long long acc[NS][NCH];
+#pragma unroll
+	for(int s = 0; s < NS; s++)
+#pragma unroll
+		for(int c = 0; c < NCH; c++) acc[s][c] = 0ULL;
+	const int tw = T.i1 - T.i0;
+	int pending = 0, jh = jb;                         // finished rows not yet summed horizontally, the first of them
+	bool failed = false;
+
+	// Horizontal sums + tail of the output pixels of rows jh .. jh + nrows - 1
+	// (a consumer barrier first: their intermediate rows are complete).
+	auto horizontal = [&](int nrows) {
+		asm volatile("bar.sync 1, %0;" ::"n"(kBulkConsumers) : "memory");
+		for(int k = threadIdx.x; k < nrows * tw; k += kBulkConsumers) {
+			const int r = k / tw;
+			const int j = jh + r, i = T.i0 + (k - r * tw);
+			const float4 *row = mid + (size_t)(j % kFuseRows) * MIDW;
+			float v[NCH], Tm[NCH];
+#pragma unroll
+			for(int c = 0; c < NCH; c++) { v[c] = 0.0f; Tm[c] = 0.0f; }
+			const int t0 = __ldg(F.hoff + i), t1 = __ldg(F.hoff + i + 1);
+			// blocked sums in hpass_pixel's order (partial sums of kHBlock taps)
+			int t = t0;
+			while(t < t1) {
+				const int tb = min(t + kHBlock, t1);
+				float pp[NCH];
+#pragma unroll
+				for(int c = 0; c < NCH; c++) pp[c] = 0.0f;
+				for(; t < tb; t++) {
+					const int src = __ldg(F.hsrc + t);
+					if(src < 0) continue;   // transparent edge: value 0
+					const float w = __ldg(F.hw + t), aw = fabsf(w);
+					const float4 I4 = row[src - T.xa];
+					const float I[4] = {I4.x, I4.y, I4.z, I4.w};
+#pragma unroll
+					for(int c = 0; c < NCH; c++) {
+						pp[c] = __fmaf_rn(I[c], w, pp[c]);
+						Tm[c] = __fmaf_rn(fabsf(I[c]), aw, Tm[c]);
+					}
+				}
+#pragma unroll
+				for(int c = 0; c < NCH; c++) v[c] = __fadd_rn(v[c], pp[c]);
+			}
+			hpass_tail<NCH>(F, i, j, v, Tm);
+		}
+	};
+
+	for(int q = 0; q < nq; q++) {
+		const int st = q % kBulkStages, use = q / kBulkStages;
+		if(!failed && !mbar_wait(full + st, use & 1, F.wait_polls)) {
+			atomicExch(F.err_flag, 1);
+			*(volatile int *)abort_flag = 1;
+			failed = true;   // keep to the barrier schedule; no more sums are taken
+		}
+		uint32_t cur[NW];
+		{
+			const uint4 v = reinterpret_cast<const uint4 *>(ring + (size_t)st * STRIP)[threadIdx.x];
+			cur[0] = v.x; cur[1] = v.y; cur[2] = v.z; cur[3] = v.w;
+		}
+		__syncwarp();
+		if(lane == 0 && !failed) mbar_arrive(empty + st);
+		float val[PX][NCH], a[PX];
+#pragma unroll
+		for(int px = 0; px < PX; px++) {
+			a[px] = 1.0f;
+#pragma unroll
+			for(int c = 0; c < NCH; c++) {
+				const int sidx = px * NCH + c;
+				unsigned int code;
+				if(DEPTH == 8) code = __byte_perm(cur[sidx >> 2], 0u, 0x4440u + (sidx & 3));
+				else code = __byte_perm(cur[sidx >> 1], 0u, (sidx & 1) ? 0x4423u : 0x4401u);
+				if(ALPHA && c == NCH - 1) {
+					a[px] = __fmul_rn(u2f(code), ainv);
+					val[px][c] = a[px];
+				}
+				else val[px][c] = dec_table<DEPTH>(s_tab, code);
+			}
+		}
+		unsigned long long v2[NCH];
+#pragma unroll
+		for(int c = 0; c < NCH; c++) v2[c] = f2_pack(val[0][c], val[1][c]);
+		if(ALPHA) {
+			const unsigned long long a2 = f2_pack(a[0], a[1]);
+#pragma unroll
+			for(int c = 0; c < NCH - 1; c++) v2[c] = f2_mul(v2[c], a2);   // premultiply
+		}
+		const float4 wq = *reinterpret_cast<const float4 *>(s_w + q * NS);
+		const float wsv[4] = {wq.x, wq.y, wq.z, wq.w};
+#pragma unroll
+		for(int s = 0; s < NS; s++) {
+			const unsigned long long w2 = f2_pack(wsv[s], wsv[s]);
+#pragma unroll
+			for(int c = 0; c < NCH; c++) acc[s][c] = f2_fma(v2[c], w2, acc[s][c]);
+		}
+		const int2 fin = s_fin[q];
+		for(int k = 0; k < fin.y; k++) {   // at most one row per position (checked by the host)
+			const int j = fin.x + k;
+			const int sj = j % NS;
+			const bool keep = j >= jb && j < je;
+#pragma unroll
+			for(int s = 0; s < NS; s++) {
+				if(s == sj) {
+					if(keep && any) {
+						float4 *o = mid + (size_t)(j % kFuseRows) * MIDW + x0;
+						float lo[NCH], hi[NCH];
+#pragma unroll
+						for(int c = 0; c < NCH; c++) f2_unpack(acc[s][c], lo[c], hi[c]);
+						o[0] = make_float4(lo[0], lo[1], lo[2], lo[3]);
+						o[1] = make_float4(hi[0], hi[1], hi[2], hi[3]);
+					}
+#pragma unroll
+					for(int c = 0; c < NCH; c++) acc[s][c] = 0ULL;
+				}
+			}
+			if(keep && ++pending == 2) {
+				if(!failed) horizontal(2);
+				else asm volatile("bar.sync 1, %0;" ::"n"(kBulkConsumers) : "memory");
+				jh += 2;
+				pending = 0;
+			}
+		}
+	}
+	if(pending > 0) {
+		if(!failed) horizontal(pending);
+		else asm volatile("bar.sync 1, %0;" ::"n"(kBulkConsumers) : "memory");
 	}
 }
 
@@ -953,6 +1193,12 @@ __device__ __forceinline__ void hpass_tail(const FJob &F, int i, int j, const fl
 			err = __fmaf_rn(fabsf(q), 2.4e-7f, err);
 			val = q;
 		}
+		if(F.dbg) {
+			const unsigned long long di = ((unsigned long long)F.k_out[k] * F.out_h + j) * F.out_w + i;
+			const unsigned long long dn = (unsigned long long)F.out_n * F.out_h * F.out_w;
+			F.dbg[di] = val;
+			F.dbg[dn + di] = err;
+		}
 		const int c = quantize_guarded(F.k_tail[k], val, err, i, j);
 		if(c < 0) {
 			if(is_alpha) redo = all;
@@ -964,7 +1210,8 @@ __device__ __forceinline__ void hpass_tail(const FJob &F, int i, int j, const fl
 	}
 	if(redo) {
 		const int slot = atomicAdd(F.flag_count, 1);
-		reinterpret_cast<int4 *>(F.flag_list)[slot] = make_int4(j * F.out_w + i, (int)redo, F.img, 0);
+		if(slot < F.flag_cap) reinterpret_cast<int4 *>(F.flag_list)[slot] = make_int4(j * F.out_w + i, (int)redo, F.img, 0);
+		else atomicExch(F.err_flag, 2);   // more entries than pixels: never in a correct run
 		if(redo == all) return;
 	}
 #pragma unroll
@@ -1019,6 +1266,11 @@ struct FastState {
 	std::vector<int> first_pos, last_pos;
 	size_t vsmem_fixed = 0, vsmem_per_pos = 0;
 	bool in_device = false;
+	// fused vertical + horizontal pass (k_vhfuse, vkernel; no hkernel): its
+	// column tiles (device copy in the blob)
+	bool fuse = false;
+	size_t o_fuse = 0;
+	const FuseTile *fuse_tiles = nullptr;
 	// vertical pass on the tensor cores (tcvert.cu) instead of vkernel's FJob launch
 	bool tc = false;
 	tc::TcJob T;

@@ -55,6 +55,13 @@ __global__ void __launch_bounds__(kBulkThreads, 2) k_vbulk(FJob F)
 }
 
 template<int NS, int NCH, bool ALPHA, int DEPTH, int PX>
+__global__ void __launch_bounds__(kBulkThreads, 2) k_vhfuse(FJob F, const FuseTile *tiles)
+{
+	extern __shared__ __align__(128) unsigned char s_fuse[];
+	vhfuse_tile<NS, NCH, ALPHA, DEPTH, PX>(F, tiles, s_fuse, blockIdx.x, blockIdx.y);
+}
+
+template<int NS, int NCH, bool ALPHA, int DEPTH, int PX>
 __global__ void __launch_bounds__(kVPxThreads) k_vstream_px(FJob F)
 {
 	extern __shared__ __align__(16) float s_dyn[];
@@ -314,10 +321,20 @@ void fast_launch_impl(cudaStream_t st, void *state, void (*mark)(void *), void *
 	cudaMemsetAsync(S.F.flag_count, 0, 3 * sizeof(int), st);
 	void *fargs[] = {&S.F};
 	void *targs[] = {&S.T};
-	cudaLaunchKernel(S.vkernel, S.vgrid, dim3(S.vthreads), S.tc ? targs : fargs, S.vsmem, st);
-	mark(markarg);
-	cudaLaunchKernel(S.hkernel, S.hgrid, dim3(kHThreads), fargs, 0, st);
-	mark(markarg);
+	void *uargs[] = {&S.F, &S.fuse_tiles};
+	if(S.fuse) {
+		// one fused launch: its time is reported as the vertical group's, the
+		// horizontal group's is empty
+		cudaLaunchKernel(S.vkernel, S.vgrid, dim3(S.vthreads), uargs, S.vsmem, st);
+		mark(markarg);
+		mark(markarg);
+	}
+	else {
+		cudaLaunchKernel(S.vkernel, S.vgrid, dim3(S.vthreads), S.tc ? targs : fargs, S.vsmem, st);
+		mark(markarg);
+		cudaLaunchKernel(S.hkernel, S.hgrid, dim3(kHThreads), fargs, 0, st);
+		mark(markarg);
+	}
 	// exact re-evaluation of flagged pixels (recomputes the vertical pass too)
 	launch_fix_flagged(st, S.J, S.F.flag_count, S.F.flag_list, (int)std::min<size_t>(S.flag_entries, 0x7fffffff));
 	mark(markarg);
@@ -332,10 +349,12 @@ void fast_release(FastInfo &fi)
 // Host preparation of one image: job layout, error model, per-image arrays
 // (in FastState::blob, placed later) and kernel choice.  'batch' picks
 // taller vertical tiles (many images fill the GPU).  Caller holds the cache lock.
-static FastState *fast_build(const Plan &P, const Job &J, bool batch, int tc_mode, std::string &err)
+static FastState *fast_build(const Plan &P, const Job &J, bool batch, int tc_mode, std::string &err,
+	bool allow_fuse = false)
 {
 	FJob F;
 	memset(&F, 0, sizeof(F));
+	F.wait_polls = kWaitPolls;
 	const Weights &WV = *P.wsets[1][0], &WH = *P.wsets[0][0];
 
 	// ---- planes: distinct (input channel, transfer, premultiply) combinations
@@ -681,6 +700,67 @@ static FastState *fast_build(const Plan &P, const Job &J, bool batch, int tc_mod
 	}
 	if(!FS->vkernel) { delete FS; err = "fast form: no kernel for this layout"; return nullptr; }
 	FS->in_device = in_device;
+	// Fused vertical + horizontal pass: where the bulk-copy vertical pass runs
+	// (rows in device memory, 16-byte aligned), at most one output row
+	// finishes per input position (downscales), and the horizontal windows
+	// are narrow (a thread per pixel).  Column tiles are chosen so that each
+	// tile's input columns, widened to 16-byte boundaries, fit one strip.
+	std::vector<FuseTile> ftiles;
+	if(allow_fuse && !batch && FS->vv.kind == 4 && FS->vv.nch == 4 && FS->vv.px == 2 && FS->vv.ns == 4 && !hwarp &&
+		WH.kind == RowKind::Sum && F.mid_h == F.out_h) {
+		int max_fin = 0;
+		for(size_t q = 1; q < S.pinfo.size(); q += 2) max_fin = std::max(max_fin, S.pinfo[q]);
+		const int al = 16 / v_bpp;   // columns per 16 bytes
+		const int maxc = kBulkConsumers * FS->vv.px;
+		const long long row_cols = (long long)P.in_bpr / v_bpp - P.crop_x;   // columns a row's bytes hold from the crop
+		bool ok = max_fin <= 1 && 16 % v_bpp == 0;
+		auto plan_tiles = [&](int ntiles) {
+			std::vector<FuseTile> t;
+			const int tw = (F.out_w + ntiles - 1) / ntiles;
+			for(int i0 = 0; i0 < F.out_w; i0 += tw) {
+				const int i1 = std::min(F.out_w, i0 + tw);
+				int lo = INT32_MAX, hi = -1;
+				for(int t2 = WH.off[i0]; t2 < WH.off[i1]; t2++)
+					if(WH.src[t2] >= 0) { lo = std::min(lo, WH.src[t2]); hi = std::max(hi, WH.src[t2]); }
+				if(hi < 0) return std::vector<FuseTile>();
+				const int xa = lo / al * al, xb = (hi + 1 + al - 1) / al * al;
+				if(xb - xa > maxc || xb > row_cols) return std::vector<FuseTile>();
+				t.push_back(FuseTile{xa, xb - xa, i0, i1});
+			}
+			return t;
+		};
+		for(int ntiles = std::max(1, F.out_w * 4 / maxc); ok && ntiles <= F.out_w && ftiles.empty(); ntiles++)
+			ftiles = plan_tiles(ntiles);
+	}
+	if(!ftiles.empty()) {
+		const void *k_ = nullptr;
+		if(FS->vv.alpha && FS->vv.depth == 16) k_ = (const void *)k_vhfuse<4, 4, true, 16, 2>;
+		const size_t fixed = (size_t)kBulkStages * kBulkConsumers * FS->vv.px * FS->vv.nch * (FS->vv.depth / 8) +
+			(size_t)kFuseRows * kBulkConsumers * FS->vv.px * sizeof(float4) + 256 + (size_t)dec_floats * sizeof(float);
+		const size_t per_pos = (size_t)FS->vv.ns * sizeof(float) + sizeof(int2);
+		const int ntiles = (int)ftiles.size();
+		int bands = std::max(1, std::min(F.mid_h, (2 * 152) / ntiles));
+		int rows = (F.mid_h + bands - 1) / bands;
+		bands = (F.mid_h + rows - 1) / rows;
+		int nq_max = 0;
+		for(int b = 0; b < bands; b++) {
+			const int jb = b * rows, je = std::min(jb + rows, F.mid_h);
+			nq_max = std::max(nq_max, S.last_pos[je - 1] - S.first_pos[jb] + 1);
+		}
+		const size_t sm = fixed + (size_t)nq_max * per_pos;
+		if(k_ && sm <= 200 * 1024 &&
+			cudaFuncSetAttribute(k_, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) == cudaSuccess) {
+			FS->fuse = true;
+			FS->vkernel = k_;
+			FS->vgrid = dim3(ntiles, bands);
+			FS->vthreads = kBulkThreads;
+			FS->vsmem = sm;
+			F.rows_per_band = rows;
+			FS->vv.kind = 6;
+			FS->o_fuse = add(ftiles.data(), ftiles.size() * sizeof(FuseTile));
+		}
+		cudaGetLastError();
+	}
 	if(S.ok) {
 		FS->first_pos = S.first_pos;
 		FS->last_pos = S.last_pos;
@@ -693,6 +773,11 @@ static FastState *fast_build(const Plan &P, const Job &J, bool batch, int tc_mod
 		FS->vsmem_per_pos = (size_t)FS->vv.ns * sizeof(float) + sizeof(int2);
 		FS->vsmem_fixed = (size_t)kBulkStages * kBulkConsumers * FS->vv.px * FS->vv.nch * (FS->vv.depth / 8) + 256 +
 			(size_t)dec_floats * sizeof(float);
+	}
+	else if(FS->vv.kind == 6) {
+		FS->vsmem_per_pos = (size_t)FS->vv.ns * sizeof(float) + sizeof(int2);
+		FS->vsmem_fixed = (size_t)kBulkStages * kBulkConsumers * FS->vv.px * FS->vv.nch * (FS->vv.depth / 8) +
+			(size_t)kFuseRows * kBulkConsumers * FS->vv.px * sizeof(float4) + 256 + (size_t)dec_floats * sizeof(float);
 	}
 	else FS->vsmem_fixed = FS->vsmem;
 	if(hwarp) {
@@ -730,11 +815,12 @@ static FastState *fast_build(const Plan &P, const Job &J, bool batch, int tc_mod
 
 // Points the image's per-image arrays at 'base' (a device copy of its blob)
 // and its flags at the given counter and list.
-static void fast_place(FastState *FS, const uint8_t *base, int *flag_count, int *flag_list, int img)
+static void fast_place(FastState *FS, const uint8_t *base, int *flag_count, int *flag_list, int img, size_t flag_cap)
 {
 	FJob &F = FS->F;
 	F.flag_count = flag_count;
 	F.flag_list = flag_list;
+	F.flag_cap = (int)std::min<size_t>(flag_cap, 0x7fffffff);
 	F.err_flag = flag_count + 2;
 	F.img = img;
 	F.hoff = (const int *)(base + FS->o_hoff);
@@ -753,6 +839,7 @@ static void fast_place(FastState *FS, const uint8_t *base, int *flag_count, int 
 		T.blk = (const int4 *)(base + FS->o_tcb);
 		T.lut = (const uint2 *)(base + FS->o_tcl);
 	}
+	FS->fuse_tiles = FS->fuse ? (const FuseTile *)(base + FS->o_fuse) : nullptr;
 	Job &J = FS->J;
 	for(int m = 0; m < dev::kMaxCh; m++) J.df_tab[m] = FS->df ? FS->df_tab[m] : nullptr;
 	J.df_atab = FS->df ? FS->df_atab : nullptr;
@@ -783,7 +870,7 @@ static void fast_place(FastState *FS, const uint8_t *base, int *flag_count, int 
 static int vbands(const FastState &FS)
 {
 	if(FS.tc) return (FS.T.nblk + FS.T.blocks_per_band - 1) / FS.T.blocks_per_band;
-	if(FS.vv.kind == 1 || FS.vv.kind == 2 || FS.vv.kind == 4) return (int)FS.vgrid.y;
+	if(FS.vv.kind == 1 || FS.vv.kind == 2 || FS.vv.kind == 4 || FS.vv.kind == 6) return (int)FS.vgrid.y;
 	return 0;
 }
 
@@ -830,8 +917,14 @@ static bool set_vbands(FastState &FS, int bands)
 static bool launch_vertical(cudaStream_t st, FastState &FS)
 {
 	void *fargs[] = {&FS.F};
+	void *uargs[] = {&FS.F, &FS.fuse_tiles};
 	void *targs[] = {&FS.T};
-	return cudaLaunchKernel(FS.vkernel, FS.vgrid, dim3(FS.vthreads), FS.tc ? targs : fargs, FS.vsmem, st) == cudaSuccess;
+	// The fused pass also lists flagged pixels: its counters start at zero
+	// for every trial launch (the scratch holding them is reused between
+	// jobs, and trials must not pile entries past the list's capacity).
+	if(FS.fuse) cudaMemsetAsync(FS.F.flag_count, 0, 3 * sizeof(int), st);
+	return cudaLaunchKernel(FS.vkernel, FS.vgrid, dim3(FS.vthreads), FS.tc ? targs : (FS.fuse ? uargs : fargs), FS.vsmem,
+		st) == cudaSuccess;
 }
 
 // Chooses the band count of FS's vertical pass (cached per geometry).  Runs
@@ -884,7 +977,7 @@ bool fast_prepare(cudaStream_t st, const Plan &P, Job &J, FastInfo &fi, std::str
 {
 	Cache &C = cache();
 	std::lock_guard<std::mutex> lk(C.mu);
-	FastState *FS = fast_build(P, J, false, fi.tc_mode, err);
+	FastState *FS = fast_build(P, J, false, fi.tc_mode, err, fi.fuse_mode != 0 && !fi.dbg);
 	if(!FS) return false;
 	const size_t flag_off = (FS->blob.size() + 255) & ~(size_t)255;
 	const size_t need = flag_off + 256 + FS->flag_entries * 16;
@@ -902,10 +995,15 @@ bool fast_prepare(cudaStream_t st, const Plan &P, Job &J, FastInfo &fi, std::str
 	}
 	uint8_t *base = (uint8_t *)C.scratch;
 	cudaMemcpyAsync(base, FS->blob.data(), FS->blob.size(), cudaMemcpyHostToDevice, st);
-	fast_place(FS, base, (int *)(base + flag_off), (int *)(base + flag_off + 256), 0);
-	if(fi.autotune) tune_vertical(st, *FS);
+	fast_place(FS, base, (int *)(base + flag_off), (int *)(base + flag_off + 256), 0, FS->flag_entries);
+	FS->F.dbg = fi.dbg;
+	for(int k = 0; k < P.mid_n && k < 4; k++) fi.plane_of[J.order[k]] = FS->F.k_plane[k];
+	if(fi.wait_polls > 0) FS->F.wait_polls = fi.wait_polls;
+	FS->F.starve = fi.starve;
+	if(fi.autotune && fi.wait_polls <= 0 && !fi.starve) tune_vertical(st, *FS);
 	fi.state = FS;
-	fi.launches = 3;
+	fi.launches = FS->fuse ? 2 : 3;
+	fi.fused = FS->fuse ? 1 : 0;
 	fi.launch_fn = fast_launch_impl;
 	fi.streaming = FS->streaming;
 	fi.slots = FS->F.ns;
@@ -927,10 +1025,11 @@ size_t fast_item_blob_bytes(const void *item) { return static_cast<const FastSta
 const void *fast_item_blob(const void *item) { return static_cast<const FastState *>(item)->blob.data(); }
 size_t fast_item_flag_entries(const void *item) { return static_cast<const FastState *>(item)->flag_entries; }
 int fast_item_htaps(const void *item) { return static_cast<const FastState *>(item)->J.wh[0].max_taps; }
+int fast_item_vtaps(const void *item) { return static_cast<const FastState *>(item)->J.wv[0].max_taps; }
 
-void fast_item_place(void *item, const uint8_t *dev_blob, int *flag_count, int *flag_list, int img)
+void fast_item_place(void *item, const uint8_t *dev_blob, int *flag_count, int *flag_list, int img, size_t flag_cap)
 {
-	fast_place(static_cast<FastState *>(item), dev_blob, flag_count, flag_list, img);
+	fast_place(static_cast<FastState *>(item), dev_blob, flag_count, flag_list, img, flag_cap);
 }
 
 void fast_item_job_df(const void *item, Job &J)
@@ -959,6 +1058,7 @@ void preload_fast_kernels()
 #undef IWG_PRE_PX
 #undef IWG_PRE_ST
 #undef IWG_PRE_GA
+	cudaFuncGetAttributes(&a, (const void *)k_vhfuse<4, 4, true, 16, 2>);
 	cudaFuncGetAttributes(&a, tc::tc_kernel(true));
 	cudaFuncGetAttributes(&a, tc::tc_kernel(false));
 	cudaFuncGetAttributes(&a, (const void *)k_hpass_fast<1>);

@@ -17,7 +17,13 @@ struct FastInfo {
 	int tc_mode = 1;     // in: vertical pass on the tensor cores: 0 never, 1 wide windows, 2 whenever eligible
 	int tc = 0;          // out: the vertical pass runs on the tensor cores
 	int autotune = 1;    // in: choose the vertical pass's band count by measurement (cached per geometry)
+	int fuse_mode = 1;   // in: 1 fuse the vertical and horizontal passes where possible, 0 never
+	int fused = 0;       // out: the passes run as one fused launch
+	int wait_polls = 0;  // in: >0 shortens the vertical pipeline's bounded waits (failure tests)
+	int starve = 0;      // in: 1: the pipeline's producer issues nothing, so its waits run out (failure tests)
 	int *flag_count_dev = nullptr;   // device counter of pixels re-evaluated exactly
+	float *dbg = nullptr;            // in: debug readback buffer of the tail's values and bounds (FJob::dbg)
+	int plane_of[4] = {0, 0, 0, 0};  // out: intermediate plane of each intermediate channel
 	void *state = nullptr;            // prepared launch state (fastpath.cu)
 	int launches = 0;
 	void (*launch_fn)(cudaStream_t, void *, void (*)(void *), void *) = nullptr;
@@ -78,8 +84,9 @@ size_t fast_item_blob_bytes(const void *item);     // per-image arrays, to copy 
 const void *fast_item_blob(const void *item);
 size_t fast_item_flag_entries(const void *item);   // flag list capacity the image needs
 int fast_item_htaps(const void *item);             // widest horizontal window
+int fast_item_vtaps(const void *item);             // widest vertical window
 // Points the image at its device copy of the blob and the shared flag list.
-void fast_item_place(void *item, const uint8_t *dev_blob, int *flag_count, int *flag_list, int img);
+void fast_item_place(void *item, const uint8_t *dev_blob, int *flag_count, int *flag_list, int img, size_t flag_cap);
 // Launches the vertical and horizontal passes of n placed images, one launch
 // per kernel variant (fastbatch.cu).  Returns the number of launches, -1 on error.
 // Load every kernel of the fast form (per image / batched) now: with lazy

@@ -166,6 +166,16 @@ struct DimRequest {
 	double true_size = 0;  // derived
 };
 
+// Debug readback of one call (option gpu:debug_values): the intermediate
+// image [mid_n][mid_h][mid_w] and, per output sample [out_n][out_h][out_w],
+// the value the quantisation starts from and its error bound (fast form;
+// 0 in the plain form, whose values are the reference's).  NaN: no value.
+struct DebugValues {
+	std::vector<double> interm, value, bound;
+	int dims[6] = {0, 0, 0, 0, 0, 0};   // mid_n, mid_h, mid_w, out_n, out_h, out_w
+	void clear() { interm.clear(); value.clear(); bound.clear(); for(int &d : dims) d = 0; }
+};
+
 struct Stats {   // per call, readable through the iwg_* extension API
 	double ms_total = 0, ms_device = 0;
 	double ms_part[4] = {0, 0, 0, 0};   // per launch group: vertical, horizontal, fix-up / scan
@@ -176,6 +186,8 @@ struct Stats {   // per call, readable through the iwg_* extension API
 	int zero_copy = 0;           // kernels read/wrote the host image buffers directly
 	int vertical_tensor = 0;     // the vertical pass ran on the tensor cores
 	int graph = 0;               // the timed passes were replayed as a CUDA graph
+	int fused = 0;               // the fp32 form's passes ran as one fused launch
+	double ms_phase[6] = {0, 0, 0, 0, 0, 0};   // plan, upload, device, download, post-pass, device part's wall
 };
 
 }  // namespace iwg
@@ -244,6 +256,7 @@ struct iw_context {
 	int out_maxcc[iwg::kMaxCh] = {0, 0, 0, 0};
 	iwg::OptState opt;
 	iwg::Stats stats;
+	iwg::DebugValues dbg;
 };
 
 namespace iwg {
@@ -281,8 +294,13 @@ void optimize(iw_context *ctx);
 // pipeline.cu
 // Device lanes (independent streams, buffers and table caches): lane 0 serves
 // the public entry points; a request server runs its serial dither scans on
-// lanes 1 .. kLanes-1.
-constexpr int kLanes = 8;
+// lanes 1 .. kLanes-1 (kSmallScanLanes of them for small outputs).  Every
+// lane is one stream (plus a download stream used only with staged copies):
+// with CUDA_DEVICE_MAX_CONNECTIONS at 32 (set when the library loads, if the
+// process has not set it), each lane's stream has a hardware queue of its
+// own, so a long scan on one lane never holds up work queued on another.
+constexpr int kLanes = 32;
+constexpr int kSmallScanLanes = 4;
 bool run_pipeline(iw_context *ctx, Plan &P, int warmup = 0, int iters = 1, int lane = 0);
 // Host wall time of the batched calls' phases, summed (ms): preparation,
 // uploads, the passes' launches, the fix-up's launch, device wait with

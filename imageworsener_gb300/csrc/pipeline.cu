@@ -172,6 +172,7 @@ __device__ void pixel_exact(const Job &J, int i, int j, bool apply_post, Interm 
 		if(oc < 0) continue;
 		const DOut &o = J.outc[oc];
 		double v = unassoc_and_bkgd(J, mc, o, s, a, alt, is_alpha);
+		if(J.dbg) J.dbg[((unsigned long long)oc * J.out_h + j) * J.out_w + i] = v;
 		if(J.out_float) {
 			float f = __double2float_rn(v);
 			if(J.negate && !is_alpha) f = __fsub_rn(1.0f, f);
@@ -826,14 +827,32 @@ __device__ __forceinline__ bool interm_df_all(const Job &J, unsigned int mask, i
 // equal to the reference's (double)(rank + 0.5) / 64.0.
 __device__ __forceinline__ float dither_threshold(int rank) { return __fmul_rn((float)rank + 0.5f, 0.015625f); }
 
+// Double-float copy of a double: hi + lo within u^2 |d| of d (d - hi is
+// exact in double: hi carries d's leading 24 bits).
+__device__ __forceinline__ dfl df_from_double(double d)
+{
+	const float hi = __double2float_rn(d);
+	return {hi, __double2float_rn(dsub(d, (double)hi))};
+}
+
+// x / y in double-float for 0 <= x <= y: a float quotient and one
+// correction from the double-float remainder; error below about 20 u^2
+// (7e-14) absolute.
+__device__ __forceinline__ dfl df_div_le1(dfl x, dfl y)
+{
+	const float q1 = __fdiv_rn(x.hi, y.hi);
+	const dfl r = df_add(x, df_mul(y, {-q1, 0.0f}));
+	return df_fast_two_sum(q1, __fdiv_rn(r.hi, y.hi));
+}
+
 // quantize_exact's code for one end of an interval, with FP64 only for the
 // two distances: the clamp, bracket and exactness tests compare bit patterns
 // (order-preserving for non-negative doubles), and the ordered-dither
-// fraction d_lo / (d_lo + d_hi) is taken in FP32.  That fraction is within
-// 3.1e-7 of the reference's double one (each float rounding adds at most
-// 2^-24 relative, the fraction is at most 1), so a decision 1e-6 or more
-// away from the threshold is the reference's; nearer, 'ok' is cleared and
-// the caller falls back to the exact path.
+// fraction d_lo / (d_lo + d_hi) is taken in double-float: within 7e-14 of
+// the exact ratio, and the reference's double fraction is within 2.3e-16 of
+// it, so a decision 1e-12 or more away from the threshold is the
+// reference's; nearer, 'ok' is cleared and the caller falls back to the
+// exact path.
 __device__ __forceinline__ int quantize_end(const DQuant &q, double v, int x, int y, bool &ok)
 {
 	long long vb = __double_as_longlong(v);
@@ -855,11 +874,13 @@ __device__ __forceinline__ int quantize_end(const DQuant &q, double v, int x, in
 	const double vc = __longlong_as_double(vb);
 	const double d_lo = dsub(vc, q.rev[clo]), d_hi = dsub(q.rev[chi], vc);
 	if(q.dfam == IW_DITHERFAMILY_ORDERED) {
-		const float fl = (float)d_lo, fh = (float)d_hi;
-		const float f = __fdiv_rn(fl, __fadd_rn(fl, fh));
+		const dfl l = df_from_double(d_lo), h = df_from_double(d_hi);
+		const dfl f = df_div_le1(l, df_add(l, h));
 		const float thr = dither_threshold(dither_rank(q.dsub, x, y));
-		if(fabsf(__fsub_rn(f, thr)) <= 1e-6f) ok = false;
-		return f >= thr ? chi : clo;
+		// f.hi - thr is exact near the threshold (Sterbenz)
+		const float diff = __fadd_rn(__fsub_rn(f.hi, thr), f.lo);
+		if(fabsf(diff) <= 1e-12f) ok = false;
+		return diff >= 0.0f ? chi : clo;
 	}
 	return dle_bits(d_hi, d_lo) ? chi : clo;
 }
@@ -994,6 +1015,62 @@ __device__ __forceinline__ bool fix_df_finish(const Job &J, int i, int j, unsign
 	return true;
 }
 
+// The FP64 path of flagged pixel (i, j) by one warp: the lanes recompute the
+// intermediate values the pixel's horizontal taps read (one vertical FP64 sum
+// per (channel, tap), for the channels in 'mask'), then lane m finishes
+// intermediate channel m -- its horizontal sum, unassociation and
+// quantisation -- with the alpha value and alpha code passed between lanes.
+// The result equals pixel_exact()'s.  Scratch 'my': maxt floats per channel.
+__device__ void fix_pixel_fp64_warp(const Job &J, int i, int j, unsigned int mask, float *my, int maxt, int lane)
+{
+	const int ntask = __popc(mask) * maxt;
+	for(int k = lane; k < ntask; k += 32) {
+		const int r = k / maxt, t = k - r * maxt;
+		const int m = nth_bit(mask, r);
+		const DWeights &W = J.wh[J.mid[m].wh];
+		const int t0 = W.kind == 1 ? i : W.off[i];
+		const int nt = W.kind == 1 ? 1 : W.off[i + 1] - t0;
+		if(t < nt) {
+			const int src = W.src[t0 + t];
+			if(src >= 0) my[m * maxt + t] = (float)interm_exact<true>(J, m, src, j);
+		}
+	}
+	__syncwarp();
+	const bool mine = lane < J.mid_n && ((mask >> lane) & 1u);
+	double s = 0.0;
+	if(mine) s = hsum_exact(J, lane, i, j, [&](int m, int k, int) { return (double)my[m * maxt + k]; });
+	const int al = J.mid_alpha >= 0 ? J.mid_alpha : 0;
+	const double a = (double)__double2float_rn(__shfl_sync(0xffffffffu, s, al));
+	int code = -1, oc = -1;
+	bool is_alpha = false;
+	if(mine) {
+		const DMid &mc = J.mid[lane];
+		is_alpha = mc.ctype == IW_CHANNELTYPE_ALPHA;
+		oc = mc.out_ch;
+		if(oc >= 0) {
+			const DOut &o = J.outc[oc];
+			const double v = unassoc_and_bkgd(J, mc, o, s, a, checker_alt(J, i, j), is_alpha);
+			if(J.out_float) {
+				float fv = __double2float_rn(v);
+				if(J.negate && !is_alpha) fv = __fsub_rn(1.0f, fv);
+				store_float(J, oc, i, j, fv);
+			}
+			else if(o.scan) J.scanbuf[((unsigned long long)oc * J.out_h + j) * J.out_w + i] = v;
+			else code = quantize_exact(o.q, v, i, j);
+		}
+	}
+	const int ac = __shfl_sync(0xffffffffu, code, al);
+	const int alpha_code = (J.mid_alpha >= 0 && J.mid[al].out_ch >= 0) ? ac : -1;
+	if(code >= 0) {
+		if(!is_alpha) {
+			if(J.negate) code = J.outc[oc].maxcc - code;
+			if(J.blacken && alpha_code == 0) code = 0;
+		}
+		store_code(J, oc, i, j, (unsigned int)code);
+	}
+	__syncwarp();
+}
+
 // Exact re-evaluation of the pixels the fast form flagged, one warp per
 // pixel.  FP64 throughput is what limits this kernel, so the work is spread
 // over as many lanes as a pixel offers: first the lanes recompute the
@@ -1007,12 +1084,13 @@ __device__ __forceinline__ bool fix_df_finish(const Job &J, int i, int j, unsign
 // block per pixel spreads the work (k_fix_leftover); while that region does
 // not reach the flagged entries (cap - L > n), else the warp does it here.
 template<bool BATCH>
-__global__ void __launch_bounds__(128, 8) k_fix_flagged_warp(Job J1, const Job *jobs, int *count, int *list, int maxt, int cap)
+__global__ void __launch_bounds__(128, 8) k_fix_flagged_warp(Job J1, const Job *jobs, int *count, int *list, int maxt, int cap,
+	int listcap)
 {
 	extern __shared__ float fix_cache[];
 	const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, wpb = blockDim.x >> 5;
 	float *my = fix_cache + (size_t)wib * dev::kMaxCh * maxt;
-	const int n = *count;
+	const int n = min(*count, listcap);
 	for(int f = blockIdx.x * wpb + wib; f < n; f += gridDim.x * wpb) {
 		const int4 e = reinterpret_cast<const int4 *>(list)[f];
 		const Job &J = BATCH ? jobs[e.z] : J1;
@@ -1032,52 +1110,149 @@ __global__ void __launch_bounds__(128, 8) k_fix_flagged_warp(Job J1, const Job *
 			continue;
 		}
 		__syncwarp();
-		const int ntask = __popc(mask) * maxt;
-		for(int k = lane; k < ntask; k += 32) {
-			const int r = k / maxt, t = k - r * maxt;
-			const int m = nth_bit(mask, r);
-			const DWeights &W = J.wh[J.mid[m].wh];
-			const int t0 = W.kind == 1 ? i : W.off[i];
-			const int nt = W.kind == 1 ? 1 : W.off[i + 1] - t0;
-			if(t < nt) {
-				const int src = W.src[t0 + t];
-				if(src >= 0) my[m * maxt + t] = (float)interm_exact<true>(J, m, src, j);
+		fix_pixel_fp64_warp(J, i, j, mask, my, maxt, lane);
+	}
+}
+
+// Double-float tier with every lane busy (windows of up to kFix2MaxTaps
+// taps per dimension).  A flagged pixel reads nv x nh input pixels (its
+// vertical taps' rows by its horizontal taps' columns).  Step 1: the lanes
+// take those pixels in turn, one pixel per lane at a time, all loads of a
+// round in flight together; each decodes its pixel once and leaves the
+// double-float term v * (a * w_v) of every masked channel in shared memory
+// (the premultiplied value times the vertical weight; the order of the
+// products does not matter to the bound below, which holds for the exact
+// real product).  Step 2: the lanes take the (channel, horizontal tap)
+// pairs in turn and sum their nv terms, certifying each float32
+// intermediate as interm_df_all does.  Step 3 is fix_df_finish.
+// Bound (u = 2^-24, A = sum of |term|): table values u^2 each (v, a, w),
+// two double-float products 5u^2 each, n accurate additions 3u^2 of the
+// running magnitude: (13 + 3n) u^2 A <= 24 n u^2 A, as interm_df_all.
+constexpr int kFix2MaxTaps = 32;
+
+__device__ bool fix_pixel_df2(const Job &J, int i, int j, unsigned int mask, float2 *P, int pstride, float *my, int maxt,
+	int lane)
+{
+	const DWeights &WH = J.wh[J.mid[0].wh], &WV = J.wv[J.mid[0].wv];
+	const int ht0 = WH.kind == 1 ? i : WH.off[i], nh = WH.kind == 1 ? 1 : WH.off[i + 1] - ht0;
+	const int vt0 = WV.kind == 1 ? j : WV.off[j], nv = WV.kind == 1 ? 1 : WV.off[j + 1] - vt0;
+	bool need_alpha = false;
+#pragma unroll
+	for(int m = 0; m < dev::kMaxCh; m++)
+		if(m < J.mid_n && ((mask >> m) & 1u) && J.mid[m].unassoc) need_alpha = true;
+	need_alpha = need_alpha && J.in_alpha < J.in_nphys && J.df_atab != nullptr;
+	const int ntask = nv * nh;
+	// step 1: four pixels per lane in flight
+	for(int k0 = 0; k0 < ntask; k0 += 128) {
+		int px[4], py[4];
+		bool live[4];
+		unsigned int ac[4], cc[4][dev::kMaxCh];
+#pragma unroll
+		for(int u = 0; u < 4; u++) {
+			const int k = k0 + 32 * u + lane;
+			live[u] = false;
+			px[u] = py[u] = 0;
+			if(k < ntask) {
+				const int r = k / nh, t = k - r * nh;
+				const int sv = WV.src[vt0 + r], sh = WH.src[ht0 + t];
+				live[u] = sv >= 0 && sh >= 0;
+				px[u] = J.crop_x + (sh < 0 ? 0 : sh);
+				py[u] = J.crop_y + (sv < 0 ? 0 : sv);
 			}
 		}
+#pragma unroll
+		for(int u = 0; u < 4; u++) {
+			ac[u] = 0;
+			if(live[u] && need_alpha) ac[u] = raw_code(J, px[u], py[u], J.in_alpha);
+#pragma unroll
+			for(int m = 0; m < dev::kMaxCh; m++) {
+				cc[u][m] = 0;
+				if(live[u] && m < J.mid_n && ((mask >> m) & 1u) && J.mid[m].in_ch < J.in_nphys)
+					cc[u][m] = raw_code(J, px[u], py[u], J.mid[m].in_ch);
+			}
+		}
+		float2 av[4], vv[4][dev::kMaxCh];
+#pragma unroll
+		for(int u = 0; u < 4; u++) {
+			av[u] = make_float2(1.0f, 0.0f);
+			if(live[u] && need_alpha) av[u] = __ldg(J.df_atab + ac[u]);
+#pragma unroll
+			for(int m = 0; m < dev::kMaxCh; m++) {
+				vv[u][m] = make_float2(1.0f, 0.0f);
+				if(live[u] && m < J.mid_n && ((mask >> m) & 1u) && J.mid[m].in_ch < J.in_nphys)
+					vv[u][m] = __ldg(J.df_tab[m] + cc[u][m]);
+			}
+		}
+#pragma unroll
+		for(int u = 0; u < 4; u++) {
+			const int k = k0 + 32 * u + lane;
+			if(k >= ntask) continue;
+			const int r = k / nh;
+			const dfl w = WV.kind == 1 ? dfl{1.0f, 0.0f} : df_of(__ldg(J.df_wv + vt0 + r));
+			const dfl aw = need_alpha ? df_mul(df_of(av[u]), w) : w;
+#pragma unroll
+			for(int m = 0; m < dev::kMaxCh; m++) {
+				if(m >= J.mid_n || !((mask >> m) & 1u)) continue;
+				dfl t = {0.0f, 0.0f};
+				if(live[u]) t = df_mul(df_of(vv[u][m]), (J.mid[m].unassoc && need_alpha) ? aw : w);
+				P[m * pstride + k] = make_float2(t.hi, t.lo);
+			}
+		}
+	}
+	__syncwarp();
+	// step 2: one (channel, horizontal tap) sum per lane at a time
+	const float kd = (float)(24 * nv) * 3.5527137e-15f + (float)(2 * nv + 2) * 1.1102231e-16f;
+	const int nm = __popc(mask);
+	bool bad = false;
+	for(int k = lane; k < nm * nh; k += 32) {
+		const int r = k / nh, t = k - r * nh;
+		const int m = nth_bit(mask, r);
+		const float2 *col = P + m * pstride + t;
+		dfl acc = {0.0f, 0.0f};
+		float A = 0.0f;
+		for(int q = 0; q < nv; q++) {
+			const float2 v = col[q * nh];
+			acc = df_add(acc, df_of(v));
+			A = __fadd_rn(A, fabsf(v.x));
+		}
+		my[m * maxt + t] = acc.hi;
+		const float delta = __fmaf_rn(A * 1.01f, kd, 1e-30f);
+		// A == 0: every term is exactly zero (see interm_df_all)
+		if(!(A == 0.0f || rounds_to_hi(acc, delta))) bad = true;
+	}
+	if(__any_sync(0xffffffffu, bad)) return false;
+	__syncwarp();
+	return fix_df_finish(J, i, j, mask, my, maxt, lane);
+}
+
+// Re-evaluation of flagged pixels, one warp per pixel: the all-lanes
+// double-float tier (fix_pixel_df2), then, for a pixel it cannot certify,
+// the FP64 path in place.  Shared memory per warp: the terms (kMaxCh x
+// maxv x maxt double-float values) and the certified intermediates
+// (kMaxCh x maxt floats).  At most 'listcap' entries are read.
+template<bool BATCH>
+__global__ void __launch_bounds__(128) k_fix_df2(Job J1, const Job *jobs, int *count, const int *list, int maxv, int maxt,
+	int listcap)
+{
+	extern __shared__ float4 fix2_smem[];
+	const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, wpb = blockDim.x >> 5;
+	const int pstride = maxv * maxt;
+	float2 *P = reinterpret_cast<float2 *>(fix2_smem) + (size_t)wib * (dev::kMaxCh * pstride + dev::kMaxCh * maxt / 2 + 2);
+	float *my = reinterpret_cast<float *>(P + dev::kMaxCh * pstride);
+	const int n = min(*count, listcap);
+	for(int f = blockIdx.x * wpb + wib; f < n; f += gridDim.x * wpb) {
+		const int4 e = reinterpret_cast<const int4 *>(list)[f];
+		const Job &J = BATCH ? jobs[e.z] : J1;
+		const int p = e.x;
+		const unsigned int mask = (unsigned int)e.y & ((1u << J.mid_n) - 1u);
+		const int i = p % J.out_w, j = p / J.out_w;
+		if(J.df_wv && fix_pixel_df2(J, i, j, mask, P, pstride, my, maxt, lane)) {
+			__syncwarp();
+			continue;
+		}
+		if(lane == 0) atomicAdd(count + 1, 1);   // pixels that needed the FP64 path
 		__syncwarp();
-		const bool mine = lane < J.mid_n && ((mask >> lane) & 1u);
-		double s = 0.0;
-		if(mine) s = hsum_exact(J, lane, i, j, [&](int m, int k, int) { return (double)my[m * maxt + k]; });
-		const int al = J.mid_alpha >= 0 ? J.mid_alpha : 0;
-		const double a = (double)__double2float_rn(__shfl_sync(0xffffffffu, s, al));
-		int code = -1, oc = -1;
-		bool is_alpha = false;
-		if(mine) {
-			const DMid &mc = J.mid[lane];
-			is_alpha = mc.ctype == IW_CHANNELTYPE_ALPHA;
-			oc = mc.out_ch;
-			if(oc >= 0) {
-				const DOut &o = J.outc[oc];
-				const double v = unassoc_and_bkgd(J, mc, o, s, a, checker_alt(J, i, j), is_alpha);
-				if(J.out_float) {
-					float fv = __double2float_rn(v);
-					if(J.negate && !is_alpha) fv = __fsub_rn(1.0f, fv);
-					store_float(J, oc, i, j, fv);
-				}
-				else if(o.scan) J.scanbuf[((unsigned long long)oc * J.out_h + j) * J.out_w + i] = v;
-				else code = quantize_exact(o.q, v, i, j);
-			}
-		}
-		const int ac = __shfl_sync(0xffffffffu, code, al);
-		const int alpha_code = (J.mid_alpha >= 0 && J.mid[al].out_ch >= 0) ? ac : -1;
-		if(code >= 0) {
-			if(!is_alpha) {
-				if(J.negate) code = J.outc[oc].maxcc - code;
-				if(J.blacken && alpha_code == 0) code = 0;
-			}
-			store_code(J, oc, i, j, (unsigned int)code);
-		}
-		__syncwarp();
+		fix_pixel_fp64_warp(J, i, j, mask, my, maxt, lane);
 	}
 }
 
@@ -1148,7 +1323,7 @@ __global__ void __launch_bounds__(256) k_fix_leftover(Job J1, const Job *jobs, c
 	int cap)
 {
 	extern __shared__ float fix_cache[];
-	const int n = *count, left = min(count[1], cap - n);
+	const int n = min(*count, cap), left = min(count[1], cap - n);
 	for(int L = blockIdx.x; L < left; L += gridDim.x) {
 		const int4 e = reinterpret_cast<const int4 *>(list)[cap - 1 - L];
 		fix_pixel_fp64_block(BATCH ? jobs[e.z] : J1, e, fix_cache, maxt);
@@ -1169,7 +1344,7 @@ __global__ void __launch_bounds__(256, 1) k_fix_wide_df(Job J1, const Job *jobs,
 	extern __shared__ float fix_cache[];
 	float *my = fix_cache;
 	__shared__ int s_ok, s_slot;
-	const int n = *count;
+	const int n = min(*count, cap);
 	const int lane = threadIdx.x & 31;
 	for(int f = blockIdx.x; f < n; f += gridDim.x) {
 		const int4 e = reinterpret_cast<const int4 *>(list)[f];
@@ -1226,9 +1401,9 @@ __global__ void __launch_bounds__(256, 1) k_fix_wide_df(Job J1, const Job *jobs,
 
 // Fallback for very wide horizontal windows: one thread per flagged pixel.
 template<bool BATCH>
-__global__ void k_fix_flagged_thread(Job J1, const Job *jobs, int *count, const int *list)
+__global__ void k_fix_flagged_thread(Job J1, const Job *jobs, int *count, const int *list, int cap)
 {
-	const int n = *count;
+	const int n = min(*count, cap);
 	for(int f = blockIdx.x * blockDim.x + threadIdx.x; f < n; f += gridDim.x * blockDim.x) {
 		const int4 e = reinterpret_cast<const int4 *>(list)[f];
 		const Job &J = BATCH ? jobs[e.z] : J1;
@@ -1243,9 +1418,24 @@ __global__ void k_fix_flagged_thread(Job J1, const Job *jobs, int *count, const 
 // pixel (double-float, then FP64), and a block per pixel for those listed at
 // the tail of the flag list (capacity 'cap' entries).  Returns the launches.
 template<bool BATCH>
-static int launch_fix(cudaStream_t st, const Job &J, const Job *jobs, int maxt, int *count, int *list, int cap)
+static int launch_fix(cudaStream_t st, const Job &J, const Job *jobs, int maxv, int maxt, int *count, int *list, int cap)
 {
 	const size_t per_warp = (size_t)dev::kMaxCh * maxt * sizeof(float);
+	{
+		// narrow windows: every lane busy (k_fix_df2), four warps per block
+		const size_t per_warp2 = ((size_t)dev::kMaxCh * maxv * maxt + (size_t)dev::kMaxCh * maxt / 2 + 2) * sizeof(float2);
+		if(maxt <= kFix2MaxTaps && maxv <= kFix2MaxTaps && per_warp2 * 4 <= 96 * 1024) {
+			static bool attr_done[2] = {false, false};
+			if(!attr_done[BATCH]) {
+				cudaFuncSetAttribute(k_fix_df2<BATCH>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024);
+				attr_done[BATCH] = true;
+			}
+			int sms2 = 152;
+			cudaDeviceGetAttribute(&sms2, cudaDevAttrMultiProcessorCount, 0);
+			k_fix_df2<BATCH><<<16 * sms2, 128, per_warp2 * 4, st>>>(J, jobs, count, list, maxv, maxt, cap);
+			return 1;
+		}
+	}
 	int wpb = 4;
 	while(wpb > 1 && per_warp * wpb > 48 * 1024) wpb >>= 1;
 	int sms = 152;
@@ -1263,29 +1453,32 @@ static int launch_fix(cudaStream_t st, const Job &J, const Job *jobs, int maxt, 
 	}
 	if(per_warp * wpb <= 48 * 1024) {
 		const bool tail = maxt >= 48;
-		k_fix_flagged_warp<BATCH><<<24 * sms, 32 * wpb, per_warp * wpb, st>>>(J, jobs, count, list, maxt, tail ? cap : 0);
+		k_fix_flagged_warp<BATCH><<<24 * sms, 32 * wpb, per_warp * wpb, st>>>(J, jobs, count, list, maxt, tail ? cap : 0, cap);
 		if(!tail) return 1;
 		k_fix_leftover<BATCH><<<4 * sms, 256, per_warp, st>>>(J, jobs, count, list, maxt, cap);
 		return 2;
 	}
-	k_fix_flagged_thread<BATCH><<<24 * sms, 64, 0, st>>>(J, jobs, count, list);
+	k_fix_flagged_thread<BATCH><<<24 * sms, 64, 0, st>>>(J, jobs, count, list, cap);
 	return 1;
 }
 
 void launch_fix_flagged(cudaStream_t st, const Job &J, int *count, int *list, int cap)
 {
-	int maxt = 1;
-	for(int m = 0; m < J.mid_n; m++) maxt = maxt > J.wh[J.mid[m].wh].max_taps ? maxt : J.wh[J.mid[m].wh].max_taps;
-	launch_fix<false>(st, J, nullptr, maxt, count, list, cap);
+	int maxt = 1, maxv = 1;
+	for(int m = 0; m < J.mid_n; m++) {
+		maxt = std::max(maxt, J.wh[J.mid[m].wh].max_taps);
+		maxv = std::max(maxv, J.wv[J.mid[m].wv].max_taps);
+	}
+	launch_fix<false>(st, J, nullptr, maxv, maxt, count, list, cap);
 }
 
 // The same for a batch: flag entries name their image in 'jobs' (device
 // memory); maxt is the widest horizontal window of any image.
-int launch_fix_flagged_batch(cudaStream_t st, const Job *jobs, int maxt, int *count, int *list, int cap)
+int launch_fix_flagged_batch(cudaStream_t st, const Job *jobs, int maxv, int maxt, int *count, int *list, int cap)
 {
 	Job none;
 	memset(&none, 0, sizeof(none));
-	return launch_fix<true>(st, none, jobs, maxt, count, list, cap);
+	return launch_fix<true>(st, none, jobs, maxv, maxt, count, list, cap);
 }
 
 // Device form of the output post-pass's property scan (optimize.cpp
@@ -1420,6 +1613,28 @@ HostPool &host_pool()
 {
 	static HostPool *p = new HostPool();   // never destroyed
 	return *p;
+}
+
+// Device copy of a host buffer the GPU can read (pageable memory on a system
+// with pageable memory access): 16-byte loads, four in flight per thread,
+// then the tail.  Both pointers 16-byte aligned.
+__global__ void __launch_bounds__(256) k_pull(uint8_t *dst, const uint8_t *src, size_t n)
+{
+	const size_t n16 = n / 16;
+	const uint4 *s16 = reinterpret_cast<const uint4 *>(src);
+	uint4 *d16 = reinterpret_cast<uint4 *>(dst);
+	const size_t stride = (size_t)gridDim.x * blockDim.x;
+	size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+	for(; i + 3 * stride < n16; i += 4 * stride) {
+		const uint4 a = s16[i], b = s16[i + stride], c = s16[i + 2 * stride], d = s16[i + 3 * stride];
+		d16[i] = a;
+		d16[i + stride] = b;
+		d16[i + 2 * stride] = c;
+		d16[i + 3 * stride] = d;
+	}
+	for(; i < n16; i += stride) d16[i] = s16[i];
+	const size_t t = n16 * 16 + (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+	if(t < n) dst[t] = src[t];
 }
 
 struct Piece { uint8_t *dst; const uint8_t *src; size_t n; };
@@ -1574,7 +1789,7 @@ struct DeviceState {
 	int device = 0;
 	int pageable = 0;          // kernels may access pageable host memory (Grace: NVLink-C2C + ATS)
 	cudaStream_t stream = nullptr;
-	DevBuf in, interm, out, scan, err, params, flags;
+	DevBuf in, interm, out, scan, err, params, flags, dbg;
 	DevBuf batch_io, batch_tab;   // batches: buffers + tables of all images
 	cudaStream_t dl_stream = nullptr;   // scan lanes: per-image downloads while the batch's scans run
 	int *done_h = nullptr;              // scan lanes: per-image completion flags (mapped host memory)
@@ -1585,6 +1800,16 @@ struct DeviceState {
 	std::vector<uint8_t> staging;
 	Stager stager;
 };
+
+// Hardware work queues: CUDA maps streams onto CUDA_DEVICE_MAX_CONNECTIONS
+// queues (8 unless set), and work queued behind a long kernel of another
+// stream on the same queue waits for it.  The lanes' streams each get a
+// queue of their own with 32; the variable is read when the process creates
+// its CUDA context, and a value the process set itself is kept.
+__attribute__((constructor)) static void iwg_hardware_queues()
+{
+	setenv("CUDA_DEVICE_MAX_CONNECTIONS", "32", 0);
+}
 
 // Lanes: independent device states (stream, buffers, table cache), so that a
 // request server can keep long serial work (dither scans) on lanes of its own,
@@ -1630,7 +1855,8 @@ void preload_kernels()
 			(const void *)kb_finalize, (const void *)k_fix_flagged_warp<true>, (const void *)k_fix_flagged_warp<false>,
 			(const void *)k_fix_wide_df<true>, (const void *)k_fix_wide_df<false>, (const void *)k_out_props,
 			(const void *)k_fix_leftover<true>, (const void *)k_fix_leftover<false>,
-			(const void *)k_fix_flagged_thread<true>, (const void *)k_fix_flagged_thread<false>})
+			(const void *)k_fix_flagged_thread<true>, (const void *)k_fix_flagged_thread<false>,
+			(const void *)k_fix_df2<true>, (const void *)k_fix_df2<false>, (const void *)k_pull})
 			cudaFuncGetAttributes(&a, k);
 		preload_fast_kernels();
 		preload_batch_kernels();
@@ -1659,7 +1885,7 @@ bool ensure_init(DeviceState &S, std::string &err)
 		err = "cudaStreamCreate failed";
 		return false;
 	}
-	for(DevBuf *b : {&S.in, &S.interm, &S.out, &S.scan, &S.err, &S.params, &S.flags, &S.batch_io, &S.batch_tab})
+	for(DevBuf *b : {&S.in, &S.interm, &S.out, &S.scan, &S.err, &S.params, &S.flags, &S.dbg, &S.batch_io, &S.batch_tab})
 		b->st = S.stream;
 	S.stager.patient = S.lane != 0;
 	if(S.lane != 0 && cudaStreamCreateWithPriority(&S.dl_stream, cudaStreamNonBlocking, least) != cudaSuccess) {
@@ -1725,18 +1951,30 @@ int plain_launch(cudaStream_t st, const Plan &P, const Job &J, Mark mark);
 // caller's pageable buffers), "stage" (pinned staging with host copy threads)
 // or "zero" (kernels read and write the caller's host buffers in place; needs
 // pageable memory access, and is slow on the first touch of fresh pages).
-// Default: "copy" for one image (fastest measured for a large image on
-// Grace), "stage" for batches (many pageable copies are slow one by one, and
-// they synchronise with work already queued).  'resident' runs need the
-// input on the device.
-enum { UP_ZERO = 0, UP_COPY = 1, UP_STAGE = 2 };
+// or "pull" (one image: a copy kernel reads the caller's input over the
+// CPU-GPU link into device memory; needs pageable memory access).  Measured
+// on GB300 (Grace, NVLink-C2C) for a freshly malloc'd 134 MB input: a kernel
+// reads it at 143-161 GB/s, while a cudaMemcpyAsync from those fresh
+// pageable pages ran near 60 GB/s (host copies into pinned memory top out
+// near 95 GB/s with 8-16 threads).  Default: "pull" for one image where the
+// GPU reads pageable memory, else "copy"; "stage" for batches on lane 0 (many
+// pageable copies are slow one by one, and they synchronise with work
+// already queued); "zero" on a server's scan lanes.  'resident' runs need
+// the input on the device.
+enum { UP_ZERO = 0, UP_COPY = 1, UP_STAGE = 2, UP_PULL = 3 };
 static int upload_mode(iw_context *ctx, const DeviceState &S, bool resident, bool many = false)
 {
 	const char *u = get_option(ctx, "gpu:upload");
-	int m = many ? UP_STAGE : UP_COPY;
+	// scan lanes (a server's error-diffusion requests: small images, many
+	// lanes) read and write the callers' buffers in place where the GPU can
+	// (no pinned staging buffer per lane, no download stream); lane 0 stages
+	// its batches
+	int m = many ? (S.lane != 0 ? UP_ZERO : UP_STAGE) : UP_PULL;
 	if(u && !strcmp(u, "copy")) m = UP_COPY;
 	if(u && !strcmp(u, "stage")) m = UP_STAGE;
 	else if(u && !strcmp(u, "zero")) m = UP_ZERO;
+	else if(u && !strcmp(u, "pull")) m = UP_PULL;
+	if(m == UP_PULL && (!S.pageable || many || ((uintptr_t)ctx->img1.pixels & 15))) m = UP_COPY;
 	if(m == UP_ZERO && (!S.pageable || resident)) m = UP_COPY;
 	return m;
 }
@@ -1897,7 +2135,11 @@ bool run_pipeline(iw_context *ctx, Plan &P, int warmup, int iters, int lane)
 	const bool zero_copy = upmode == UP_ZERO;
 	const size_t interm_bytes = (size_t)P.mid_n * J.interm_plane * sizeof(float);
 	const size_t out_bytes = P.out_bpr * (size_t)P.out_h;
-	if((!zero_copy && (!S.in.ensure(in_bytes ? in_bytes : 16) || !S.out.ensure(out_bytes))) ||
+	// failure tests: option gpu:fail_alloc=1 makes this call's device
+	// allocation fail as cudaMalloc would when memory runs out
+	const char *fa = get_option(ctx, "gpu:fail_alloc");
+	const bool inject_oom = fa && !strcmp(fa, "1");
+	if(inject_oom || (!zero_copy && (!S.in.ensure(in_bytes ? in_bytes : 16) || !S.out.ensure(out_bytes))) ||
 		!S.interm.ensure(interm_bytes) || !S.params.ensure(S.staging.size() + 256)) {
 		iw_set_error(ctx, "Out of GPU memory");
 		return false;
@@ -1918,14 +2160,30 @@ bool run_pipeline(iw_context *ctx, Plan &P, int warmup, int iters, int lane)
 	for(const Fixup &f : fix) *f.slot = (const uint8_t *)S.params.p + f.off;
 
 	cudaStream_t st = S.stream;
+	// phase events: upload, device passes, download
+	struct PhaseEvents {
+		cudaEvent_t e[4] = {nullptr, nullptr, nullptr, nullptr};
+		PhaseEvents() { for(cudaEvent_t &x : e) cudaEventCreate(&x); }
+		~PhaseEvents() { for(cudaEvent_t x : e) if(x) cudaEventDestroy(x); }
+	} phases;
+	cudaEvent_t *const ph = phases.e;
+	cudaEventRecord(ph[0], st);
 	cudaMemcpyAsync(S.params.p, S.staging.data(), S.staging.size(), cudaMemcpyHostToDevice, st);
 	if(upmode == UP_COPY) cudaMemcpyAsync(S.in.p, ctx->img1.pixels, in_bytes, cudaMemcpyHostToDevice, st);
+	if(upmode == UP_PULL && in_bytes) {
+		int sms = 152;
+		cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, S.device);
+		const size_t n16 = in_bytes / 16;
+		const unsigned blocks = (unsigned)std::max<size_t>(1, std::min<size_t>((n16 + 1023) / 1024, (size_t)8 * sms));
+		k_pull<<<blocks, 256, 0, st>>>((uint8_t *)S.in.p, (const uint8_t *)ctx->img1.pixels, in_bytes);
+	}
 	if(upmode == UP_STAGE &&
 		!stage_h2d(S.stager, st, {Xfer{(uint8_t *)S.in.p, (uint8_t *)ctx->img1.pixels, in_bytes}})) {
 		iw_set_error(ctx, "Out of pinned host memory");
 		return false;
 	}
 
+	cudaEventRecord(ph[1], st);
 	const char *prec = get_option(ctx, "gpu:precision");
 	bool want_plain = prec && !strcmp(prec, "fp64");
 	FastInfo fi;
@@ -1934,15 +2192,40 @@ bool run_pipeline(iw_context *ctx, Plan &P, int warmup, int iters, int lane)
 		fi.tc_mode = (vt && !strcmp(vt, "cuda")) ? 0 : ((vt && !strcmp(vt, "tensor")) ? 2 : 1);
 		const char *at = get_option(ctx, "gpu:autotune");
 		fi.autotune = !(at && !strcmp(at, "off"));
+		const char *fu = get_option(ctx, "gpu:fuse");
+		fi.fuse_mode = !(fu && !strcmp(fu, "off"));
+		// failure tests: gpu:wait_test=1 starves the bulk-copy pipeline (its
+		// producer issues no copies, so no barrier it waits on ever
+		// completes) and shortens its waits to a few thousand polls
+		const char *wt = get_option(ctx, "gpu:wait_test");
+		fi.starve = (wt && !strcmp(wt, "1")) ? 1 : 0;
+		fi.wait_polls = fi.starve ? 4096 : 0;
 	}
 	bool fast = !want_plain && fast_eligible(P, J, fi);
 	ctx->stats.form = fast ? 1 : 0;
+	// Debug readback (option gpu:debug_values=1, one untimed pass): the
+	// intermediate image and, per output sample, the value the tail quantises
+	// (and, in the fast form, its error bound) are copied to the context.
+	const char *dbgopt = get_option(ctx, "gpu:debug_values");
+	const bool want_dbg = dbgopt && !strcmp(dbgopt, "1") && warmup == 0 && iters <= 1 && P.out_sampletype == IW_SAMPLETYPE_UINT;
+	const size_t dbg_n = (size_t)P.out_n * P.out_w * P.out_h;
+	ctx->dbg.clear();
+	if(want_dbg) {
+		if(!S.dbg.ensure(dbg_n * 8 + 16)) {
+			iw_set_error(ctx, "Out of GPU memory");
+			return false;
+		}
+		cudaMemsetAsync(S.dbg.p, 0xff, dbg_n * 8, st);   // NaN: no value
+		if(fast) fi.dbg = (float *)S.dbg.p;
+		else J.dbg = (double *)S.dbg.p;
+	}
 	ctx->stats.vertical_tensor = 0;
 	if(fast && !fast_prepare(st, P, J, fi, err)) {
 		iw_set_error(ctx, err.c_str());
 		return false;
 	}
 	ctx->stats.vertical_tensor = fast ? fi.tc : 0;
+	ctx->stats.fused = fast ? fi.fused : 0;
 
 	// The device passes, launched warmup+iters times; the input stays resident.
 	// Events bracket every launch group of the timed iterations.
@@ -2023,10 +2306,42 @@ bool run_pipeline(iw_context *ctx, Plan &P, int warmup, int iters, int lane)
 		}
 	}
 	if(S.lane != 0) wait_stream(st, true);   // downloads queued once the kernels are done (as for batches)
+	if(want_dbg) {
+		// intermediate planes in intermediate-channel order, then the values
+		// (and bounds): all as doubles on the host
+		const size_t plane = (size_t)J.interm_plane;
+		std::vector<float> im((size_t)P.mid_n * plane), fv(fast ? 2 * dbg_n : 0);
+		std::vector<double> dv(fast ? 0 : dbg_n);
+		for(int m = 0; m < P.mid_n; m++)
+			cudaMemcpyAsync(im.data() + (size_t)m * plane, J.interm + (size_t)(fast ? fi.plane_of[m] : m) * plane,
+				plane * sizeof(float), cudaMemcpyDeviceToHost, st);
+		if(fast) cudaMemcpyAsync(fv.data(), S.dbg.p, 2 * dbg_n * sizeof(float), cudaMemcpyDeviceToHost, st);
+		else cudaMemcpyAsync(dv.data(), S.dbg.p, dbg_n * sizeof(double), cudaMemcpyDeviceToHost, st);
+		if(cudaStreamSynchronize(st) == cudaSuccess) {
+			ctx->dbg.interm.assign(im.begin(), im.end());
+			if(fast) {
+				ctx->dbg.value.assign(fv.begin(), fv.begin() + dbg_n);
+				ctx->dbg.bound.assign(fv.begin() + dbg_n, fv.end());
+			}
+			else {
+				ctx->dbg.value = dv;
+				ctx->dbg.bound.assign(dbg_n, 0.0);
+			}
+			ctx->dbg.dims[0] = P.mid_n; ctx->dbg.dims[1] = J.mid_h; ctx->dbg.dims[2] = J.mid_w;
+			ctx->dbg.dims[3] = P.out_n; ctx->dbg.dims[4] = P.out_h; ctx->dbg.dims[5] = P.out_w;
+		}
+	}
+	cudaEventRecord(ph[2], st);
 	if(props) cudaMemcpyAsync(&prop_flags, S.flags.p, sizeof(unsigned int), cudaMemcpyDeviceToHost, st);
-	if(upmode == UP_COPY) cudaMemcpyAsync(ctx->img2.pixels, S.out.p, out_bytes, cudaMemcpyDeviceToHost, st);
+	if(upmode == UP_COPY || upmode == UP_PULL) cudaMemcpyAsync(ctx->img2.pixels, S.out.p, out_bytes, cudaMemcpyDeviceToHost, st);
 	if(upmode == UP_STAGE) stage_d2h(S.stager, st, {Xfer{(uint8_t *)S.out.p, (uint8_t *)ctx->img2.pixels, out_bytes}});
+	cudaEventRecord(ph[3], st);
 	cudaError_t ce = wait_stream(st, S.lane != 0);
+	for(int k = 0; k < 3; k++) {
+		float v = 0.0f;
+		ctx->stats.ms_phase[1 + k] = (ce == cudaSuccess && cudaEventElapsedTime(&v, ph[k], ph[k + 1]) == cudaSuccess) ? v : 0.0;
+	}
+	cudaGetLastError();
 	if(ce == cudaSuccess) ce = cudaGetLastError();
 	ctx->opt_dev_props = (ce == cudaSuccess && props) ? (int)(prop_flags | 0x100u) : 0;
 	ctx->stats.flagged = 0;
@@ -2040,7 +2355,7 @@ bool run_pipeline(iw_context *ctx, Plan &P, int warmup, int iters, int lane)
 		if(ce == cudaSuccess && nflag[2]) {
 			fast_release(fi);
 			for(cudaEvent_t e : ev) cudaEventDestroy(e);
-			iw_set_error(ctx, "A device wait ran out of time (vertical pass)");
+			iw_set_error(ctx, nflag[2] == 2 ? "Internal: flag list overflow" : "A device wait ran out of time (vertical pass)");
 			return false;
 		}
 	}
@@ -2283,10 +2598,11 @@ bool run_batch(const std::vector<iw_context *> &ctxs, const std::vector<Plan *> 
 	};
 	if(!S.batch_tab.ensure(tab.size())) return fail_all("Out of GPU memory (batch tables)");
 	uint8_t *tbase = (uint8_t *)S.batch_tab.p;
-	int maxt = 1;
+	int maxt = 1, maxv = 1;
 	for(int k = 0; k < m; k++) {
-		fast_item_place(items[k], tbase + o_blob[k], flag_count, flag_list, k);
+		fast_item_place(items[k], tbase + o_blob[k], flag_count, flag_list, k, nflag);
 		maxt = std::max(maxt, fast_item_htaps(items[k]));
+		maxv = std::max(maxv, fast_item_vtaps(items[k]));
 		// the job record gets the image's placed double-float pointers
 		fast_item_job_df(items[k], djobs[k]);
 		memcpy(tab.data() + o_jobs + (size_t)k * sizeof(Job), &djobs[k], sizeof(Job));
@@ -2325,7 +2641,7 @@ bool run_batch(const std::vector<iw_context *> &ctxs, const std::vector<Plan *> 
 	// graphs.)
 	const bool graphed = false;
 	int launches = fast_launch_batch(st, items.data(), m, err, ev_h, ev_f, [&]() {
-		return launch_fix_flagged_batch(st, (const Job *)(tbase + o_jobs), maxt, flag_count, flag_list,
+		return launch_fix_flagged_batch(st, (const Job *)(tbase + o_jobs), maxv, maxt, flag_count, flag_list,
 			(int)std::min<size_t>(nflag, 0x7fffffff));
 	}, nullptr);
 	pt.mark(2);
@@ -2665,7 +2981,21 @@ extern "C" int iwg_get_stats(struct iw_context *ctx, struct iwg_stats *out)
 	out->flagged_exact = ctx->stats.flagged_exact;
 	out->vertical_tensor = ctx->stats.vertical_tensor;
 	out->graph = ctx->stats.graph;
+	out->fused = ctx->stats.fused;
+	for(int k = 0; k < 6; k++) out->ms_phase[k] = ctx->stats.ms_phase[k];
 	return 1;
+}
+
+extern "C" long long iwg_debug_values(struct iw_context *ctx, int which, double *out, long long max_count, int *dims)
+{
+	const std::vector<double> *v = which == 0 ? &ctx->dbg.interm : which == 1 ? &ctx->dbg.value :
+		which == 2 ? &ctx->dbg.bound : nullptr;
+	if(!v) return -1;
+	if(dims)
+		for(int k = 0; k < 3; k++) dims[k] = ctx->dbg.dims[(which == 0 ? 0 : 3) + k];
+	const long long n = (long long)v->size();
+	if(out) memcpy(out, v->data(), (size_t)std::min(n, max_count < 0 ? 0 : max_count) * sizeof(double));
+	return n;
 }
 
 extern "C" int iwg_device_info(char *buf, int buflen)

@@ -225,13 +225,19 @@ void dispatcher_loop(iwg_server *S)
 	}
 }
 
-// A scan worker of class 'cls' (0 small, 1 large): takes every queued request
-// of its class that fits the device budget the workers share (a worker may
-// take one request whatever the budget when no other scan holds memory) and
-// runs them as one batch on its own lane.
+// A scan worker of class 'cls' (0 small, 1 large): takes queued requests of
+// its class that fit the device budget the workers share (a worker may take
+// one request whatever the budget when no other scan holds memory), at most
+// kScanBatch[cls] of them, and runs them as one batch on its own lane.  Large
+// scans take seconds and each worker holds its lane until its batch ends, so
+// large batches stay small: a request that arrives goes to an idle lane
+// rather than behind a long scan, and a backlog still fills two per lane.
+constexpr int kScanBatch[2] = {16, 2};
+
 void slow_loop(iwg_server *S, int lane, int cls)
 {
 	std::deque<iwg::Request *> &q = S->slow[cls];
+	const int max_batch = std::min(S->max_batch, kScanBatch[cls]);
 	for(;;) {
 		std::vector<iwg::Request *> batch;
 		size_t bytes = 0;
@@ -242,7 +248,7 @@ void slow_loop(iwg_server *S, int lane, int cls)
 					(!q.empty() && (S->slow_bytes == 0 || S->slow_bytes + q.front()->bytes <= S->budget));
 			});
 			if(q.empty()) return;
-			while(!q.empty() && (int)batch.size() < S->max_batch) {
+			while(!q.empty() && (int)batch.size() < max_batch) {
 				iwg::Request *r = q.front();
 				if((!batch.empty() || S->slow_bytes > 0) && S->slow_bytes + bytes + r->bytes > S->budget) break;
 				bytes += r->bytes;
@@ -298,7 +304,8 @@ extern "C" struct iwg_server *iwg_server_create(size_t device_budget, int max_ba
 	for(int k = 0; k < nplan; k++) S->planners.emplace_back(planner_loop, S);
 	for(int k = 0; k < 2 * nfin; k++) S->finishers.emplace_back(finisher_loop, S, k & 1);
 	S->dispatcher = std::thread(dispatcher_loop, S);
-	for(int lane = 1; lane < iwg::kLanes; lane++) S->scan_workers.emplace_back(slow_loop, S, lane, lane & 1);
+	for(int lane = 1; lane < iwg::kLanes; lane++)
+		S->scan_workers.emplace_back(slow_loop, S, lane, lane <= iwg::kSmallScanLanes ? 0 : 1);
 	return S;
 }
 

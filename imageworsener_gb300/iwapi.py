@@ -352,3 +352,99 @@ def run_served(lib: IWLib, jobs: Sequence[Job], budget: int = 0, max_batch: int 
         for ctx in ctxs:
             lib.iw_destroy_context(ctx)
 
+
+
+class GpuStats(C.Structure):
+    """struct iwg_stats (include/imagew_gb300.h)."""
+    _fields_ = [("ms_total", C.c_double), ("ms_device", C.c_double), ("ms_part", C.c_double * 4),
+                ("flagged", C.c_longlong), ("form", C.c_int), ("kernels", C.c_int), ("zero_copy", C.c_int),
+                ("flagged_exact", C.c_longlong), ("vertical_tensor", C.c_int), ("graph", C.c_int),
+                ("fused", C.c_int), ("ms_phase", C.c_double * 6)]
+
+
+def _stats_dict(lib: IWLib, ctx) -> dict:
+    st = GpuStats()
+    lib.dll.iwg_get_stats.argtypes = [C.c_void_p, C.POINTER(GpuStats)]
+    lib.dll.iwg_get_stats(ctx, C.byref(st))
+    return {"form": st.form, "flagged": st.flagged, "flagged_exact": st.flagged_exact,
+            "vertical_tensor": st.vertical_tensor, "fused": st.fused, "kernels": st.kernels,
+            "ms_device": st.ms_device, "ms_part": list(st.ms_part), "ms_phase": list(st.ms_phase)}
+
+
+def run_job_stats(lib: IWLib, job: Job) -> tuple:
+    """``run_job`` through libimagew_gb300, also returning its iwg_stats as a dict."""
+    ctx = lib.iw_create_context(None)
+    if not ctx:
+        raise MemoryError("iw_create_context failed")
+    try:
+        _setup(lib, ctx, job)
+        ok = bool(lib.iw_process_image(ctx))
+        return _collect(lib, ctx, ok, []), _stats_dict(lib, ctx)
+    finally:
+        lib.iw_destroy_context(ctx)
+
+
+def run_debug_values(lib: IWLib, job: Job, precision: str):
+    """Runs ``job`` once in the given form ("fp32" or "fp64") with the
+    library's debug readback on and returns (result, interm, value, bound,
+    stats): the intermediate image [n][rows][cols], the linear-light value
+    each output sample is quantised from [channel][row][col] and, for the
+    fp32 form, its rigorous error bound (all float64 numpy arrays; NaN where
+    the tail decided without a value)."""
+    import numpy as np
+    f = lib.dll.iwg_debug_values
+    f.restype = C.c_longlong
+    f.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_longlong, C.POINTER(C.c_int)]
+    ctx = lib.iw_create_context(None)
+    if not ctx:
+        raise MemoryError("iw_create_context failed")
+    try:
+        _setup(lib, ctx, job)
+        lib.iw_set_option(ctx, b"gpu:precision", precision.encode())
+        lib.iw_set_option(ctx, b"gpu:debug_values", b"1")
+        ok = bool(lib.iw_process_image(ctx))
+        res = _collect(lib, ctx, ok, [])
+        arrays = []
+        for which in range(3):
+            dims = (C.c_int * 3)()
+            n = f(ctx, which, None, 0, dims)
+            a = np.empty(max(n, 0), dtype=np.float64)
+            if n > 0:
+                f(ctx, which, a.ctypes.data, n, dims)
+                a = a.reshape(tuple(dims))
+            arrays.append(a)
+        return res, arrays[0], arrays[1], arrays[2], _stats_dict(lib, ctx)
+    finally:
+        lib.iw_destroy_context(ctx)
+
+
+def fp_error(lib: IWLib, job: Job) -> dict:
+    """Max and RMS error of the fp32 form's linear-light values against the
+    fp64 form's (which are the reference's), at the two points the reference
+    stores them: the float intermediate after the vertical pass and the value
+    each output sample is quantised from; plus how many samples exceed the
+    fp32 form's own bound (must be 0) and the flagged-pixel fraction."""
+    import numpy as np
+    r32, i32, v32, e32, s32 = run_debug_values(lib, job, "fp32")
+    r64, i64, v64, _, s64 = run_debug_values(lib, job, "fp64")
+    out = {"form": s32["form"], "identical_output": r32.ok and r64.ok and r32.key() == r64.key()}
+    if s32["form"] != 1 or i32.shape != i64.shape or v32.shape != v64.shape:
+        out["note"] = "the fp32 form does not take this configuration"
+        return out
+    di = np.abs(i32 - i64)
+    ok = ~(np.isnan(v32) | np.isnan(v64))
+    dv = np.abs(v32 - v64)[ok]
+    eb = e32[ok]
+    npx = v32.shape[1] * v32.shape[2]
+    out.update({
+        "interm_max": float(di.max()) if di.size else 0.0,
+        "interm_rms": float(np.sqrt(np.mean(di * di))) if di.size else 0.0,
+        "final_max": float(dv.max()) if dv.size else 0.0,
+        "final_rms": float(np.sqrt(np.mean(dv * dv))) if dv.size else 0.0,
+        "final_bound_max": float(eb.max()) if eb.size else 0.0,
+        "final_max_over_bound": float((dv / np.maximum(eb, 1e-300)).max()) if dv.size else 0.0,
+        "bound_violations": int((dv > eb).sum()),
+        "samples": int(dv.size), "flagged_fraction": s32["flagged"] / npx,
+        "flagged_left_to_fp64": s32["flagged_exact"], "vertical_tensor": s32["vertical_tensor"],
+    })
+    return out

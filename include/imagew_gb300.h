@@ -50,6 +50,16 @@ struct iwg_stats {
 	int graph;             /* 1: iwg_process_image_timed replayed the passes
 	                          as a CUDA graph (ms_device is then the mean time
 	                          of one replay) */
+	int fused;             /* 1: the fp32 form ran its vertical and
+	                          horizontal passes as one fused launch (no
+	                          intermediate image in device memory; see the
+	                          "gpu:fuse" option) */
+	double ms_phase[6];    /* iw_process_image() by phase, ms: [0] planning
+	                          (host), [1] input upload, [2] device passes,
+	                          [3] output download (these three by CUDA events
+	                          on the library's stream), [4] output post-pass
+	                          (host), [5] the device part's host wall time
+	                          (tables, launches, waits; contains 1-3) */
 };
 
 /* Copies the statistics of the context's last run into *out.  Returns 1. */
@@ -62,6 +72,22 @@ IW_EXPORT(int) iwg_get_stats(struct iw_context *ctx, struct iwg_stats *out);
  * what iw_process_image() returns.  Meant for benchmarking the pixel passes
  * apart from host<->device transfers.  Returns 1 on success. */
 IW_EXPORT(int) iwg_process_image_timed(struct iw_context *ctx, int warmup, int iters);
+
+/* Debug readback for measuring the FP32 form's error against the FP64 form.
+ * No counterpart in the reference.  After iw_process_image() on a context
+ * with the option "gpu:debug_values" set to "1" (integer output), copies one
+ * array of the run into out (at most max_count doubles) and its three
+ * dimensions into dims (if not NULL):
+ *   which 0: the intermediate image after the vertical pass, one plane per
+ *            intermediate channel (alpha in its own plane), [n][rows][cols];
+ *   which 1: per output sample, the linear-light value the quantisation
+ *            starts from (after unassociating alpha), [channel][row][col];
+ *   which 2: the FP32 form's rigorous bound on that value's distance from
+ *            the FP64 form's (0 in the FP64 form).
+ * NaN marks a sample the tail decided without a value (a blackened colour
+ * sample, an undecidable alpha).  Returns the array's length (also with
+ * out == NULL), or -1 for an unknown 'which'. */
+IW_EXPORT(long long) iwg_debug_values(struct iw_context *ctx, int which, double *out, long long max_count, int *dims);
 
 /* Writes a one-line description of the CUDA device the library uses into
  * buf (NUL-terminated, at most buflen bytes).  Returns 0 if no device. */

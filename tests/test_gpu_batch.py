@@ -65,9 +65,9 @@ def test_batch_repeat_is_stable(gpulib):
     assert [r.key() for r in a] == [r.key() for r in b]
 
 
-@pytest.mark.parametrize("mode", ["zero", "copy", "stage"])
+@pytest.mark.parametrize("mode", ["zero", "copy", "stage", "pull"])
 def test_transfer_modes_identical(gpulib, mode):
-    """Zero copy, cudaMemcpy and pinned staging give the same bytes, alone and batched."""
+    """Zero copy, cudaMemcpy, pinned staging and the pull kernel give the same bytes, alone and batched."""
     jobs = W.batch(12, seed=41, max_side=600)
     opt = [("iw_set_option", b"gpu:upload", mode.encode())]
     ref = [run_job(gpulib, j) for j in jobs]
