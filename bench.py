@@ -339,7 +339,7 @@ def run_reference_arm(args, rank, world):
 
 
 def batch_leg(lib: IWLib, n_images: int, pool_size: int, cpu_threads: int, cpu_images: int,
-              modes=("stage", "copy", "zero")):
+              modes=("stage", "pull", "copy", "zero")):
     """The batched configuration: n_images contexts (image content drawn from a
     pool of pool_size generated images, sizes log-uniform 64..2048, gray/RGB/RGBA,
     8/16-bit, five filters, each fitted to a 256x256 box) through one

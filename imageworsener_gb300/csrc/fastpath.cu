@@ -25,6 +25,8 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -732,6 +734,11 @@ static FastState *fast_build(const Plan &P, const Job &J, bool batch, int tc_mod
 		for(int ntiles = std::max(1, F.out_w * 4 / maxc); ok && ntiles <= F.out_w && ftiles.empty(); ntiles++)
 			ftiles = plan_tiles(ntiles);
 	}
+	if(getenv("IWG_TRACE"))
+		fprintf(stderr, "iwg fast_build: vertical kind %d ns %d nch %d alpha %d depth %d px %d in_device %d arith %d "
+			"stream %d hwarp %d allow_fuse %d tiles %d mid %dx%d out %dx%d\n", FS->vv.kind, FS->vv.ns, FS->vv.nch,
+			FS->vv.alpha, FS->vv.depth, FS->vv.px, (int)in_device, (int)S.arith, (int)S.ok, (int)hwarp, (int)allow_fuse,
+			(int)ftiles.size(), F.mid_w, F.mid_h, F.out_w, F.out_h);
 	if(!ftiles.empty()) {
 		const void *k_ = nullptr;
 		if(FS->vv.alpha && FS->vv.depth == 16) k_ = (const void *)k_vhfuse<4, 4, true, 16, 2>;

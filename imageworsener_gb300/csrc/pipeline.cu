@@ -1637,6 +1637,35 @@ __global__ void __launch_bounds__(256) k_pull(uint8_t *dst, const uint8_t *src, 
 	if(t < n) dst[t] = src[t];
 }
 
+// The same for a batch: block b copies images b, b + grid, ... (16-byte
+// words where both ends are aligned, bytes otherwise).
+struct PullItem { uint8_t *dst; const uint8_t *src; unsigned long long n; };
+
+__global__ void __launch_bounds__(256) k_pull_many(const PullItem *items, int count)
+{
+	for(int it = blockIdx.x; it < count; it += gridDim.x) {
+		const PullItem p = items[it];
+		if(((uintptr_t)p.src | (uintptr_t)p.dst) & 15) {
+			for(unsigned long long b = threadIdx.x; b < p.n; b += blockDim.x) p.dst[b] = p.src[b];
+			continue;
+		}
+		const unsigned long long n16 = p.n / 16;
+		const uint4 *s16 = reinterpret_cast<const uint4 *>(p.src);
+		uint4 *d16 = reinterpret_cast<uint4 *>(p.dst);
+		unsigned long long i = threadIdx.x;
+		for(; i + 3 * blockDim.x < n16; i += 4 * blockDim.x) {
+			const uint4 a = s16[i], b = s16[i + blockDim.x], c = s16[i + 2 * blockDim.x], d = s16[i + 3 * blockDim.x];
+			d16[i] = a;
+			d16[i + blockDim.x] = b;
+			d16[i + 2 * blockDim.x] = c;
+			d16[i + 3 * blockDim.x] = d;
+		}
+		for(; i < n16; i += blockDim.x) d16[i] = s16[i];
+		const unsigned long long t = n16 * 16 + threadIdx.x;
+		if(t < p.n) p.dst[t] = p.src[t];
+	}
+}
+
 struct Piece { uint8_t *dst; const uint8_t *src; size_t n; };
 
 // memcpy of many pieces, split in 1 MiB parts over the host pool.
@@ -1856,7 +1885,8 @@ void preload_kernels()
 			(const void *)k_fix_wide_df<true>, (const void *)k_fix_wide_df<false>, (const void *)k_out_props,
 			(const void *)k_fix_leftover<true>, (const void *)k_fix_leftover<false>,
 			(const void *)k_fix_flagged_thread<true>, (const void *)k_fix_flagged_thread<false>,
-			(const void *)k_fix_df2<true>, (const void *)k_fix_df2<false>, (const void *)k_pull})
+			(const void *)k_fix_df2<true>, (const void *)k_fix_df2<false>, (const void *)k_pull,
+			(const void *)k_pull_many})
 			cudaFuncGetAttributes(&a, k);
 		preload_fast_kernels();
 		preload_batch_kernels();
@@ -1962,7 +1992,7 @@ int plain_launch(cudaStream_t st, const Plan &P, const Job &J, Mark mark);
 // already queued); "zero" on a server's scan lanes.  'resident' runs need
 // the input on the device.
 enum { UP_ZERO = 0, UP_COPY = 1, UP_STAGE = 2, UP_PULL = 3 };
-static int upload_mode(iw_context *ctx, const DeviceState &S, bool resident, bool many = false)
+static int upload_mode(iw_context *ctx, const DeviceState &S, bool resident, bool many = false, bool pull_many = false)
 {
 	const char *u = get_option(ctx, "gpu:upload");
 	// scan lanes (a server's error-diffusion requests: small images, many
@@ -1974,6 +2004,7 @@ static int upload_mode(iw_context *ctx, const DeviceState &S, bool resident, boo
 	if(u && !strcmp(u, "stage")) m = UP_STAGE;
 	else if(u && !strcmp(u, "zero")) m = UP_ZERO;
 	else if(u && !strcmp(u, "pull")) m = UP_PULL;
+	if(m == UP_PULL && many && pull_many && S.pageable) return m;   // a batch: one copy kernel for every image
 	if(m == UP_PULL && (!S.pageable || many || ((uintptr_t)ctx->img1.pixels & 15))) m = UP_COPY;
 	if(m == UP_ZERO && (!S.pageable || resident)) m = UP_COPY;
 	return m;
@@ -2505,7 +2536,7 @@ bool run_batch(const std::vector<iw_context *> &ctxs, const std::vector<Plan *> 
 	if(sel.empty()) return true;
 
 	// one transfer mode for the batch: the first image's
-	const int upmode = upload_mode(ctxs[sel[0]], S, false, true);
+	const int upmode = upload_mode(ctxs[sel[0]], S, false, true, true);
 	const bool zc = upmode == UP_ZERO;
 	// buffers of every image, the packed weight lists and the flag list in one block
 	size_t top = 0;
@@ -2588,6 +2619,15 @@ bool run_batch(const std::vector<iw_context *> &ctxs, const std::vector<Plan *> 
 	std::vector<Job> djobs(m);
 	for(int k = 0; k < m; k++) djobs[k] = jobs[item_img[k]];
 	const size_t o_jobs = add(djobs.data(), djobs.size() * sizeof(Job));
+	size_t o_pull = 0;
+	if(upmode == UP_PULL) {
+		std::vector<PullItem> pv(m);
+		for(int k = 0; k < m; k++) {
+			const int i = item_img[k];
+			pv[k] = PullItem{base + o_in[i], (const uint8_t *)ctxs[i]->img1.pixels, (unsigned long long)in_bytes[i]};
+		}
+		o_pull = add(pv.data(), pv.size() * sizeof(PullItem));
+	}
 	auto fail_all = [&](const char *msg) {
 		for(int k = 0; k < m; k++) {
 			iw_set_error(ctxs[item_img[k]], msg);
@@ -2628,6 +2668,11 @@ bool run_batch(const std::vector<iw_context *> &ctxs, const std::vector<Plan *> 
 		}
 		if(!stage_h2d(S.stager, st, xs)) return fail_all("Out of pinned host memory");
 	}
+	if(upmode == UP_PULL) {
+		int sms = 152;
+		cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, S.device);
+		k_pull_many<<<(unsigned)std::min(m, 8 * sms), 256, 0, st>>>((const PullItem *)(tbase + o_pull), m);
+	}
 	cudaMemsetAsync(flag_count, 0, 3 * sizeof(int), st);
 	cudaEvent_t ev_h, ev_f;
 	cudaEventCreate(&ev_h);
@@ -2652,7 +2697,7 @@ bool run_batch(const std::vector<iw_context *> &ctxs, const std::vector<Plan *> 
 			const int i = item_img[k];
 			cudaMemcpyAsync(ctxs[i]->img2.pixels, base + o_out[i], out_bytes[i], cudaMemcpyDeviceToHost, st);
 		}
-	if(upmode == UP_STAGE) {
+	if(upmode == UP_STAGE || upmode == UP_PULL) {
 		std::vector<Xfer> xs;
 		for(int k = 0; k < m; k++) {
 			const int i = item_img[k];
