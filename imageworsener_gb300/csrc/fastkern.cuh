@@ -546,9 +546,12 @@ __device__ __forceinline__ void vbulk_tile(const FJob &F, unsigned char *s_raw, 
 // and the guarded quantisation tail of those rows' output pixels from shared
 // memory (same operations and order as hpass_pixel, so the same values,
 // bounds, codes and flags as the two-kernel form).
-// Requirements (checked by the host): at most one output row finishes per
-// input position (downscales), the tile's input columns fit one strip of
-// kBulkConsumers * PX pixels, every horizontal source of the tile lies in
+// Rows are summed horizontally two at a time, as soon as the second one
+// finishes, wherever they finish (several rows can finish at one input
+// position where the image's last row ends their windows): the four-row
+// ring then always holds the two rows being summed and at most two filling.
+// Requirements (checked by the host): the tile's input columns fit one strip
+// of kBulkConsumers * PX pixels, every horizontal source of the tile lies in
 // [xa, xa + nc), rows 16-byte aligned, nc * bytes per pixel a multiple of 16.
 // ---------------------------------------------------------------------------
 template<int NPL>
@@ -728,7 +731,7 @@ __device__ __forceinline__ void vhfuse_tile(const FJob &F, const FuseTile *tiles
 			for(int c = 0; c < NCH; c++) acc[s][c] = f2_fma(v2[c], w2, acc[s][c]);
 		}
 		const int2 fin = s_fin[q];
-		for(int k = 0; k < fin.y; k++) {   // at most one row per position (checked by the host)
+		for(int k = 0; k < fin.y; k++) {
 			const int j = fin.x + k;
 			const int sj = j % NS;
 			const bool keep = j >= jb && j < je;

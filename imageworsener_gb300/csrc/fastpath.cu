@@ -703,19 +703,16 @@ static FastState *fast_build(const Plan &P, const Job &J, bool batch, int tc_mod
 	if(!FS->vkernel) { delete FS; err = "fast form: no kernel for this layout"; return nullptr; }
 	FS->in_device = in_device;
 	// Fused vertical + horizontal pass: where the bulk-copy vertical pass runs
-	// (rows in device memory, 16-byte aligned), at most one output row
-	// finishes per input position (downscales), and the horizontal windows
-	// are narrow (a thread per pixel).  Column tiles are chosen so that each
+	// (rows in device memory, 16-byte aligned) and the horizontal windows are
+	// narrow (a thread per pixel).  Column tiles are chosen so that each
 	// tile's input columns, widened to 16-byte boundaries, fit one strip.
 	std::vector<FuseTile> ftiles;
 	if(allow_fuse && !batch && FS->vv.kind == 4 && FS->vv.nch == 4 && FS->vv.px == 2 && FS->vv.ns == 4 && !hwarp &&
 		WH.kind == RowKind::Sum && F.mid_h == F.out_h) {
-		int max_fin = 0;
-		for(size_t q = 1; q < S.pinfo.size(); q += 2) max_fin = std::max(max_fin, S.pinfo[q]);
 		const int al = 16 / v_bpp;   // columns per 16 bytes
 		const int maxc = kBulkConsumers * FS->vv.px;
 		const long long row_cols = (long long)P.in_bpr / v_bpp - P.crop_x;   // columns a row's bytes hold from the crop
-		bool ok = max_fin <= 1 && 16 % v_bpp == 0;
+		bool ok = 16 % v_bpp == 0;
 		auto plan_tiles = [&](int ntiles) {
 			std::vector<FuseTile> t;
 			const int tw = (F.out_w + ntiles - 1) / ntiles;
