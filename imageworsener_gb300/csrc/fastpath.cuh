@@ -17,7 +17,7 @@ struct FastInfo {
 	int tc_mode = 1;     // in: vertical pass on the tensor cores: 0 never, 1 wide windows, 2 whenever eligible
 	int tc = 0;          // out: the vertical pass runs on the tensor cores
 	int autotune = 1;    // in: choose the vertical pass's band count by measurement (cached per geometry)
-	int fuse_mode = 1;   // in: 1 fuse the vertical and horizontal passes where possible, 0 never
+	int fuse_mode = 0;   // in: 1 fuse the vertical and horizontal passes where possible, 0 never
 	int fused = 0;       // out: the passes run as one fused launch
 	int wait_polls = 0;  // in: >0 shortens the vertical pipeline's bounded waits (failure tests)
 	int starve = 0;      // in: 1: the pipeline's producer issues nothing, so its waits run out (failure tests)

@@ -2223,8 +2223,11 @@ bool run_pipeline(iw_context *ctx, Plan &P, int warmup, int iters, int lane)
 		fi.tc_mode = (vt && !strcmp(vt, "cuda")) ? 0 : ((vt && !strcmp(vt, "tensor")) ? 2 : 1);
 		const char *at = get_option(ctx, "gpu:autotune");
 		fi.autotune = !(at && !strcmp(at, "off"));
+		// the fused pass is measured slower than the two passes today (its
+		// vertical and horizontal phases serialise inside each block): on
+		// request only
 		const char *fu = get_option(ctx, "gpu:fuse");
-		fi.fuse_mode = !(fu && !strcmp(fu, "off"));
+		fi.fuse_mode = (fu && !strcmp(fu, "on")) ? 1 : 0;
 		// failure tests: gpu:wait_test=1 starves the bulk-copy pipeline (its
 		// producer issues no copies, so no barrier it waits on ever
 		// completes) and shortens its waits to a few thousand polls

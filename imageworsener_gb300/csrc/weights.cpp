@@ -11,6 +11,9 @@
 
 #include <cmath>
 #include <cstring>
+#include <map>
+#include <mutex>
+#include <tuple>
 
 #ifndef M_PI
 #define M_PI 3.14159265358979323846
@@ -20,6 +23,7 @@ namespace iwg {
 
 bool Weights::same_as(const Weights &o) const
 {
+	if(this == &o) return true;   // the same memoized list
 	return kind == o.kind && n_in == o.n_in && n_out == o.n_out && edge_value == o.edge_value &&
 		off == o.off && src == o.src && w == o.w && pos == o.pos;
 }
@@ -236,6 +240,24 @@ std::shared_ptr<const Weights> build_weights(iw_context *ctx, const DimRequest &
 			return nullptr;
 		}
 	}
+	// Weight lists depend only on the settings setup_dim reads and the sizes:
+	// built once per process for each distinct set (a plan asks for one per
+	// intermediate channel and dimension, and a server or a batch sees the
+	// same geometries again and again).  Bounded: cleared past kMemoMax.
+	auto bits = [](double v) { uint64_t b; memcpy(&b, &v, sizeof b); return b; };
+	const double eff_offset = S.offset;
+	const double eff_edge = S.edge_value;
+	using Key = std::tuple<int, int, uint64_t, uint64_t, uint64_t, uint64_t, uint64_t, uint64_t, int, int>;
+	const Key key{d.family, d.edge, bits(d.blur), bits(d.p1), bits(d.p2), bits(d.true_size), bits(eff_offset),
+		bits(eff_edge), n_in, n_out};
+	static std::mutex memo_mu;
+	static std::map<Key, std::shared_ptr<const Weights>> *memo = new std::map<Key, std::shared_ptr<const Weights>>();
+	constexpr size_t kMemoMax = 1024;
+	{
+		std::lock_guard<std::mutex> lk(memo_mu);
+		auto it = memo->find(key);
+		if(it != memo->end()) return it->second;
+	}
 	auto wt = std::make_shared<Weights>();
 	wt->n_in = n_in;
 	wt->n_out = n_out;
@@ -265,6 +287,11 @@ std::shared_ptr<const Weights> build_weights(iw_context *ctx, const DimRequest &
 		}
 		if(sa > wt->wsum_abs_max) wt->wsum_abs_max = sa;
 		if(sn > wt->wsum_neg_max) wt->wsum_neg_max = sn;
+	}
+	{
+		std::lock_guard<std::mutex> lk(memo_mu);
+		if(memo->size() >= kMemoMax) memo->clear();
+		(*memo)[key] = wt;
 	}
 	return wt;
 }

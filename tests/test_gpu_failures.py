@@ -28,8 +28,8 @@ pytestmark = pytest.mark.gpu
 def _job(extra, fuse=True):
     job = W.precision(n=1024, out=250)
     job.calls = list(job.calls) + [("iw_set_option", b"gpu:autotune", b"off")] + list(extra)
-    if not fuse:
-        job.calls.append(("iw_set_option", b"gpu:fuse", b"off"))
+    if fuse:
+        job.calls.append(("iw_set_option", b"gpu:fuse", b"on"))
     return job
 
 

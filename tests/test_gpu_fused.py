@@ -1,7 +1,7 @@
 """The fused vertical + horizontal pass of the fp32 form (one launch, the
-intermediate rows kept in shared memory) against the CPU oracle and against
-the same library with fusion off (option gpu:fuse=off: the two-kernel form
-with the intermediate image in device memory).  16-bit RGBA downscales with
+intermediate rows kept in shared memory; option gpu:fuse=on) against the CPU
+oracle and against the default two-kernel form (the intermediate image in
+device memory).  16-bit RGBA downscales with
 premultiplied alpha are the layout it takes; the cases vary the width (tile
 planning, 16-byte alignment of the tile strips), the scale factor, the
 filter, crops, dither and the output size.  Integer output: byte-identical."""
@@ -49,19 +49,23 @@ def test_fused_matches_oracle_and_unfused(gpulib, oracle, case):
     seed = 1000 + CASES.index(case)
     job = make_job(case, seed)
     want = run_job(oracle, job)
+    job.calls = list(job.calls) + [("iw_set_option", b"gpu:fuse", b"on")]
     got, st = run_job_stats(gpulib, job)
     assert got.ok, got.error
     assert st["form"] == 1
     job_off = make_job(case, seed)
-    job_off.calls = list(job_off.calls) + [("iw_set_option", b"gpu:fuse", b"off")]
     off, st_off = run_job_stats(gpulib, job_off)
     assert st_off["fused"] == 0
     assert got.key() == want.key(), "fused output differs from the oracle"
     assert off.key() == want.key(), "two-kernel output differs from the oracle"
 
 
-def test_precision_workload_is_fused(gpulib):
-    """The precision configuration takes the fused pass (and stays
-    byte-identical: its full-size digest is checked in test_gpu_parity)."""
-    res, st = run_job_stats(gpulib, W.precision(n=1024, out=250))
+def test_precision_workload_takes_fused_pass_on_request(gpulib, oracle):
+    """The precision configuration's layout takes the fused pass when asked,
+    with the reference's bytes."""
+    job = W.precision(n=1024, out=250)
+    want = run_job(oracle, job)
+    job.calls = list(job.calls) + [("iw_set_option", b"gpu:fuse", b"on")]
+    res, st = run_job_stats(gpulib, job)
     assert res.ok and st["form"] == 1 and st["fused"] == 1
+    assert res.key() == want.key()
