@@ -131,6 +131,29 @@ __device__ __forceinline__ dfl df_add(dfl x, dfl y)
 	return df_fast_two_sum(v.hi, __fadd_rn(t.lo, v.lo));
 }
 
+// x + y with the error bounded by the operands' magnitudes rather than the
+// result's: TwoSum of the high parts, the low parts added in FP32, one
+// renormalisation.  |error| <= 2.01 u^2 (|x| + |y|) (one rounding of the
+// low parts' sum, below u^2 (|x| + |y|), and one of its sum with the
+// TwoSum error, below u^2 |x.hi + y.hi| (1 + u)^2).  Where a bound is
+// stated in the sum of the terms' magnitudes -- a running sum of n terms
+// gains at most 2.01 n u^2 of it -- this is as good as the accurate form
+// in far fewer operations.
+__device__ __forceinline__ dfl df_add_sloppy(dfl x, dfl y)
+{
+	const dfl s = df_two_sum(x.hi, y.hi);
+	return df_fast_two_sum(s.hi, __fadd_rn(s.lo, __fadd_rn(x.lo, y.lo)));
+}
+
+// A float times a double-float: the exact product of the high parts
+// (TwoProd by FMA) plus the low part's product; error below 2 u^2 |x y|.
+__device__ __forceinline__ dfl df_mul_f(float x, dfl y)
+{
+	const float p = __fmul_rn(x, y.hi);
+	const float e = __fmaf_rn(x, y.hi, -p);
+	return df_fast_two_sum(p, __fmaf_rn(x, y.lo, e));
+}
+
 __device__ __forceinline__ dfl df_mul(dfl x, dfl y)
 {
 	const float ch = __fmul_rn(x.hi, y.hi);

@@ -972,7 +972,7 @@ __device__ __forceinline__ bool fix_df_finish(const Job &J, int i, int j, unsign
 				if(W.src[t0 + t] < 0) continue;
 				const float I = my[lane * maxt + t];
 				const dfl w = df_of(J.df_wh[t0 + t]);
-				s = df_add(s, df_mul({I, 0.0f}, w));
+				s = df_add_sloppy(s, df_mul_f(I, w));   // per term below 3u^2 (table) + 2u^2 + 2.01u^2 of A
 				A = __fmaf_rn(fabsf(I), fabsf(w.hi), A);
 			}
 		}
@@ -1126,9 +1126,41 @@ __global__ void __launch_bounds__(128, 8) k_fix_flagged_warp(Job J1, const Job *
 // pairs in turn and sum their nv terms, certifying each float32
 // intermediate as interm_df_all does.  Step 3 is fix_df_finish.
 // Bound (u = 2^-24, A = sum of |term|): table values u^2 each (v, a, w),
-// two double-float products 5u^2 each, n accurate additions 3u^2 of the
-// running magnitude: (13 + 3n) u^2 A <= 24 n u^2 A, as interm_df_all.
+// two double-float products 5u^2 each, n additions 2.01u^2 of the running
+// magnitude (df_add_sloppy): (13 + 2.01n) u^2 A <= 24 n u^2 A, as
+// interm_df_all.
 constexpr int kFix2MaxTaps = 32;
+
+// The codes of every channel of stored pixel (px, py): one aligned 8- or
+// 4-byte load for 16-bit RGBA and 8-bit RGBA rows (where 'wide' says the
+// image's rows and base allow it), else byte loads.
+__device__ __forceinline__ void pixel_codes(const Job &J, int px, int py, bool wide, unsigned int (&c)[dev::kMaxCh])
+{
+	const uint8_t *row = J.in + (unsigned long long)py * J.in_bpr;
+	if(wide && J.in_depth == 16) {
+		const uint2 v = __ldg(reinterpret_cast<const uint2 *>(row) + px);
+		c[0] = __byte_perm(v.x, 0u, 0x4401u);
+		c[1] = __byte_perm(v.x, 0u, 0x4423u);
+		c[2] = __byte_perm(v.y, 0u, 0x4401u);
+		c[3] = __byte_perm(v.y, 0u, 0x4423u);
+		return;
+	}
+	if(wide) {
+		const unsigned int v = __ldg(reinterpret_cast<const unsigned int *>(row) + px);
+#pragma unroll
+		for(int k = 0; k < dev::kMaxCh; k++) c[k] = (v >> (8 * k)) & 0xffu;
+		return;
+	}
+#pragma unroll
+	for(int k = 0; k < dev::kMaxCh; k++) c[k] = k < J.in_nphys ? raw_code(J, px, py, k) : 0u;
+}
+
+// c[k] for a run-time k, by selects (an indexed register array would live in
+// local memory)
+__device__ __forceinline__ unsigned int pick4(const unsigned int (&c)[dev::kMaxCh], int k)
+{
+	return k == 0 ? c[0] : (k == 1 ? c[1] : (k == 2 ? c[2] : c[3]));
+}
 
 __device__ bool fix_pixel_df2(const Job &J, int i, int j, unsigned int mask, float2 *P, int pstride, float *my, int maxt,
 	int lane)
@@ -1141,19 +1173,30 @@ __device__ bool fix_pixel_df2(const Job &J, int i, int j, unsigned int mask, flo
 	for(int m = 0; m < dev::kMaxCh; m++)
 		if(m < J.mid_n && ((mask >> m) & 1u) && J.mid[m].unassoc) need_alpha = true;
 	need_alpha = need_alpha && J.in_alpha < J.in_nphys && J.df_atab != nullptr;
+	// whole-pixel loads: 4 channels of 16 or 8 bits, rows and base aligned
+	const bool wide = J.in_nphys == 4 && (J.in_depth == 16 || J.in_depth == 8) &&
+		(((uintptr_t)J.in | (uintptr_t)J.in_bpr) & (J.in_depth == 16 ? 7u : 3u)) == 0;
 	const int ntask = nv * nh;
+	// lane's task k = r * nh + t, advanced by 32 at a time without division
+	const float inv_nh = 1.0f / (float)nh;
 	// step 1: four pixels per lane in flight
 	for(int k0 = 0; k0 < ntask; k0 += 128) {
-		int px[4], py[4];
+		int px[4], py[4], rr[4];
 		bool live[4];
-		unsigned int ac[4], cc[4][dev::kMaxCh];
+		unsigned int cc[4][dev::kMaxCh];
 #pragma unroll
 		for(int u = 0; u < 4; u++) {
 			const int k = k0 + 32 * u + lane;
 			live[u] = false;
 			px[u] = py[u] = 0;
+			rr[u] = 0;
 			if(k < ntask) {
-				const int r = k / nh, t = k - r * nh;
+				// k < 2^12 here: the float quotient is exact enough to floor (checked below)
+				int r = __float2int_rz(__fmul_rn((float)k + 0.5f, inv_nh));
+				r -= (r * nh > k) ? 1 : 0;
+				r += ((r + 1) * nh <= k) ? 1 : 0;
+				const int t = k - r * nh;
+				rr[u] = r;
 				const int sv = WV.src[vt0 + r], sh = WH.src[ht0 + t];
 				live[u] = sv >= 0 && sh >= 0;
 				px[u] = J.crop_x + (sh < 0 ? 0 : sh);
@@ -1162,33 +1205,29 @@ __device__ bool fix_pixel_df2(const Job &J, int i, int j, unsigned int mask, flo
 		}
 #pragma unroll
 		for(int u = 0; u < 4; u++) {
-			ac[u] = 0;
-			if(live[u] && need_alpha) ac[u] = raw_code(J, px[u], py[u], J.in_alpha);
+			if(live[u]) pixel_codes(J, px[u], py[u], wide, cc[u]);
+			else {
 #pragma unroll
-			for(int m = 0; m < dev::kMaxCh; m++) {
-				cc[u][m] = 0;
-				if(live[u] && m < J.mid_n && ((mask >> m) & 1u) && J.mid[m].in_ch < J.in_nphys)
-					cc[u][m] = raw_code(J, px[u], py[u], J.mid[m].in_ch);
+				for(int m = 0; m < dev::kMaxCh; m++) cc[u][m] = 0u;
 			}
 		}
 		float2 av[4], vv[4][dev::kMaxCh];
 #pragma unroll
 		for(int u = 0; u < 4; u++) {
 			av[u] = make_float2(1.0f, 0.0f);
-			if(live[u] && need_alpha) av[u] = __ldg(J.df_atab + ac[u]);
+			if(live[u] && need_alpha) av[u] = __ldg(J.df_atab + pick4(cc[u], J.in_alpha));
 #pragma unroll
 			for(int m = 0; m < dev::kMaxCh; m++) {
 				vv[u][m] = make_float2(1.0f, 0.0f);
 				if(live[u] && m < J.mid_n && ((mask >> m) & 1u) && J.mid[m].in_ch < J.in_nphys)
-					vv[u][m] = __ldg(J.df_tab[m] + cc[u][m]);
+					vv[u][m] = __ldg(J.df_tab[m] + pick4(cc[u], J.mid[m].in_ch));
 			}
 		}
 #pragma unroll
 		for(int u = 0; u < 4; u++) {
 			const int k = k0 + 32 * u + lane;
 			if(k >= ntask) continue;
-			const int r = k / nh;
-			const dfl w = WV.kind == 1 ? dfl{1.0f, 0.0f} : df_of(__ldg(J.df_wv + vt0 + r));
+			const dfl w = WV.kind == 1 ? dfl{1.0f, 0.0f} : df_of(__ldg(J.df_wv + vt0 + rr[u]));
 			const dfl aw = need_alpha ? df_mul(df_of(av[u]), w) : w;
 #pragma unroll
 			for(int m = 0; m < dev::kMaxCh; m++) {
@@ -1200,25 +1239,29 @@ __device__ bool fix_pixel_df2(const Job &J, int i, int j, unsigned int mask, flo
 		}
 	}
 	__syncwarp();
-	// step 2: one (channel, horizontal tap) sum per lane at a time
+	// step 2: one (channel, horizontal tap) sum per lane at a time; terms
+	// added with df_add_sloppy (2.01 u^2 of the magnitudes so far each)
 	const float kd = (float)(24 * nv) * 3.5527137e-15f + (float)(2 * nv + 2) * 1.1102231e-16f;
 	const int nm = __popc(mask);
 	bool bad = false;
+	int r = 0, t = lane;
+	while(t >= nh) { t -= nh; r++; }
 	for(int k = lane; k < nm * nh; k += 32) {
-		const int r = k / nh, t = k - r * nh;
 		const int m = nth_bit(mask, r);
 		const float2 *col = P + m * pstride + t;
 		dfl acc = {0.0f, 0.0f};
 		float A = 0.0f;
 		for(int q = 0; q < nv; q++) {
 			const float2 v = col[q * nh];
-			acc = df_add(acc, df_of(v));
+			acc = df_add_sloppy(acc, df_of(v));
 			A = __fadd_rn(A, fabsf(v.x));
 		}
 		my[m * maxt + t] = acc.hi;
 		const float delta = __fmaf_rn(A * 1.01f, kd, 1e-30f);
 		// A == 0: every term is exactly zero (see interm_df_all)
 		if(!(A == 0.0f || rounds_to_hi(acc, delta))) bad = true;
+		t += 32;
+		while(t >= nh) { t -= nh; r++; }
 	}
 	if(__any_sync(0xffffffffu, bad)) return false;
 	__syncwarp();
