@@ -1176,9 +1176,9 @@ __device__ bool fix_pixel_df2(const Job &J, int i, int j, unsigned int mask, flo
 	// whole-pixel loads: 4 channels of 16 or 8 bits, rows and base aligned
 	const bool wide = J.in_nphys == 4 && (J.in_depth == 16 || J.in_depth == 8) &&
 		(((uintptr_t)J.in | (uintptr_t)J.in_bpr) & (J.in_depth == 16 ? 7u : 3u)) == 0;
-	const int ntask = nv * nh;
-	// lane's task k = r * nh + t, advanced by 32 at a time without division
-	const float inv_nh = 1.0f / (float)nh;
+	const int ntask = nv * nh;   // 0 if either window is empty
+	// lane's task k = r * nh + t, found without an integer division
+	const float inv_nh = nh > 0 ? 1.0f / (float)nh : 0.0f;
 	// step 1: four pixels per lane in flight
 	for(int k0 = 0; k0 < ntask; k0 += 128) {
 		int px[4], py[4], rr[4];
@@ -1244,9 +1244,12 @@ __device__ bool fix_pixel_df2(const Job &J, int i, int j, unsigned int mask, flo
 	const float kd = (float)(24 * nv) * 3.5527137e-15f + (float)(2 * nv + 2) * 1.1102231e-16f;
 	const int nm = __popc(mask);
 	bool bad = false;
+	// (t, r) of task k = lane, advanced by 32 per step; a window without
+	// taps (nh == 0) has no sums to take
 	int r = 0, t = lane;
-	while(t >= nh) { t -= nh; r++; }
-	for(int k = lane; k < nm * nh; k += 32) {
+	if(nh > 0)
+		while(t >= nh) { t -= nh; r++; }
+	for(int k = lane; nh > 0 && k < nm * nh; k += 32) {
 		const int m = nth_bit(mask, r);
 		const float2 *col = P + m * pstride + t;
 		dfl acc = {0.0f, 0.0f};
