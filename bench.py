@@ -193,12 +193,12 @@ def output_digest(lib: IWLib, ctx) -> str:
     return r.digest()
 
 
-def device_timed(lib: IWLib, job, warmup: int, steps: int, form: str, vertical: str = "auto"):
+def device_timed(lib: IWLib, job, warmup: int, steps: int, form: str, vertical: str = "auto", extra=()):
     lib.dll.iwg_process_image_timed.restype = C.c_int
     lib.dll.iwg_process_image_timed.argtypes = [C.c_void_p, C.c_int, C.c_int]
     lib.dll.iwg_get_stats.argtypes = [C.c_void_p, C.POINTER(Stats)]
     ctx = make_ctx(lib, job, [("iw_set_option", b"gpu:precision", form.encode()),
-                              ("iw_set_option", b"gpu:vertical", vertical.encode())])
+                              ("iw_set_option", b"gpu:vertical", vertical.encode())] + list(extra))
     try:
         ok = lib.dll.iwg_process_image_timed(ctx, warmup, steps)
         if not ok:
@@ -584,6 +584,8 @@ def main():
     ap.add_argument("--serve-seconds", type=float, default=60.0, help="serving leg: length of the arrival stream (0: skip)")
     ap.add_argument("--serve-rate", type=float, default=2000.0, help="serving leg: requests per second")
     ap.add_argument("--no-large", action="store_true", help="skip the large-downscale leg")
+    ap.add_argument("--fuse", action="store_true",
+                    help="device-timed leg with the fused vertical+horizontal pass (option gpu:fuse=on)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     rank, world, local = dist_env()
@@ -613,7 +615,8 @@ def main():
     with ClockSampler(local) as clk:
         barrier()
         progress("device-timed fp32")
-        st, dig_fast = device_timed(lib, job, args.warmup, args.steps, "fp32")
+        st, dig_fast = device_timed(lib, job, args.warmup, args.steps, "fp32",
+                                    extra=[("iw_set_option", b"gpu:fuse", b"on")] if args.fuse else ())
         barrier()
         progress("device-timed fp64")
         st64, dig_plain = device_timed(lib, job, 1, max(2, min(args.steps, 5)), "fp64")
