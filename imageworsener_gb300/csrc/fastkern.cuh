@@ -1114,77 +1114,6 @@ __device__ __forceinline__ void hpass_pixel(const FJob &F, int i, int j)
 	hpass_tail<NPL>(F, i, j, v, T);
 }
 
-// Horizontal pass + tail for one output row segment, staged: the block
-// first copies the intermediate columns its pixels read ([xa, xa + nc) of
-// row j, every plane; coalesced loads) into shared memory, then each thread
-// sums its pixel's taps from there in exactly hpass_pixel's order (same
-// blocked partial sums, same operations), so values, bounds, codes and flags
-// are the same; only the loads differ.  Shared memory: NPL * ncmax floats.
-template<int NPL>
-__device__ __forceinline__ void hpass_stage_tile(const FJob &F, const int2 *segs, float *s_row, int ncmax, int bx, int j)
-{
-	const int2 sg = segs[bx];   // (xa, nc)
-	const float *rowbase = F.interm + (unsigned long long)j * F.mid_w + sg.x;
-#pragma unroll
-	for(int c = 0; c < NPL; c++)
-		for(int x = threadIdx.x; x < sg.y; x += blockDim.x)
-			s_row[c * ncmax + x] = __ldcs(rowbase + (unsigned long long)c * F.plane + x);
-	__syncthreads();
-	const int i = bx * blockDim.x + threadIdx.x;
-	if(i >= F.out_w || j >= F.out_h) return;
-	float v[NPL], T[NPL];
-#pragma unroll
-	for(int c = 0; c < NPL; c++) { v[c] = 0.0f; T[c] = 0.0f; }
-	const int t0 = F.hoff[i], t1 = F.hoff[i + 1];
-	const float *srow = s_row - sg.x;   // indexed by the input column
-	int t = t0;
-	while(t < t1) {
-		const int tb = min(t + kHBlock, t1);
-		float p[NPL];
-#pragma unroll
-		for(int c = 0; c < NPL; c++) p[c] = 0.0f;
-		for(; t + 4 <= tb; t += 4) {
-			int src[4];
-			float w[4], I[4][NPL];
-#pragma unroll
-			for(int u = 0; u < 4; u++) {
-				src[u] = __ldg(F.hsrc + t + u);
-				w[u] = __ldg(F.hw + t + u);
-			}
-#pragma unroll
-			for(int u = 0; u < 4; u++) {
-				const int sc = src[u] < 0 ? sg.x : src[u];
-#pragma unroll
-				for(int c = 0; c < NPL; c++) I[u][c] = srow[c * ncmax + sc];
-			}
-#pragma unroll
-			for(int u = 0; u < 4; u++) {
-				const float aw = fabsf(w[u]);
-#pragma unroll
-				for(int c = 0; c < NPL; c++) {
-					const float x = src[u] < 0 ? 0.0f : I[u][c];
-					p[c] = __fmaf_rn(x, w[u], p[c]);
-					T[c] = __fmaf_rn(fabsf(x), aw, T[c]);
-				}
-			}
-		}
-		for(; t < tb; t++) {
-			const int src = __ldg(F.hsrc + t);
-			if(src < 0) continue;   // transparent edge: value 0
-			const float w = __ldg(F.hw + t), aw = fabsf(w);
-#pragma unroll
-			for(int c = 0; c < NPL; c++) {
-				const float I = srow[c * ncmax + src];
-				p[c] = __fmaf_rn(I, w, p[c]);
-				T[c] = __fmaf_rn(fabsf(I), aw, T[c]);
-			}
-		}
-#pragma unroll
-		for(int c = 0; c < NPL; c++) v[c] = __fadd_rn(v[c], p[c]);
-	}
-	hpass_tail<NPL>(F, i, j, v, T);
-}
-
 // Horizontal pass for wide windows, a warp per output pixel (i, j): lane l
 // accumulates taps l, l+32, ... (fused multiply-adds from 0), then a butterfly
 // of five additions gives every lane the same total, so a product passes
@@ -1340,12 +1269,6 @@ struct FastState {
 	std::vector<int> first_pos, last_pos;
 	size_t vsmem_fixed = 0, vsmem_per_pos = 0;
 	bool in_device = false;
-	// staged horizontal pass (k_hpass_stage): per block column, the input
-	// columns its pixels read (xa, nc), and the widest of them
-	bool hstage = false;
-	size_t o_hseg = 0;
-	const int2 *hsegs = nullptr;
-	int hncmax = 0;
 	// fused vertical + horizontal pass (k_vhfuse, vkernel; no hkernel): its
 	// column tiles (device copy in the blob)
 	bool fuse = false;

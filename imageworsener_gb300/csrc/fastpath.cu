@@ -83,13 +83,6 @@ __global__ void __launch_bounds__(kHThreads) k_hpass_fast(FJob F)
 	hpass_pixel<NPL>(F, blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y);
 }
 
-template<int NPL>
-__global__ void __launch_bounds__(kHThreads) k_hpass_stage(FJob F, const int2 *segs, int ncmax)
-{
-	extern __shared__ __align__(16) float s_hrow[];
-	hpass_stage_tile<NPL>(F, segs, s_hrow, ncmax, blockIdx.x, blockIdx.y);
-}
-
 // wide windows: a warp per output pixel, kHThreads / 32 pixels per block
 template<int NPL>
 __global__ void __launch_bounds__(kHThreads) k_hpass_warp(FJob F)
@@ -341,11 +334,7 @@ void fast_launch_impl(cudaStream_t st, void *state, void (*mark)(void *), void *
 	else {
 		cudaLaunchKernel(S.vkernel, S.vgrid, dim3(S.vthreads), S.tc ? targs : fargs, S.vsmem, st);
 		mark(markarg);
-		if(S.hstage) {
-			void *hargs[] = {&S.F, &S.hsegs, &S.hncmax};
-			cudaLaunchKernel(S.hkernel, S.hgrid, dim3(kHThreads), hargs, (size_t)S.F.npl * S.hncmax * sizeof(float), st);
-		}
-		else cudaLaunchKernel(S.hkernel, S.hgrid, dim3(kHThreads), fargs, 0, st);
+		cudaLaunchKernel(S.hkernel, S.hgrid, dim3(kHThreads), fargs, 0, st);
 		mark(markarg);
 	}
 	// exact re-evaluation of flagged pixels (recomputes the vertical pass too)
@@ -812,32 +801,6 @@ static FastState *fast_build(const Plan &P, const Job &J, bool batch, int tc_mod
 		default: FS->hkernel = (const void *)k_hpass_fast<4>; break;
 		}
 		FS->hgrid = dim3((F.out_w + kHThreads - 1) / kHThreads, F.out_h);
-		// staged form: each block's input columns in shared memory (one image)
-		if(!batch && WH.kind == RowKind::Sum) {
-			const int gx = (int)FS->hgrid.x;
-			std::vector<int2> segs(gx);
-			int ncmax = 1;
-			for(int bx = 0; bx < gx; bx++) {
-				const int i0 = bx * kHThreads, i1 = std::min(F.out_w, i0 + kHThreads);
-				int lo = INT32_MAX, hi = -1;
-				for(int t2 = WH.off[i0]; t2 < WH.off[i1]; t2++)
-					if(WH.src[t2] >= 0) { lo = std::min(lo, WH.src[t2]); hi = std::max(hi, WH.src[t2]); }
-				if(hi < 0) { lo = 0; hi = 0; }
-				segs[bx] = make_int2(lo, hi - lo + 1);
-				ncmax = std::max(ncmax, hi - lo + 1);
-			}
-			if((size_t)nplanes * ncmax * sizeof(float) <= 48 * 1024) {
-				FS->hstage = true;
-				FS->hncmax = ncmax;
-				FS->o_hseg = add(segs.data(), segs.size() * sizeof(int2));
-				switch(nplanes) {
-				case 1: FS->hkernel = (const void *)k_hpass_stage<1>; break;
-				case 2: FS->hkernel = (const void *)k_hpass_stage<2>; break;
-				case 3: FS->hkernel = (const void *)k_hpass_stage<3>; break;
-				default: FS->hkernel = (const void *)k_hpass_stage<4>; break;
-				}
-			}
-		}
 	}
 	F.vgx = (int)FS->vgrid.x;
 	F.vgy = (int)FS->vgrid.y;
@@ -881,7 +844,6 @@ static void fast_place(FastState *FS, const uint8_t *base, int *flag_count, int 
 		T.lut = (const uint2 *)(base + FS->o_tcl);
 	}
 	FS->fuse_tiles = FS->fuse ? (const FuseTile *)(base + FS->o_fuse) : nullptr;
-	FS->hsegs = FS->hstage ? (const int2 *)(base + FS->o_hseg) : nullptr;
 	Job &J = FS->J;
 	for(int m = 0; m < dev::kMaxCh; m++) J.df_tab[m] = FS->df ? FS->df_tab[m] : nullptr;
 	J.df_atab = FS->df ? FS->df_atab : nullptr;
@@ -1103,10 +1065,6 @@ void preload_fast_kernels()
 	cudaFuncGetAttributes(&a, (const void *)k_vhfuse<4, 4, true, 16, 2>);
 	cudaFuncGetAttributes(&a, tc::tc_kernel(true));
 	cudaFuncGetAttributes(&a, tc::tc_kernel(false));
-	cudaFuncGetAttributes(&a, (const void *)k_hpass_stage<1>);
-	cudaFuncGetAttributes(&a, (const void *)k_hpass_stage<2>);
-	cudaFuncGetAttributes(&a, (const void *)k_hpass_stage<3>);
-	cudaFuncGetAttributes(&a, (const void *)k_hpass_stage<4>);
 	cudaFuncGetAttributes(&a, (const void *)k_hpass_fast<1>);
 	cudaFuncGetAttributes(&a, (const void *)k_hpass_fast<2>);
 	cudaFuncGetAttributes(&a, (const void *)k_hpass_fast<3>);
