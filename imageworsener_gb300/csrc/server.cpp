@@ -228,11 +228,14 @@ void dispatcher_loop(iwg_server *S)
 // A scan worker of class 'cls' (0 small, 1 large): takes queued requests of
 // its class that fit the device budget the workers share (a worker may take
 // one request whatever the budget when no other scan holds memory), at most
-// kScanBatch[cls] of them, and runs them as one batch on its own lane.  Large
-// scans take seconds and each worker holds its lane until its batch ends, so
-// large batches stay small: a request that arrives goes to an idle lane
-// rather than behind a long scan, and a backlog still fills two per lane.
-constexpr int kScanBatch[2] = {16, 2};
+// kScanBatch[cls] of them, and runs them as one batch on its own lane (their
+// scans concurrently, each request handed on as its own scan ends).  Large
+// scans take seconds and a worker holds its lane until its batch ends, so a
+// request that arrives while lanes are idle gets one alone; only a backlog
+// fills batches, up to four per lane.  (Measured with two: the serving
+// configuration's error-diffused upscales need about 34 lane-seconds per
+// second against 27 large lanes, and their queue still grew.)
+constexpr int kScanBatch[2] = {16, 4};
 
 void slow_loop(iwg_server *S, int lane, int cls)
 {
