@@ -966,7 +966,7 @@ bool iwg::plan_needs_scan(const iwg::Plan &P)
 // intermediate, output, flag entries; scan buffers for serial dither).
 size_t iwg::batch_device_bytes(const iwg::Plan &P)
 {
-	const size_t in = P.in_bpr * (size_t)(P.orient >= 4 ? P.img1_w : P.img1_h);
+	const size_t in = plan_in_bpr(P) * (size_t)(P.orient >= 4 ? P.img1_w : P.img1_h);
 	const size_t mid = (size_t)P.mid_n * P.crop_w * P.out_h * sizeof(float);
 	const size_t out = P.out_bpr * (size_t)P.out_h;
 	size_t scan = 0;

@@ -55,7 +55,7 @@ struct Job {
 	// input image (device copy of the caller's bytes)
 	const uint8_t *in;
 	unsigned long long in_bpr;
-	int in_depth, in_float, in_nphys, orient, img1_w, img1_h;
+	int in_depth, in_float, in_nphys, orient, img1_w, img1_h;   // in_float: 1 float samples, 2 linearised doubles
 	int crop_x, crop_y, crop_w, crop_h;
 	int in_alpha;                 // logical alpha channel
 	const double *alpha_tab;      // alpha code -> value, null if the alpha channel is virtual
@@ -223,6 +223,12 @@ __device__ __forceinline__ double in_value(const Job &J, int x, int y, int ch, c
 	if(ch >= J.in_nphys) return 1.0;   // virtual alpha: opaque
 	int px, py;
 	phys_xy(J, x, y, px, py);
+	if(J.in_float == 2) {   // float input linearised on the host: one double per sample
+		const uint8_t *p = J.in + (unsigned long long)py * J.in_bpr + (size_t)(J.in_nphys * px + ch) * 8;
+		double d;
+		memcpy(&d, p, 8);
+		return d;
+	}
 	if(J.in_float) {
 		const uint8_t *p = J.in + (unsigned long long)py * J.in_bpr + (size_t)(J.in_nphys * px + ch) * 4;
 		float f;

@@ -139,7 +139,20 @@ struct Plan {
 
 	// resampling: weight sets per dimension (index 0 = H, 1 = V)
 	std::vector<std::shared_ptr<const Weights>> wsets[2];
+
+	// 32-bit float input in a non-linear colour space: the stored image with
+	// every colour sample converted to linear light on the host (glibc pow,
+	// the reference's formulas; alpha samples as they are), one double per
+	// sample, lin_bpr bytes per stored row.  The device reads these instead
+	// of the caller's floats.
+	std::shared_ptr<const std::vector<double>> lin_in;
+	size_t lin_bpr = 0;
 };
+
+// The input bytes the device passes read and their row stride: the caller's
+// image, or its linearised copy (Plan::lin_in).
+inline const void *plan_input(const iw_context *ctx, const Plan &P);
+inline size_t plan_in_bpr(const Plan &P) { return P.lin_in ? P.lin_bpr : P.in_bpr; }
 
 struct OptState {
 	int width = 0, height = 0, imgtype = 0, bit_depth = 0;
@@ -260,6 +273,11 @@ struct iw_context {
 };
 
 namespace iwg {
+
+inline const void *plan_input(const iw_context *ctx, const Plan &P)
+{
+	return P.lin_in ? (const void *)P.lin_in->data() : (const void *)ctx->img1.pixels;
+}
 
 // plan.cpp
 bool build_plan(iw_context *ctx, Plan &P);

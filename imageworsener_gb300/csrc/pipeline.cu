@@ -2051,7 +2051,7 @@ static int upload_mode(iw_context *ctx, const DeviceState &S, bool resident, boo
 	else if(u && !strcmp(u, "zero")) m = UP_ZERO;
 	else if(u && !strcmp(u, "pull")) m = UP_PULL;
 	if(m == UP_PULL && many && pull_many && S.pageable) return m;   // a batch: one copy kernel for every image
-	if(m == UP_PULL && (!S.pageable || many || ((uintptr_t)ctx->img1.pixels & 15))) m = UP_COPY;
+	if(m == UP_PULL && (!S.pageable || many || ((uintptr_t)ctx->img1.pixels & 15))) m = UP_COPY;   // (a linearised copy is 16-byte aligned too)
 	if(m == UP_ZERO && (!S.pageable || resident)) m = UP_COPY;
 	return m;
 }
@@ -2063,9 +2063,9 @@ static int upload_mode(iw_context *ctx, const DeviceState &S, bool resident, boo
 static bool make_job(iw_context *ctx, const Plan &P, DeviceState &S, Packer &pk, std::vector<Fixup> &fix, Job &J)
 {
 	memset(&J, 0, sizeof(J));
-	J.in_bpr = P.in_bpr;
+	J.in_bpr = plan_in_bpr(P);
 	J.in_depth = P.in_depth;
-	J.in_float = P.in_sampletype == IW_SAMPLETYPE_FLOATINGPOINT;
+	J.in_float = P.lin_in ? 2 : (P.in_sampletype == IW_SAMPLETYPE_FLOATINGPOINT ? 1 : 0);
 	J.in_nphys = P.in_nphys;
 	J.orient = P.orient;
 	J.img1_w = P.img1_w;
@@ -2200,7 +2200,7 @@ bool run_pipeline(iw_context *ctx, Plan &P, int warmup, int iters, int lane)
 	std::vector<Fixup> fix;
 	if(!make_job(ctx, P, S, pk, fix, J)) return false;
 	const int phys_h = P.orient >= 4 ? P.img1_w : P.img1_h;
-	const size_t in_bytes = P.in_bpr * (size_t)phys_h;
+	const size_t in_bytes = plan_in_bpr(P) * (size_t)phys_h;
 	const bool any_scan = J.any_scan != 0;
 
 	// ---- buffers ----
@@ -2230,7 +2230,7 @@ bool run_pipeline(iw_context *ctx, Plan &P, int warmup, int iters, int lane)
 		J.scanbuf = (double *)S.scan.p;
 		J.errbuf = (double *)S.err.p;
 	}
-	J.in = zero_copy ? (const uint8_t *)ctx->img1.pixels : (const uint8_t *)S.in.p;
+	J.in = zero_copy ? (const uint8_t *)plan_input(ctx, P) : (const uint8_t *)S.in.p;
 	J.interm = (float *)S.interm.p;
 	J.out = zero_copy ? (uint8_t *)ctx->img2.pixels : (uint8_t *)S.out.p;
 	ctx->stats.zero_copy = zero_copy;
@@ -2246,16 +2246,16 @@ bool run_pipeline(iw_context *ctx, Plan &P, int warmup, int iters, int lane)
 	cudaEvent_t *const ph = phases.e;
 	cudaEventRecord(ph[0], st);
 	cudaMemcpyAsync(S.params.p, S.staging.data(), S.staging.size(), cudaMemcpyHostToDevice, st);
-	if(upmode == UP_COPY) cudaMemcpyAsync(S.in.p, ctx->img1.pixels, in_bytes, cudaMemcpyHostToDevice, st);
+	if(upmode == UP_COPY) cudaMemcpyAsync(S.in.p, plan_input(ctx, P), in_bytes, cudaMemcpyHostToDevice, st);
 	if(upmode == UP_PULL && in_bytes) {
 		int sms = 152;
 		cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, S.device);
 		const size_t n16 = in_bytes / 16;
 		const unsigned blocks = (unsigned)std::max<size_t>(1, std::min<size_t>((n16 + 1023) / 1024, (size_t)8 * sms));
-		k_pull<<<blocks, 256, 0, st>>>((uint8_t *)S.in.p, (const uint8_t *)ctx->img1.pixels, in_bytes);
+		k_pull<<<blocks, 256, 0, st>>>((uint8_t *)S.in.p, (const uint8_t *)plan_input(ctx, P), in_bytes);
 	}
 	if(upmode == UP_STAGE &&
-		!stage_h2d(S.stager, st, {Xfer{(uint8_t *)S.in.p, (uint8_t *)ctx->img1.pixels, in_bytes}})) {
+		!stage_h2d(S.stager, st, {Xfer{(uint8_t *)S.in.p, (uint8_t *)plan_input(ctx, P), in_bytes}})) {
 		iw_set_error(ctx, "Out of pinned host memory");
 		return false;
 	}
@@ -2598,7 +2598,7 @@ bool run_batch(const std::vector<iw_context *> &ctxs, const std::vector<Plan *> 
 	std::vector<size_t> o_in(n, 0), o_mid(n, 0), o_out(n, 0), in_bytes(n, 0), out_bytes(n, 0);
 	for(int i : sel) {
 		const Plan &P = *plans[i];
-		in_bytes[i] = P.in_bpr * (size_t)(P.orient >= 4 ? P.img1_w : P.img1_h);
+		in_bytes[i] = plan_in_bpr(P) * (size_t)(P.orient >= 4 ? P.img1_w : P.img1_h);
 		out_bytes[i] = P.out_bpr * (size_t)P.out_h;
 		if(!zc) o_in[i] = take(in_bytes[i] ? in_bytes[i] : 16);
 		o_mid[i] = take((size_t)P.mid_n * jobs[i].interm_plane * sizeof(float));
@@ -2625,7 +2625,7 @@ bool run_batch(const std::vector<iw_context *> &ctxs, const std::vector<Plan *> 
 		ctx->img2.bpr = P.out_bpr;
 		ctx->img2.pixels = (iw_byte *)iw_malloc_large(ctx, P.out_bpr, P.out_h);
 		if(!ctx->img2.pixels) { status[i] = -1; continue; }
-		J.in = zc ? (const uint8_t *)ctx->img1.pixels : base + o_in[i];
+		J.in = zc ? (const uint8_t *)plan_input(ctx, P) : base + o_in[i];
 		J.interm = (float *)(base + o_mid[i]);
 		J.out = zc ? (uint8_t *)ctx->img2.pixels : base + o_out[i];
 		ready.push_back(i);
@@ -2673,7 +2673,7 @@ bool run_batch(const std::vector<iw_context *> &ctxs, const std::vector<Plan *> 
 		std::vector<PullItem> pv(m);
 		for(int k = 0; k < m; k++) {
 			const int i = item_img[k];
-			pv[k] = PullItem{base + o_in[i], (const uint8_t *)ctxs[i]->img1.pixels, (unsigned long long)in_bytes[i]};
+			pv[k] = PullItem{base + o_in[i], (const uint8_t *)plan_input(ctxs[i], *plans[i]), (unsigned long long)in_bytes[i]};
 		}
 		o_pull = add(pv.data(), pv.size() * sizeof(PullItem));
 	}
@@ -2707,13 +2707,13 @@ bool run_batch(const std::vector<iw_context *> &ctxs, const std::vector<Plan *> 
 	if(upmode == UP_COPY)
 		for(int k = 0; k < m; k++) {
 			const int i = item_img[k];
-			cudaMemcpyAsync(base + o_in[i], ctxs[i]->img1.pixels, in_bytes[i], cudaMemcpyHostToDevice, st);
+			cudaMemcpyAsync(base + o_in[i], plan_input(ctxs[i], *plans[i]), in_bytes[i], cudaMemcpyHostToDevice, st);
 		}
 	if(upmode == UP_STAGE) {
 		std::vector<Xfer> xs;
 		for(int k = 0; k < m; k++) {
 			const int i = item_img[k];
-			xs.push_back({base + o_in[i], (uint8_t *)ctxs[i]->img1.pixels, in_bytes[i]});
+			xs.push_back({base + o_in[i], (uint8_t *)plan_input(ctxs[i], *plans[i]), in_bytes[i]});
 		}
 		if(!stage_h2d(S.stager, st, xs)) return fail_all("Out of pinned host memory");
 	}
@@ -2859,7 +2859,7 @@ bool run_batch_plain(const std::vector<iw_context *> &ctxs, const std::vector<Pl
 	std::vector<size_t> o_in(n, 0), o_mid(n, 0), o_out(n, 0), o_scan(n, 0), o_err(n, 0), in_bytes(n, 0), out_bytes(n, 0);
 	for(int i : sel) {
 		const Plan &P = *plans[i];
-		in_bytes[i] = P.in_bpr * (size_t)(P.orient >= 4 ? P.img1_w : P.img1_h);
+		in_bytes[i] = plan_in_bpr(P) * (size_t)(P.orient >= 4 ? P.img1_w : P.img1_h);
 		out_bytes[i] = P.out_bpr * (size_t)P.out_h;
 		if(!zc) o_in[i] = take(in_bytes[i] ? in_bytes[i] : 16);
 		o_mid[i] = take((size_t)P.mid_n * jobs[i].interm_plane * sizeof(float));
@@ -2883,7 +2883,7 @@ bool run_batch_plain(const std::vector<iw_context *> &ctxs, const std::vector<Pl
 		ctx->img2.bpr = P.out_bpr;
 		ctx->img2.pixels = (iw_byte *)iw_malloc_large(ctx, P.out_bpr, P.out_h);
 		if(!ctx->img2.pixels) { status[i] = -1; continue; }
-		J.in = zc ? (const uint8_t *)ctx->img1.pixels : base + o_in[i];
+		J.in = zc ? (const uint8_t *)plan_input(ctx, P) : base + o_in[i];
 		J.interm = (float *)(base + o_mid[i]);
 		J.out = zc ? (uint8_t *)ctx->img2.pixels : base + o_out[i];
 		if(J.any_scan) {
@@ -2939,7 +2939,7 @@ bool run_batch_plain(const std::vector<iw_context *> &ctxs, const std::vector<Pl
 	cudaMemcpyAsync(tbase, tab.data(), tab.size(), cudaMemcpyHostToDevice, st);
 	std::vector<Xfer> xin, xout;
 	for(int i : run) {
-		xin.push_back({base + o_in[i], (uint8_t *)ctxs[i]->img1.pixels, in_bytes[i]});
+		xin.push_back({base + o_in[i], (uint8_t *)plan_input(ctxs[i], *plans[i]), in_bytes[i]});
 		xout.push_back({base + o_out[i], (uint8_t *)ctxs[i]->img2.pixels, out_bytes[i]});
 	}
 	if(upmode == UP_COPY)

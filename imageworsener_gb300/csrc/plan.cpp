@@ -9,6 +9,7 @@
 
 #include <cmath>
 #include <cstring>
+#include <thread>
 #include <ctime>
 
 namespace iwg {
@@ -208,6 +209,48 @@ static bool ref_fits_large(iw_context *ctx, size_t n1, size_t n2)
 		return false;
 	}
 	return ref_fits(ctx, n1 * n2);
+}
+
+// The reference converts each float sample of a colour channel to linear
+// light with libm as it reads it (x_to_linear_sample of the raw float,
+// src/imagew-main.c:53-66 and :353-359; alpha samples are not converted).
+// Here the host converts the stored image once, with the same formulas
+// (to_linear) and glibc, on all host threads; the device passes read the
+// resulting doubles (Plan::lin_in).  Samples are read as stored (4 bytes
+// each, rows P.in_bpr apart); the copy keeps the stored layout, one double per
+// sample.
+static void linearise_float_input(iw_context *ctx, Plan &P)
+{
+	const iw_image &im = ctx->img1;
+	const int pw = P.orient >= 4 ? P.img1_h : P.img1_w;   // stored width and rows
+	const int ph = P.orient >= 4 ? P.img1_w : P.img1_h;
+	const int nphys = P.in_nphys;
+	const int alpha = IW_IMGTYPE_HAS_ALPHA(im.imgtype) ? nphys - 1 : -1;
+	const size_t per_row = (size_t)pw * nphys;
+	auto out = std::make_shared<std::vector<double>>(per_row * (size_t)(ph > 0 ? ph : 0));
+	const iw_csdescr cs = ctx->cs_in;
+	const unsigned char *base = (const unsigned char *)im.pixels;
+	auto rows = [&](int r0, int r1) {
+		for(int r = r0; r < r1; r++) {
+			const unsigned char *src = base + (size_t)r * P.in_bpr;
+			double *dst = out->data() + (size_t)r * per_row;
+			for(size_t k = 0; k < per_row; k++) {
+				float f;
+				memcpy(&f, src + 4 * k, 4);
+				const int ch = (int)(k % (size_t)nphys);
+				dst[k] = ch == alpha ? (double)f : to_linear((double)f, cs);
+			}
+		}
+	};
+	const int nt = std::max(1, std::min((int)std::thread::hardware_concurrency(), ph / 16));
+	if(nt <= 1) rows(0, ph);
+	else {
+		std::vector<std::thread> th;
+		for(int t = 0; t < nt; t++) th.emplace_back(rows, (int)((long long)ph * t / nt), (int)((long long)ph * (t + 1) / nt));
+		for(std::thread &x : th) x.join();
+	}
+	P.lin_in = out;
+	P.lin_bpr = per_row * sizeof(double);
 }
 
 bool build_plan(iw_context *ctx, Plan &P)
@@ -442,12 +485,8 @@ bool build_plan(iw_context *ctx, Plan &P)
 	P.blacken = P.out_sampletype == IW_SAMPLETYPE_UINT && !P.reduced_out && IW_IMGTYPE_HAS_ALPHA(P.out_type);
 
 	if(im.sampletype == IW_SAMPLETYPE_FLOATINGPOINT && im.bit_depth == 32 && !ctx->no_gamma &&
-		ctx->cs_in.cstype != IW_CSTYPE_LINEAR) {
-		// Converting arbitrary float samples needs pow() per sample; the GPU
-		// path only takes floating-point input that is already linear.
-		iw_set_error(ctx, "Floating-point input must use a linear input colorspace");
-		return false;
-	}
+		ctx->cs_in.cstype != IW_CSTYPE_LINEAR)
+		linearise_float_input(ctx, P);
 
 	// The reference's buffers and their size limits, checked without
 	// allocating, in its order, before any device work

@@ -14,16 +14,9 @@ pytestmark = pytest.mark.gpu
 
 FORMS = ["fp32", "fp64"]
 
-# Documented limitation: floating-point input (only the MIFF codec produces it)
-# is accepted when it is already linear; converting it needs glibc pow() per
-# sample, which the library does not evaluate on the device.
-FLOAT_LIMIT = "Floating-point input must use a linear input colorspace"
-
-
 def same(job, want_key, got):
-    if got.error == FLOAT_LIMIT and not got.ok:
-        assert job.sampletype == 1, "the float-input limitation fired on integer input"
-        return True
+    # (floating-point input in a non-linear colour space included: the host
+    # linearises it with glibc, as the reference does per sample)
     return want_key == got.key()
 
 
@@ -37,8 +30,6 @@ def test_golden_grid(gpulib, form):
     bad = []
     for job, digest, meta in load_grid():
         res = run_job(gpulib, with_form(job, form))
-        if res.error == FLOAT_LIMIT and job.sampletype == 1:
-            continue
         if res.digest() != digest:
             bad.append((meta["seed"], res.error))
     assert not bad, f"{len(bad)} cases differ from the reference: {bad[:8]}"

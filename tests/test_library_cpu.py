@@ -89,23 +89,19 @@ def test_planning_errors_match_oracle_without_gpu(gpulib, oracle):
         assert (a.ok, a.error) == (b.ok, b.error)
 
 
-FLOAT_NONLINEAR = "Floating-point input must use a linear input colorspace"
-
-
 @pytest.mark.parametrize("block", range(4))
 def test_planning_warnings_match_oracle_on_random_grid(gpulib, oracle, block):
     """The library's planning (output type, depth, colour space, background
     and offset decisions) raises the same warnings as the oracle, in the same
     order, on the random settings grid.  Without a GPU the run stops after
-    planning with a CUDA error; with one it completes.  The one documented
-    refusal is 32-bit float input in a non-linear colour space."""
+    planning with a CUDA error; with one it completes."""
     import iwcases
     bad = []
     for seed in range(block * 600, block * 600 + 600):
         a = run_job(gpulib, iwcases.random_case(seed), keep_warnings=True)
         b = run_job(oracle, iwcases.random_case(seed), keep_warnings=True)
         if b.ok:
-            status_ok = a.ok or "CUDA" in (a.error or "") or a.error == FLOAT_NONLINEAR
+            status_ok = a.ok or "CUDA" in (a.error or "")
         else:
             status_ok = not a.ok and a.error == b.error
         if not status_ok or a.warnings != b.warnings:
