@@ -254,6 +254,9 @@ def e2e_timed(lib: IWLib, job, warmup: int, steps: int, extra_calls=()):
         zc["phase_ms_median"] = {"plan": med[0], "h2d": med[1], "device": med[2], "d2h": med[3], "post_pass": med[4],
                                  "device_part_wall": med[5]}
         zc["h2d_GBps"] = n / 1e6 / med[1] if med[1] > 0 else None
+        k = max(range(len(times)), key=lambda q: times[q])
+        names = ("plan", "h2d", "device", "d2h", "post_pass", "device_part_wall")
+        zc["slowest_step"] = {"ms": 1000.0 * times[k], "phase_ms": dict(zip(names, phases[k]))}
     return times, dig, zc
 
 
@@ -668,7 +671,7 @@ def main():
     peak, peak_src = peaks()
     parts = list(st.ms_part)
     names = ["vertical pass (k_vbulk / k_vstream_px)", "horizontal pass + guarded quantisation (k_hpass_fast)",
-             "re-evaluation of flagged pixels, double-float then FP64 (k_fix_flagged_warp)"]
+             "re-evaluation of flagged pixels, double-float then FP64 (k_fix_tile)"]
     slowest = max(range(3), key=lambda k: parts[k])
     # The roofline is reported for the vertical pass: it moves the compulsory
     # bytes (the input image) and is the HBM-bound kernel of the pipeline.

@@ -35,9 +35,11 @@ struct DQuant {
 	const double *rev;     // maxcc+1
 	const double *nc;      // 255
 	const long long *rec;  // error diffusion: 8 words per bracket (P+1)
-	const float *Uf;       // float copies (fast form)
-	const float *revf;
+	const float *lut;      // or null: kBracketLutCells search start points for U[1..P]
+	                       // (cell c: the count of float-rounded edges <= c / kBracketLutCells)
 };
+
+constexpr int kBracketLutCells = 1024;
 
 struct DMid {
 	int ctype, in_ch, to_gray, out_ch, unassoc, wh, wv;

@@ -13,6 +13,8 @@
 #include <algorithm>
 #include <chrono>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -137,9 +139,10 @@ struct Group {
 	size_t off_idx = 0, off_start = 0;
 };
 
-// Grow-only device buffer for the batch's job array and block tables.  Calls
-// are serialised by the pipeline's lock and the stream is synchronised before
-// the next batch reuses it.
+// Grow-only device buffer for the batch's job array and block tables, one
+// per stream: a batch writes its tables and launches its kernels on its own
+// stream, so the next batch's writes into the same buffer are ordered after
+// them, and batches on other streams (lanes) never share it.
 struct BatchArena {
 	void *p = nullptr;
 	size_t cap = 0;
@@ -158,10 +161,12 @@ struct BatchArena {
 	}
 };
 
-BatchArena &arena()
+BatchArena &arena(cudaStream_t st)
 {
-	static BatchArena *a = new BatchArena();
-	return *a;
+	static std::mutex mu;
+	static auto *m = new std::map<cudaStream_t, BatchArena>();
+	std::lock_guard<std::mutex> lk(mu);
+	return (*m)[st];   // std::map: references stay valid as entries are added
 }
 
 }  // namespace
@@ -238,7 +243,7 @@ int fast_launch_batch(cudaStream_t st, void *const *items, int n, std::string &e
 		}
 	}
 	const auto t_tab = std::chrono::steady_clock::now();
-	BatchArena &A = arena();
+	BatchArena &A = arena(st);
 	if(!A.ensure(host.size(), st)) {
 		err = "Out of GPU memory (batch tables)";
 		return -1;

@@ -6,8 +6,8 @@
 // quantisation tail then decides the output code for the whole interval
 // [v - E, v + E]; if a decision boundary of the reference (a code bracket
 // edge, a nearest-colour midpoint, an ordered-dither threshold) lies inside,
-// the pixel is flagged and recomputed exactly in FP64 by k_fix_flagged
-// (pipeline.cu).  Output bytes therefore equal the plain form's.
+// the pixel is flagged and re-evaluated by the fix-up kernels (pipeline.cu:
+// certified double-float, then FP64).  Output bytes therefore equal the plain form's.
 //
 // Error bound (u = 2^-24, per pass with n taps and weights w):
 //   decode   |a' - a| <= e_dec + r_dec * a          (e_dec measured over every code)
@@ -105,8 +105,10 @@ struct Cache {
 	std::mutex tab_mu;    // the device table cache 'dev' (and the decode-error record)
 	struct Entry { std::shared_ptr<const void> keep; std::shared_ptr<const void> derived; void *dev; };
 	std::map<std::pair<const void *, int>, Entry> dev;
-	void *scratch = nullptr;
-	size_t scratch_cap = 0;
+	// each stream's per-image device block (grown stream-ordered on its own
+	// stream, so a block is never reallocated under another stream's work)
+	struct Scratch { void *p = nullptr; size_t cap = 0; };
+	std::map<cudaStream_t, Scratch> scratch;
 };
 
 Cache &cache()
@@ -320,7 +322,7 @@ bool fast_eligible(const Plan &P, const Job &J, FastInfo &fi)
 void fast_launch_impl(cudaStream_t st, void *state, void (*mark)(void *), void *markarg)
 {
 	FastState &S = *static_cast<FastState *>(state);
-	cudaMemsetAsync(S.F.flag_count, 0, 3 * sizeof(int), st);
+	cudaMemsetAsync(S.F.flag_count, 0, 4 * sizeof(int), st);
 	void *fargs[] = {&S.F};
 	void *targs[] = {&S.T};
 	void *uargs[] = {&S.F, &S.fuse_tiles};
@@ -807,6 +809,9 @@ static FastState *fast_build(const Plan &P, const Job &J, bool batch, int tc_mod
 	F.hgx = (int)FS->hgrid.x;
 	FS->F = F;
 	FS->J = J;
+	// start points of the re-evaluation's bracket searches: the tail's tables
+	static_assert(kLutCells == dev::kBracketLutCells, "one cell count for both searches");
+	for(int oc = 0; oc < P.out_n; oc++) FS->J.outc[oc].q.lut = tails[oc].use_nc ? nullptr : tails[oc].lut;
 	FS->blob = std::move(blob);
 	FS->o_hoff = o_hoff; FS->o_hsrc = o_hsrc; FS->o_hw = o_hw;
 	FS->o_voff = o_voff; FS->o_vsrc = o_vsrc; FS->o_vw = o_vw;
@@ -926,7 +931,7 @@ static bool launch_vertical(cudaStream_t st, FastState &FS)
 	// The fused pass also lists flagged pixels: its counters start at zero
 	// for every trial launch (the scratch holding them is reused between
 	// jobs, and trials must not pile entries past the list's capacity).
-	if(FS.fuse) cudaMemsetAsync(FS.F.flag_count, 0, 3 * sizeof(int), st);
+	if(FS.fuse) cudaMemsetAsync(FS.F.flag_count, 0, 4 * sizeof(int), st);
 	return cudaLaunchKernel(FS.vkernel, FS.vgrid, dim3(FS.vthreads), FS.tc ? targs : (FS.fuse ? uargs : fargs), FS.vsmem,
 		st) == cudaSuccess;
 }
@@ -985,19 +990,20 @@ bool fast_prepare(cudaStream_t st, const Plan &P, Job &J, FastInfo &fi, std::str
 	if(!FS) return false;
 	const size_t flag_off = (FS->blob.size() + 255) & ~(size_t)255;
 	const size_t need = flag_off + 256 + FS->flag_entries * 16;
-	if(need > C.scratch_cap) {
-		if(C.scratch) cudaFreeAsync(C.scratch, st);
-		C.scratch = nullptr;
-		C.scratch_cap = 0;
-		if(cudaMallocAsync(&C.scratch, need + need / 8, st) != cudaSuccess) {
+	Cache::Scratch &SC = C.scratch[st];
+	if(need > SC.cap) {
+		if(SC.p) cudaFreeAsync(SC.p, st);
+		SC.p = nullptr;
+		SC.cap = 0;
+		if(cudaMallocAsync(&SC.p, need + need / 8, st) != cudaSuccess) {
 			cudaGetLastError();
 			delete FS;
 			err = "Out of GPU memory (fast form)";
 			return false;
 		}
-		C.scratch_cap = need + need / 8;
+		SC.cap = need + need / 8;
 	}
-	uint8_t *base = (uint8_t *)C.scratch;
+	uint8_t *base = (uint8_t *)SC.p;
 	cudaMemcpyAsync(base, FS->blob.data(), FS->blob.size(), cudaMemcpyHostToDevice, st);
 	fast_place(FS, base, (int *)(base + flag_off), (int *)(base + flag_off + 256), 0, FS->flag_entries);
 	FS->F.dbg = fi.dbg;
@@ -1043,6 +1049,7 @@ void fast_item_job_df(const void *item, Job &J)
 	J.df_atab = K.df_atab;
 	J.df_wv = K.df_wv;
 	J.df_wh = K.df_wh;
+	for(int oc = 0; oc < dev::kMaxCh; oc++) J.outc[oc].q.lut = K.outc[oc].q.lut;
 }
 
 void fast_item_free(void *item) { delete static_cast<FastState *>(item); }

@@ -91,6 +91,56 @@ __device__ __forceinline__ double interm_exact(const Job &J, int m, int x, int j
 	return (double)__double2float_rn(s);
 }
 
+// interm_exact<true> with its loads issued ahead: eight taps' samples (and
+// alphas), then their decode-table values, in flight together; the FP64
+// operations are interm_exact's, in its order, so the value is the same.
+// For the re-evaluation of the fast form, whose plans have no grayscale
+// conversion, early background, float input or orientation change (others
+// take interm_exact itself).
+__device__ double interm_exact_ahead(const Job &J, int m, int x, int j)
+{
+	const DMid &mc = J.mid[m];
+	const DWeights &W = J.wv[mc.wv];
+	if(mc.to_gray || J.bk_early || J.in_float || J.orient != 0 || W.kind == 1) return interm_exact<true>(J, m, x, j);
+	const int tb = W.off[j], te = W.off[j + 1];
+	const int px = J.crop_x + x;
+	const bool has_ch = mc.in_ch < J.in_nphys, has_a = J.in_alpha < J.in_nphys;
+	double s = 0.0;
+	for(int t0 = tb; t0 < te; t0 += 8) {
+		int src[8];
+#pragma unroll
+		for(int u = 0; u < 8; u++) src[u] = t0 + u < te ? W.src[t0 + u] : -1;
+		unsigned int cv[8], ca[8];
+#pragma unroll
+		for(int u = 0; u < 8; u++) {
+			cv[u] = ca[u] = 0u;
+			if(src[u] < 0) continue;
+			const int py = J.crop_y + src[u];
+			if(has_ch) cv[u] = raw_code(J, px, py, mc.in_ch);
+			if(mc.unassoc && has_a) ca[u] = raw_code(J, px, py, J.in_alpha);
+		}
+		double v[8], a[8], w[8];
+#pragma unroll
+		for(int u = 0; u < 8; u++) {
+			v[u] = has_ch ? mc.tab[0][cv[u]] : 1.0;               // in_value (virtual channel: 1)
+			a[u] = (mc.unassoc && has_a) ? J.alpha_tab[ca[u]] : 1.0;
+			w[u] = t0 + u < te ? W.w[t0 + u] : 0.0;
+		}
+#pragma unroll
+		for(int u = 0; u < 8; u++) {
+			if(t0 + u >= te) break;
+			double d = W.edge_value;
+			if(src[u] >= 0) {
+				d = v[u];
+				if(mc.unassoc) d = dmul(d, a[u]);   // decode_exact
+			}
+			s = dadd(s, dmul(d, w[u]));
+		}
+	}
+	if(J.intclamp) s = s < 0.0 ? 0.0 : (s > 1.0 ? 1.0 : s);
+	return (double)__double2float_rn(s);
+}
+
 // Horizontal pass of one channel for output pixel (i, j).  interm(m, k, x)
 // returns the exact intermediate value of channel m at column x, the k-th tap.
 template<class Interm>
@@ -289,10 +339,20 @@ __device__ __forceinline__ double clamp01_bits(double v)
 	return v;
 }
 
-// Bracket index k (U[k] <= v < U[k+1]) of v >= +0, by binary search.
+// Bracket index k (U[k] <= v < U[k+1]) of v in [+0, 1]: the count of
+// U[1..P] <= v, from a start point in q.lut (stepped to the exact count in
+// double; any start gives the same count), else by binary search.
 __device__ __forceinline__ int bracket_index(const DQuant &q, long long vb)
 {
 	const long long *U = reinterpret_cast<const long long *>(q.U) + 1;
+	if(q.lut) {
+		const float vf = __double2float_rd(__longlong_as_double(vb));
+		const int cell = min(max((int)__fmul_rn(vf, (float)kBracketLutCells), 0), kBracketLutCells - 1);
+		int k = (int)__ldg(q.lut + cell);
+		while(k < q.P && __ldg(U + k) <= vb) k++;
+		while(k > 0 && __ldg(U + k - 1) > vb) k--;
+		return k;
+	}
 	int lo = 0, hi = q.P;
 	while(lo < hi) {
 		const int mid = (lo + hi) >> 1;
@@ -845,30 +905,30 @@ __device__ __forceinline__ dfl df_div_le1(dfl x, dfl y)
 	return df_fast_two_sum(q1, __fdiv_rn(r.hi, y.hi));
 }
 
-// quantize_exact's code for one end of an interval, with FP64 only for the
-// two distances: the clamp, bracket and exactness tests compare bit patterns
-// (order-preserving for non-negative doubles), and the ordered-dither
-// fraction d_lo / (d_lo + d_hi) is taken in double-float: within 7e-14 of
-// the exact ratio, and the reference's double fraction is within 2.3e-16 of
-// it, so a decision 1e-12 or more away from the threshold is the
-// reference's; nearer, 'ok' is cleared and the caller falls back to the
-// exact path.
-__device__ __forceinline__ int quantize_end(const DQuant &q, double v, int x, int y, bool &ok)
+// quantize_exact's code for one end of an interval (quantize_end), with FP64
+// only for the two distances: the clamp, bracket and exactness tests compare
+// bit patterns (order-preserving for non-negative doubles), and the
+// ordered-dither fraction d_lo / (d_lo + d_hi) is taken in double-float:
+// within 7e-14 of the exact ratio, and the reference's double fraction is
+// within 2.3e-16 of it, so a decision 1e-12 or more away from the threshold
+// is the reference's; nearer, 'ok' is cleared and the caller falls back to
+// the exact path.
+//
+// The bits quantize_end decides on: v clamped to [+0, 1]; false for NaN
+// (both candidate codes of a NaN convert to 0).
+__device__ __forceinline__ bool quant_bits(double v, long long &vb)
 {
-	long long vb = __double_as_longlong(v);
-	if((vb & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL) return 0;   // NaN: both candidate codes convert to 0
+	vb = __double_as_longlong(v);
+	if((vb & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL) return false;
 	if(vb < 0) vb = 0;                                                  // v < 0 (or -0): +0
 	else if(vb > 0x3ff0000000000000LL) vb = 0x3ff0000000000000LL;       // v > 1: 1
-	if(q.use_nc) {
-		const long long *nc = reinterpret_cast<const long long *>(q.nc);
-		int lo = 0, hi = 255;
-		while(lo < hi) {
-			const int mid = (lo + hi) >> 1;
-			if(__ldg(nc + mid) <= vb) lo = mid + 1; else hi = mid;
-		}
-		return lo;
-	}
-	const int k = bracket_index(q, vb);
+	return true;
+}
+
+// quantize_end's decision for clamped bits vb in bracket k (no nearest-colour
+// table).
+__device__ __forceinline__ int quantize_in(const DQuant &q, long long vb, int k, int x, int y, bool &ok)
+{
 	const int clo = q.code[k], chi = q.code[k + 1];
 	if(k == q.P || vb < __ldg(reinterpret_cast<const long long *>(q.X) + k)) return clo;   // exact
 	const double vc = __longlong_as_double(vb);
@@ -885,109 +945,154 @@ __device__ __forceinline__ int quantize_end(const DQuant &q, double v, int x, in
 	return dle_bits(d_hi, d_lo) ? chi : clo;
 }
 
+// Bracket k of clamped bits vb with its decision record r (q.rec, 8 words
+// per bracket): from q.lut's start point (else a binary search), stepped
+// until r.lo <= vb < r.hi -- the bracket bracket_index finds.
+__device__ __forceinline__ int bracket_rec(const DQuant &q, long long vb, EdRec &r)
+{
+	int k;
+	if(q.lut) {
+		const float vf = __double2float_rd(__longlong_as_double(vb));
+		const int cell = min(max((int)__fmul_rn(vf, (float)kBracketLutCells), 0), kBracketLutCells - 1);
+		k = min((int)__ldg(q.lut + cell), q.P);
+	}
+	else k = bracket_index(q, vb);
+	r = ed_rec(q.rec, k);
+	while(k < q.P && r.hi <= vb) r = ed_rec(q.rec, ++k);
+	while(k > 0 && r.lo > vb) r = ed_rec(q.rec, --k);
+	return k;
+}
+
+// quantize_in from bracket k's record.
+__device__ __forceinline__ int quantize_in_rec(const DQuant &q, long long vb, int k, const EdRec &r, int x, int y, bool &ok)
+{
+	if(k == q.P || vb < r.x) return r.code_lo;   // exact
+	const double vc = __longlong_as_double(vb);
+	const double d_lo = dsub(vc, r.rev_lo), d_hi = dsub(r.rev_hi, vc);
+	if(q.dfam == IW_DITHERFAMILY_ORDERED) {
+		const dfl l = df_from_double(d_lo), h = df_from_double(d_hi);
+		const dfl f = df_div_le1(l, df_add(l, h));
+		const float thr = dither_threshold(dither_rank(q.dsub, x, y));
+		const float diff = __fadd_rn(__fsub_rn(f.hi, thr), f.lo);
+		if(fabsf(diff) <= 1e-12f) ok = false;
+		return diff >= 0.0f ? r.code_hi : r.code_lo;
+	}
+	return dle_bits(d_hi, d_lo) ? r.code_hi : r.code_lo;
+}
+
+__device__ __forceinline__ int quantize_end(const DQuant &q, double v, int x, int y, bool &ok)
+{
+	long long vb;
+	if(!quant_bits(v, vb)) return 0;
+	if(q.use_nc) {
+		const long long *nc = reinterpret_cast<const long long *>(q.nc);
+		int lo = 0, hi = 255;
+		while(lo < hi) {
+			const int mid = (lo + hi) >> 1;
+			if(__ldg(nc + mid) <= vb) lo = mid + 1; else hi = mid;
+		}
+		return lo;
+	}
+	return quantize_in(q, vb, bracket_index(q, vb), x, y, ok);
+}
+
 // Output code of every v in [vlo, vhi] as quantize_exact computes it;
 // 'ok' false if it is not the same code over the interval (the decision is
 // monotone in v within a bracket, and each end is checked above).
 __device__ __forceinline__ int quantize_interval(const DQuant &q, double vlo, double vhi, int x, int y, bool &ok)
 {
-	const int clo = quantize_end(q, vlo, x, y, ok), chi = quantize_end(q, vhi, x, y, ok);
+	long long blo, bhi;
+	if(q.use_nc || !quant_bits(vlo, blo) || !quant_bits(vhi, bhi)) {
+		const int clo = quantize_end(q, vlo, x, y, ok), chi = quantize_end(q, vhi, x, y, ok);
+		if(clo != chi) ok = false;
+		return clo;
+	}
+	// vlo <= vhi, so their brackets are in order: one search, and vhi's
+	// bracket is vlo's unless vhi reaches that bracket's upper edge U[k+1]
+	if(q.rec) {
+		EdRec r, rh;
+		const int k = bracket_rec(q, blo, r);
+		int khi = k;
+		rh = r;
+		if(k < q.P && r.hi <= bhi) khi = bracket_rec(q, bhi, rh);
+		const int clo = quantize_in_rec(q, blo, k, r, x, y, ok), chi = quantize_in_rec(q, bhi, khi, rh, x, y, ok);
+		if(clo != chi) ok = false;
+		return clo;
+	}
+	const int k = bracket_index(q, blo);
+	const int khi = (k < q.P && __ldg(reinterpret_cast<const long long *>(q.U) + 1 + k) <= bhi) ? bracket_index(q, bhi) : k;
+	const int clo = quantize_in(q, blo, k, x, y, ok), chi = quantize_in(q, bhi, khi, x, y, ok);
 	if(clo != chi) ok = false;
 	return clo;
 }
 
-// Starts loading the input window of flagged pixel (i, j) -- the rows of its
-// vertical taps, the byte range of its horizontal taps -- into L1 (whole
-// warp, one prefetch per 32 bytes).  The re-evaluation then reads it with
-// chains of dependent loads (tap -> sample -> decode table) that would
-// otherwise each wait for DRAM.  A hint only: identity orientation, byte
-// samples.
-__device__ __forceinline__ void prefetch_window(const Job &J, int i, int j, int lane)
+// Horizontal taps of output column i (the fast form's one horizontal
+// weight set): source columns, double-float weights (null: one tap of
+// weight 1) and their count.
+__device__ __forceinline__ void h_taps(const Job &J, int i, const int *&src, const float2 *&w, int &n)
 {
-	if(J.orient != 0 || J.in_depth < 8) return;
-	const DWeights &WH = J.wh[J.mid[0].wh], &WV = J.wv[J.mid[0].wv];
-	int xlo = 0x7fffffff, xhi = -1;
-	const int t0 = WH.kind == 1 ? i : WH.off[i], nt = WH.kind == 1 ? 1 : WH.off[i + 1] - t0;
-	for(int t = lane; t < nt; t += 32) {
-		const int s = WH.src[t0 + t];
-		if(s >= 0) { xlo = min(xlo, s); xhi = max(xhi, s); }
+	const DWeights &W = J.wh[J.mid[0].wh];
+	if(W.kind == 1) {
+		src = W.src + i;
+		w = nullptr;
+		n = 1;
 	}
-	xlo = __reduce_min_sync(0xffffffffu, xlo);
-	xhi = __reduce_max_sync(0xffffffffu, xhi);
-	if(xhi < 0) return;
-	const unsigned long long bpp = (unsigned long long)J.in_nphys * (J.in_depth / 8);
-	const unsigned long long b0 = (unsigned long long)(J.crop_x + xlo) * bpp, b1 = (unsigned long long)(J.crop_x + xhi + 1) * bpp;
-	const int tb = WV.kind == 1 ? j : WV.off[j], nv = WV.kind == 1 ? 1 : WV.off[j + 1] - tb;
-	for(int t = lane; t < nv; t += 32) {
-		const int s = WV.src[tb + t];
-		if(s < 0) continue;
-		const uint8_t *row = J.in + (unsigned long long)(J.crop_y + s) * J.in_bpr;
-		for(unsigned long long b = b0; b < b1; b += 32) asm volatile("prefetch.global.L1 [%0];" :: "l"(row + b));
-		asm volatile("prefetch.global.L1 [%0];" :: "l"(row + b1 - 1));
+	else {
+		src = W.src + W.off[i];
+		w = J.df_wh + W.off[i];
+		n = W.off[i + 1] - W.off[i];
 	}
 }
 
-__device__ __forceinline__ bool fix_df_finish(const Job &J, int i, int j, unsigned int mask, const float *my, int maxt, int lane);
-
-// Re-evaluates flagged pixel (i, j) in double-float (whole warp); returns
-// true (warp-uniform) with the codes stored if every decision was certain.
-__device__ bool fix_pixel_df(const Job &J, int i, int j, unsigned int mask, float *my, int maxt, int lane)
+// Second half of the double-float re-evaluation of pixel (i, j), by a group
+// of GW lanes (GW = 4: several pixels per warp, GW = 32: one): lane m of
+// the group sums channel m's horizontal taps (hsrc, hw, nh as h_taps gives
+// them) from the certified intermediate values in 'my' (maxt per channel),
+// unassociates and quantises; true (group-uniform) with the codes stored if
+// every decision was certain.  Every lane of the warp calls it; a lane whose
+// group has no pixel passes live = false and never touches J.
+template<int GW>
+__device__ __forceinline__ bool fix_df_finish_g(const Job &J, int i, int j, unsigned int mask, const float *my, int maxt,
+	int lane, bool live, const int *hsrc, const float2 *hw, int nh)
 {
-	prefetch_window(J, i, j, lane);
-	bool bad = false;
-	{
-		// one lane per horizontal tap, all masked channels at once
-		const DWeights &W = J.wh[J.mid[0].wh];
-		const int t0 = W.kind == 1 ? i : W.off[i];
-		const int nt = W.kind == 1 ? 1 : W.off[i + 1] - t0;
-		for(int t = lane; t < nt; t += 32) {
-			const int src = W.src[t0 + t];
-			if(src >= 0 && !interm_df_all(J, mask, src, j, my + t, maxt)) bad = true;
-		}
-	}
-	if(__any_sync(0xffffffffu, bad)) return false;
-	__syncwarp();
-	return fix_df_finish(J, i, j, mask, my, maxt, lane);
-}
-
-// Second half of the double-float re-evaluation of pixel (i, j), one warp:
-// lane m sums channel m's horizontal taps from the certified intermediate
-// values in 'my' (maxt per channel), unassociates and quantises; true
-// (warp-uniform) with the codes stored if every decision was certain.
-__device__ __forceinline__ bool fix_df_finish(const Job &J, int i, int j, unsigned int mask, const float *my, int maxt, int lane)
-{
-	const bool mine = lane < J.mid_n && ((mask >> lane) & 1u);
+	static_assert(GW == 4 || GW == 32, "lane groups of 4 or 32");
+	const int ch = lane & (GW - 1);
+	const unsigned int gmask = GW == 32 ? 0xffffffffu : (((1u << GW) - 1u) << (lane & ~(GW - 1)));
+	const bool mine = live && ch < J.mid_n && ((mask >> ch) & 1u);
 	dfl s = {0.0f, 0.0f};
 	float A = 0.0f;
-	int nh = 1;
-	if(mine) {
-		const DWeights &W = J.wh[J.mid[lane].wh];
-		if(W.kind == 1) {
-			if(W.src[i] >= 0) s.hi = my[lane * maxt];
-			A = fabsf(s.hi);
-		}
-		else {
-			const int t0 = W.off[i];
-			nh = W.off[i + 1] - t0;
-			for(int t = 0; t < nh; t++) {
-				if(W.src[t0 + t] < 0) continue;
-				const float I = my[lane * maxt + t];
-				const dfl w = df_of(J.df_wh[t0 + t]);
-				s = df_add_sloppy(s, df_mul_f(I, w));   // per term below 3u^2 (table) + 2u^2 + 2.01u^2 of A
-				A = __fmaf_rn(fabsf(I), fabsf(w.hi), A);
+	if(!mine) nh = 1;
+	else {
+		for(int tb = 0; tb < nh; tb += 8) {   // eight taps' loads in flight together
+			int src[8];
+			float I[8];
+			float2 w[8];
+#pragma unroll
+			for(int u = 0; u < 8; u++) {
+				const int t = tb + u;
+				src[u] = t < nh ? hsrc[t] : -1;
+				I[u] = t < nh ? my[ch * maxt + t] : 0.0f;
+				w[u] = t >= nh ? make_float2(0.0f, 0.0f) : (hw ? hw[t] : make_float2(1.0f, 0.0f));
+			}
+#pragma unroll
+			for(int u = 0; u < 8; u++) {
+				if(src[u] < 0) continue;   // edge taps add nothing
+				s = df_add_sloppy(s, df_mul_f(I[u], df_of(w[u])));   // per term below 3u^2 (table) + 2u^2 + 2.01u^2 of A
+				A = __fmaf_rn(fabsf(I[u]), fabsf(w[u].x), A);
 			}
 		}
 	}
 	const float ds = __fmaf_rn(A * 1.01f, (float)(20 * nh) * 3.5527137e-15f + (float)(2 * nh + 2) * 1.1102231e-16f, 1e-30f);
 	// the float alpha the reference divides by
-	const int al = J.mid_alpha >= 0 ? J.mid_alpha : 0;
+	const int al = (live && J.mid_alpha >= 0) ? J.mid_alpha : 0;
 	bool a_ok = true;
-	if(mine && lane == al && J.mid_alpha >= 0) a_ok = A == 0.0f || rounds_to_hi(s, ds);   // A == 0: exact zero
-	const float a32 = __shfl_sync(0xffffffffu, s.hi, al);
-	if(!__shfl_sync(0xffffffffu, a_ok ? 1 : 0, al)) return false;
+	if(mine && ch == al && J.mid_alpha >= 0) a_ok = A == 0.0f || rounds_to_hi(s, ds);   // A == 0: exact zero
+	const float a32 = __shfl_sync(0xffffffffu, s.hi, al, GW);
+	bool ok = __shfl_sync(0xffffffffu, a_ok ? 1 : 0, al, GW) != 0;
 	int code = -1, oc = -1;
-	bool is_alpha = false, ok = true;
-	if(mine) {
-		const DMid &mc = J.mid[lane];
+	bool is_alpha = false;
+	if(mine && ok) {
+		const DMid &mc = J.mid[ch];
 		is_alpha = mc.ctype == IW_CHANNELTYPE_ALPHA;
 		oc = mc.out_ch;
 		dfl v = s;
@@ -1002,8 +1107,9 @@ __device__ __forceinline__ bool fix_df_finish(const Job &J, int i, int j, unsign
 			code = quantize_interval(J.outc[oc].q, dsub(vd, d), dadd(vd, d), i, j, ok);
 		}
 	}
-	if(__any_sync(0xffffffffu, !ok)) return false;
-	const int ac = __shfl_sync(0xffffffffu, code, al);
+	const bool gbad = (__ballot_sync(0xffffffffu, !ok) & gmask) != 0u;
+	const int ac = __shfl_sync(0xffffffffu, code, al, GW);
+	if(gbad || !live) return false;
 	const int alpha_code = (J.mid_alpha >= 0 && J.mid[al].out_ch >= 0) ? ac : -1;
 	if(code >= 0) {
 		if(!is_alpha) {
@@ -1015,121 +1121,14 @@ __device__ __forceinline__ bool fix_df_finish(const Job &J, int i, int j, unsign
 	return true;
 }
 
-// The FP64 path of flagged pixel (i, j) by one warp: the lanes recompute the
-// intermediate values the pixel's horizontal taps read (one vertical FP64 sum
-// per (channel, tap), for the channels in 'mask'), then lane m finishes
-// intermediate channel m -- its horizontal sum, unassociation and
-// quantisation -- with the alpha value and alpha code passed between lanes.
-// The result equals pixel_exact()'s.  Scratch 'my': maxt floats per channel.
-__device__ void fix_pixel_fp64_warp(const Job &J, int i, int j, unsigned int mask, float *my, int maxt, int lane)
+__device__ __forceinline__ bool fix_df_finish(const Job &J, int i, int j, unsigned int mask, const float *my, int maxt, int lane)
 {
-	const int ntask = __popc(mask) * maxt;
-	for(int k = lane; k < ntask; k += 32) {
-		const int r = k / maxt, t = k - r * maxt;
-		const int m = nth_bit(mask, r);
-		const DWeights &W = J.wh[J.mid[m].wh];
-		const int t0 = W.kind == 1 ? i : W.off[i];
-		const int nt = W.kind == 1 ? 1 : W.off[i + 1] - t0;
-		if(t < nt) {
-			const int src = W.src[t0 + t];
-			if(src >= 0) my[m * maxt + t] = (float)interm_exact<true>(J, m, src, j);
-		}
-	}
-	__syncwarp();
-	const bool mine = lane < J.mid_n && ((mask >> lane) & 1u);
-	double s = 0.0;
-	if(mine) s = hsum_exact(J, lane, i, j, [&](int m, int k, int) { return (double)my[m * maxt + k]; });
-	const int al = J.mid_alpha >= 0 ? J.mid_alpha : 0;
-	const double a = (double)__double2float_rn(__shfl_sync(0xffffffffu, s, al));
-	int code = -1, oc = -1;
-	bool is_alpha = false;
-	if(mine) {
-		const DMid &mc = J.mid[lane];
-		is_alpha = mc.ctype == IW_CHANNELTYPE_ALPHA;
-		oc = mc.out_ch;
-		if(oc >= 0) {
-			const DOut &o = J.outc[oc];
-			const double v = unassoc_and_bkgd(J, mc, o, s, a, checker_alt(J, i, j), is_alpha);
-			if(J.out_float) {
-				float fv = __double2float_rn(v);
-				if(J.negate && !is_alpha) fv = __fsub_rn(1.0f, fv);
-				store_float(J, oc, i, j, fv);
-			}
-			else if(o.scan) J.scanbuf[((unsigned long long)oc * J.out_h + j) * J.out_w + i] = v;
-			else code = quantize_exact(o.q, v, i, j);
-		}
-	}
-	const int ac = __shfl_sync(0xffffffffu, code, al);
-	const int alpha_code = (J.mid_alpha >= 0 && J.mid[al].out_ch >= 0) ? ac : -1;
-	if(code >= 0) {
-		if(!is_alpha) {
-			if(J.negate) code = J.outc[oc].maxcc - code;
-			if(J.blacken && alpha_code == 0) code = 0;
-		}
-		store_code(J, oc, i, j, (unsigned int)code);
-	}
-	__syncwarp();
+	const int *hsrc;
+	const float2 *hw;
+	int nh;
+	h_taps(J, i, hsrc, hw, nh);
+	return fix_df_finish_g<32>(J, i, j, mask, my, maxt, lane, true, hsrc, hw, nh);
 }
-
-// Exact re-evaluation of the pixels the fast form flagged, one warp per
-// pixel.  FP64 throughput is what limits this kernel, so the work is spread
-// over as many lanes as a pixel offers: first the lanes recompute the
-// intermediate values the pixel's horizontal taps read (one vertical FP64 sum
-// per (channel, tap), for the channels in the pixel's mask), then lane m
-// finishes intermediate channel m -- its horizontal sum, unassociation and
-// quantisation -- with the alpha value and alpha code passed between lanes.
-// The result equals pixel_exact()'s.  Scratch: 'maxt' floats per channel per warp.
-// Pixels the double-float tier cannot certify go to the FP64 path.  They are
-// listed at the tail of the flag list (entry cap-1-L for the L-th), where a
-// block per pixel spreads the work (k_fix_leftover); while that region does
-// not reach the flagged entries (cap - L > n), else the warp does it here.
-template<bool BATCH>
-__global__ void __launch_bounds__(128, 8) k_fix_flagged_warp(Job J1, const Job *jobs, int *count, int *list, int maxt, int cap,
-	int listcap)
-{
-	extern __shared__ float fix_cache[];
-	const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, wpb = blockDim.x >> 5;
-	float *my = fix_cache + (size_t)wib * dev::kMaxCh * maxt;
-	const int n = min(*count, listcap);
-	for(int f = blockIdx.x * wpb + wib; f < n; f += gridDim.x * wpb) {
-		const int4 e = reinterpret_cast<const int4 *>(list)[f];
-		const Job &J = BATCH ? jobs[e.z] : J1;
-		const int p = e.x;
-		const unsigned int mask = (unsigned int)e.y & ((1u << J.mid_n) - 1u);
-		const int i = p % J.out_w, j = p / J.out_w;
-		if(J.df_wv && fix_pixel_df(J, i, j, mask, my, maxt, lane)) {
-			__syncwarp();
-			continue;
-		}
-		int slot = 0;
-		if(lane == 0) slot = cap - 1 - atomicAdd(count + 1, 1);   // pixels that needed the FP64 path
-		slot = __shfl_sync(0xffffffffu, slot, 0);
-		if(slot >= n) {   // room at the tail: a block per pixel takes it
-			if(lane == 0) reinterpret_cast<int4 *>(list)[slot] = e;
-			__syncwarp();
-			continue;
-		}
-		__syncwarp();
-		fix_pixel_fp64_warp(J, i, j, mask, my, maxt, lane);
-	}
-}
-
-// Double-float tier with every lane busy (windows of up to kFix2MaxTaps
-// taps per dimension).  A flagged pixel reads nv x nh input pixels (its
-// vertical taps' rows by its horizontal taps' columns).  Step 1: the lanes
-// take those pixels in turn, one pixel per lane at a time, all loads of a
-// round in flight together; each decodes its pixel once and leaves the
-// double-float term v * (a * w_v) of every masked channel in shared memory
-// (the premultiplied value times the vertical weight; the order of the
-// products does not matter to the bound below, which holds for the exact
-// real product).  Step 2: the lanes take the (channel, horizontal tap)
-// pairs in turn and sum their nv terms, certifying each float32
-// intermediate as interm_df_all does.  Step 3 is fix_df_finish.
-// Bound (u = 2^-24, A = sum of |term|): table values u^2 each (v, a, w),
-// two double-float products 5u^2 each, n additions 2.01u^2 of the running
-// magnitude (df_add_sloppy): (13 + 2.01n) u^2 A <= 24 n u^2 A, as
-// interm_df_all.
-constexpr int kFix2MaxTaps = 32;
 
 // The codes of every channel of stored pixel (px, py): one aligned 8- or
 // 4-byte load for 16-bit RGBA and 8-bit RGBA rows (where 'wide' says the
@@ -1162,150 +1161,9 @@ __device__ __forceinline__ unsigned int pick4(const unsigned int (&c)[dev::kMaxC
 	return k == 0 ? c[0] : (k == 1 ? c[1] : (k == 2 ? c[2] : c[3]));
 }
 
-__device__ bool fix_pixel_df2(const Job &J, int i, int j, unsigned int mask, float2 *P, int pstride, float *my, int maxt,
-	int lane)
-{
-	const DWeights &WH = J.wh[J.mid[0].wh], &WV = J.wv[J.mid[0].wv];
-	const int ht0 = WH.kind == 1 ? i : WH.off[i], nh = WH.kind == 1 ? 1 : WH.off[i + 1] - ht0;
-	const int vt0 = WV.kind == 1 ? j : WV.off[j], nv = WV.kind == 1 ? 1 : WV.off[j + 1] - vt0;
-	bool need_alpha = false;
-#pragma unroll
-	for(int m = 0; m < dev::kMaxCh; m++)
-		if(m < J.mid_n && ((mask >> m) & 1u) && J.mid[m].unassoc) need_alpha = true;
-	need_alpha = need_alpha && J.in_alpha < J.in_nphys && J.df_atab != nullptr;
-	// whole-pixel loads: 4 channels of 16 or 8 bits, rows and base aligned
-	const bool wide = J.in_nphys == 4 && (J.in_depth == 16 || J.in_depth == 8) &&
-		(((uintptr_t)J.in | (uintptr_t)J.in_bpr) & (J.in_depth == 16 ? 7u : 3u)) == 0;
-	const int ntask = nv * nh;   // 0 if either window is empty
-	// lane's task k = r * nh + t, found without an integer division
-	const float inv_nh = nh > 0 ? 1.0f / (float)nh : 0.0f;
-	// step 1: four pixels per lane in flight
-	for(int k0 = 0; k0 < ntask; k0 += 128) {
-		int px[4], py[4], rr[4];
-		bool live[4];
-		unsigned int cc[4][dev::kMaxCh];
-#pragma unroll
-		for(int u = 0; u < 4; u++) {
-			const int k = k0 + 32 * u + lane;
-			live[u] = false;
-			px[u] = py[u] = 0;
-			rr[u] = 0;
-			if(k < ntask) {
-				// k < 2^12 here: the float quotient is exact enough to floor (checked below)
-				int r = __float2int_rz(__fmul_rn((float)k + 0.5f, inv_nh));
-				r -= (r * nh > k) ? 1 : 0;
-				r += ((r + 1) * nh <= k) ? 1 : 0;
-				const int t = k - r * nh;
-				rr[u] = r;
-				const int sv = WV.src[vt0 + r], sh = WH.src[ht0 + t];
-				live[u] = sv >= 0 && sh >= 0;
-				px[u] = J.crop_x + (sh < 0 ? 0 : sh);
-				py[u] = J.crop_y + (sv < 0 ? 0 : sv);
-			}
-		}
-#pragma unroll
-		for(int u = 0; u < 4; u++) {
-			if(live[u]) pixel_codes(J, px[u], py[u], wide, cc[u]);
-			else {
-#pragma unroll
-				for(int m = 0; m < dev::kMaxCh; m++) cc[u][m] = 0u;
-			}
-		}
-		float2 av[4], vv[4][dev::kMaxCh];
-#pragma unroll
-		for(int u = 0; u < 4; u++) {
-			av[u] = make_float2(1.0f, 0.0f);
-			if(live[u] && need_alpha) av[u] = __ldg(J.df_atab + pick4(cc[u], J.in_alpha));
-#pragma unroll
-			for(int m = 0; m < dev::kMaxCh; m++) {
-				vv[u][m] = make_float2(1.0f, 0.0f);
-				if(live[u] && m < J.mid_n && ((mask >> m) & 1u) && J.mid[m].in_ch < J.in_nphys)
-					vv[u][m] = __ldg(J.df_tab[m] + pick4(cc[u], J.mid[m].in_ch));
-			}
-		}
-#pragma unroll
-		for(int u = 0; u < 4; u++) {
-			const int k = k0 + 32 * u + lane;
-			if(k >= ntask) continue;
-			const dfl w = WV.kind == 1 ? dfl{1.0f, 0.0f} : df_of(__ldg(J.df_wv + vt0 + rr[u]));
-			const dfl aw = need_alpha ? df_mul(df_of(av[u]), w) : w;
-#pragma unroll
-			for(int m = 0; m < dev::kMaxCh; m++) {
-				if(m >= J.mid_n || !((mask >> m) & 1u)) continue;
-				dfl t = {0.0f, 0.0f};
-				if(live[u]) t = df_mul(df_of(vv[u][m]), (J.mid[m].unassoc && need_alpha) ? aw : w);
-				P[m * pstride + k] = make_float2(t.hi, t.lo);
-			}
-		}
-	}
-	__syncwarp();
-	// step 2: one (channel, horizontal tap) sum per lane at a time; terms
-	// added with df_add_sloppy (2.01 u^2 of the magnitudes so far each)
-	const float kd = (float)(24 * nv) * 3.5527137e-15f + (float)(2 * nv + 2) * 1.1102231e-16f;
-	const int nm = __popc(mask);
-	bool bad = false;
-	// (t, r) of task k = lane, advanced by 32 per step; a window without
-	// taps (nh == 0) has no sums to take
-	int r = 0, t = lane;
-	if(nh > 0)
-		while(t >= nh) { t -= nh; r++; }
-	for(int k = lane; nh > 0 && k < nm * nh; k += 32) {
-		const int m = nth_bit(mask, r);
-		const float2 *col = P + m * pstride + t;
-		dfl acc = {0.0f, 0.0f};
-		float A = 0.0f;
-		for(int q = 0; q < nv; q++) {
-			const float2 v = col[q * nh];
-			acc = df_add_sloppy(acc, df_of(v));
-			A = __fadd_rn(A, fabsf(v.x));
-		}
-		my[m * maxt + t] = acc.hi;
-		const float delta = __fmaf_rn(A * 1.01f, kd, 1e-30f);
-		// A == 0: every term is exactly zero (see interm_df_all)
-		if(!(A == 0.0f || rounds_to_hi(acc, delta))) bad = true;
-		t += 32;
-		while(t >= nh) { t -= nh; r++; }
-	}
-	if(__any_sync(0xffffffffu, bad)) return false;
-	__syncwarp();
-	return fix_df_finish(J, i, j, mask, my, maxt, lane);
-}
-
-// Re-evaluation of flagged pixels, one warp per pixel: the all-lanes
-// double-float tier (fix_pixel_df2), then, for a pixel it cannot certify,
-// the FP64 path in place.  Shared memory per warp: the terms (kMaxCh x
-// maxv x maxt double-float values) and the certified intermediates
-// (kMaxCh x maxt floats).  At most 'listcap' entries are read.
-template<bool BATCH>
-__global__ void __launch_bounds__(128) k_fix_df2(Job J1, const Job *jobs, int *count, const int *list, int maxv, int maxt,
-	int listcap)
-{
-	extern __shared__ float4 fix2_smem[];
-	const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, wpb = blockDim.x >> 5;
-	const int pstride = maxv * maxt;
-	float2 *P = reinterpret_cast<float2 *>(fix2_smem) + (size_t)wib * (dev::kMaxCh * pstride + dev::kMaxCh * maxt / 2 + 2);
-	float *my = reinterpret_cast<float *>(P + dev::kMaxCh * pstride);
-	const int n = min(*count, listcap);
-	for(int f = blockIdx.x * wpb + wib; f < n; f += gridDim.x * wpb) {
-		const int4 e = reinterpret_cast<const int4 *>(list)[f];
-		const Job &J = BATCH ? jobs[e.z] : J1;
-		const int p = e.x;
-		const unsigned int mask = (unsigned int)e.y & ((1u << J.mid_n) - 1u);
-		const int i = p % J.out_w, j = p / J.out_w;
-		if(J.df_wv && fix_pixel_df2(J, i, j, mask, P, pstride, my, maxt, lane)) {
-			__syncwarp();
-			continue;
-		}
-		if(lane == 0) atomicAdd(count + 1, 1);   // pixels that needed the FP64 path
-		__syncwarp();
-		fix_pixel_fp64_warp(J, i, j, mask, my, maxt, lane);
-	}
-}
-
 // The FP64 path of one flagged pixel, by a whole block: the block's threads
 // recompute the intermediate values of every (channel, horizontal tap) at
-// once, then warp 0 finishes each channel as k_fix_flagged_warp does (lane m:
-// channel m).  Every thread of the block calls it with the same entry.
+// once, then warp 0 finishes each channel (lane m: channel m).  Every thread of the block calls it with the same entry.
 __device__ void fix_pixel_fp64_block(const Job &J, int4 e, float *my, int maxt)
 {
 	const int lane = threadIdx.x & 31;
@@ -1321,7 +1179,7 @@ __device__ void fix_pixel_fp64_block(const Job &J, int4 e, float *my, int maxt)
 		const int nt = W.kind == 1 ? 1 : W.off[i + 1] - t0;
 		if(t < nt) {
 			const int src = W.src[t0 + t];
-			if(src >= 0) my[m * maxt + t] = (float)interm_exact<true>(J, m, src, j);
+			if(src >= 0) my[m * maxt + t] = (float)interm_exact_ahead(J, m, src, j);
 		}
 	}
 	__syncthreads();
@@ -1362,14 +1220,365 @@ __device__ void fix_pixel_fp64_block(const Job &J, int4 e, float *my, int maxt)
 	__syncthreads();   // 'my' is reused by the next pixel
 }
 
-// The FP64 path for the pixels listed at the tail of the flag list, one
-// block per pixel.
+// Re-evaluation of flagged pixels with small windows (up to 1280 input
+// pixels per flagged pixel), a few pixels per block, each step one link of
+// dependent loads long:
+// step 0: the block's flag entries, then its pixels' vertical and horizontal
+//   taps (source rows / columns and double-float weights) into shared memory;
+// step 1: every (pixel, vertical tap, horizontal tap) input pixel is loaded
+//   once -- up to kFixStageTasks per thread, all loads in flight together --
+//   and decoded for every masked channel, leaving the double-float term
+//   v * (a * w_v) in shared memory (an edge row leaves +0);
+// step 2: thread (pixel, horizontal tap, channel) sums its column's terms
+//   with df_add_sloppy and certifies the float intermediate as
+//   interm_df_all does (bound (13 + 2.01 nv) u^2 A <= 24 nv u^2 A, which
+//   holds for the exact real products in any order);
+// step 3: four lanes of warp 0 per pixel finish it (fix_df_finish_g): the
+//   decision reads one bracket record (q.rec) found from q.lut's start;
+// step 4: a pixel steps 2-3 could not certify takes the FP64 path in place,
+//   the whole block on it (fix_pixel_fp64_block).
+// Shared memory (fix_stage_bytes): terms [pb][kMaxCh][maxv][maxt] float2,
+// values [pb][kMaxCh][maxt] float, vertical and horizontal weights and
+// sources.  Launch: pb * kMaxCh * maxt <= blockDim.x and
+// pb * maxv * maxt <= kFixStageTasks * blockDim.x, pb <= 8.
+constexpr int kFixStageThreads = 320;
+constexpr int kFixStageTasks = 4;
+
+__host__ __device__ __forceinline__ size_t fix_stage_bytes(int pb, int maxv, int maxt)
+{
+	const size_t terms = (size_t)pb * dev::kMaxCh * maxv * maxt * sizeof(float2);
+	const size_t vals = (((size_t)pb * dev::kMaxCh * maxt + 1) & ~(size_t)1) * sizeof(float);
+	return terms + vals + (size_t)pb * (maxv + maxt) * (sizeof(float2) + sizeof(int));
+}
+
+template<bool BATCH>
+__global__ void __launch_bounds__(kFixStageThreads, 2) k_fix_stage(Job J1, const Job *jobs, int *count, const int *list,
+	int maxv, int maxt, int pb, int listcap)
+{
+	extern __shared__ float4 fixs_smem[];
+	const int TV = maxv * maxt;
+	float2 *const s_term = reinterpret_cast<float2 *>(fixs_smem);
+	float *const s_val = reinterpret_cast<float *>(s_term + (size_t)pb * dev::kMaxCh * TV);
+	float2 *const s_vw = reinterpret_cast<float2 *>(s_val + ((pb * dev::kMaxCh * maxt + 1) & ~1));
+	float2 *const s_hw = s_vw + pb * maxv;
+	int *const s_vsrc = reinterpret_cast<int *>(s_hw + pb * maxt);
+	int *const s_hsrc = s_vsrc + pb * maxv;
+	__shared__ int4 s_e[8];
+	__shared__ int s_nv[8], s_nh[8], s_bad[8];
+	const int n = min(*count, listcap);
+	for(int f0 = blockIdx.x * pb; f0 < n; f0 += gridDim.x * pb) {
+		// ---- step 0: entries, then taps ----
+		if(threadIdx.x < 8) {
+			const int g = threadIdx.x;
+			int4 e = make_int4(0, 0, 0, 0);
+			int nv = 0, nh = 0, bad = 0;
+			if(g < pb && f0 + g < n) {
+				e = reinterpret_cast<const int4 *>(list)[f0 + g];
+				const Job &J = BATCH ? jobs[e.z] : J1;
+				const int i = e.x % J.out_w, j = e.x / J.out_w;
+				const DWeights &WH = J.wh[J.mid[0].wh], &WV = J.wv[J.mid[0].wv];
+				nh = WH.kind == 1 ? 1 : WH.off[i + 1] - WH.off[i];
+				nv = WV.kind == 1 ? 1 : WV.off[j + 1] - WV.off[j];
+				// windows never exceed the launch's maxv x maxt; a pixel
+				// without double-float tables goes to the FP64 path
+				if(J.df_wv == nullptr || nv > maxv || nh > maxt) {
+					bad = 1;
+					nv = nh = 0;
+				}
+			}
+			s_e[g] = e;
+			s_nv[g] = nv;
+			s_nh[g] = nh;
+			s_bad[g] = bad;
+		}
+		__syncthreads();
+		for(int idx = threadIdx.x; idx < pb * (maxv + maxt); idx += blockDim.x) {
+			const bool vert = idx < pb * maxv;
+			const int q = vert ? idx : idx - pb * maxv;
+			const int g = vert ? q / maxv : q / maxt, r = vert ? q - g * maxv : q - g * maxt;
+			if(r >= (vert ? s_nv[g] : s_nh[g])) continue;
+			const int4 e = s_e[g];
+			const Job &J = BATCH ? jobs[e.z] : J1;
+			const int i = e.x % J.out_w, j = e.x / J.out_w;
+			if(vert) {
+				const DWeights &WV = J.wv[J.mid[0].wv];
+				const int t0 = WV.kind == 1 ? j : WV.off[j];
+				s_vsrc[g * maxv + r] = WV.src[t0 + r];
+				s_vw[g * maxv + r] = WV.kind == 1 ? make_float2(1.0f, 0.0f) : J.df_wv[t0 + r];
+			}
+			else {
+				const DWeights &WH = J.wh[J.mid[0].wh];
+				const int t0 = WH.kind == 1 ? i : WH.off[i];
+				s_hsrc[g * maxt + r] = WH.src[t0 + r];
+				s_hw[g * maxt + r] = WH.kind == 1 ? make_float2(1.0f, 0.0f) : J.df_wh[t0 + r];
+			}
+		}
+		__syncthreads();
+		// ---- step 1: the terms ----
+		{
+			const int total = pb * TV;
+			int gg[kFixStageTasks], rr[kFixStageTasks], tt[kFixStageTasks];
+			bool in[kFixStageTasks], live[kFixStageTasks];
+			unsigned int cc[kFixStageTasks][dev::kMaxCh];
+#pragma unroll
+			for(int u = 0; u < kFixStageTasks; u++) {
+				const int q = threadIdx.x + u * blockDim.x;
+				gg[u] = rr[u] = tt[u] = 0;
+				in[u] = live[u] = false;
+				if(q < total) {
+					const int g = q / TV, rem = q - g * TV, r = rem / maxt, t = rem - r * maxt;
+					gg[u] = g;
+					rr[u] = r;
+					tt[u] = t;
+					in[u] = r < s_nv[g] && t < s_nh[g];
+					live[u] = in[u] && s_vsrc[g * maxv + r] >= 0 && s_hsrc[g * maxt + t] >= 0;
+				}
+#pragma unroll
+				for(int m = 0; m < dev::kMaxCh; m++) cc[u][m] = 0u;
+			}
+#pragma unroll
+			for(int u = 0; u < kFixStageTasks; u++) {
+				if(!live[u]) continue;
+				const Job &J = BATCH ? jobs[s_e[gg[u]].z] : J1;
+				const bool wide = J.in_nphys == 4 && (J.in_depth == 16 || J.in_depth == 8) &&
+					(((uintptr_t)J.in | (uintptr_t)J.in_bpr) & (J.in_depth == 16 ? 7u : 3u)) == 0;
+				pixel_codes(J, J.crop_x + s_hsrc[gg[u] * maxt + tt[u]], J.crop_y + s_vsrc[gg[u] * maxv + rr[u]], wide, cc[u]);
+			}
+			float2 av[kFixStageTasks], vv[kFixStageTasks][dev::kMaxCh];
+#pragma unroll
+			for(int u = 0; u < kFixStageTasks; u++) {
+				av[u] = make_float2(1.0f, 0.0f);
+#pragma unroll
+				for(int m = 0; m < dev::kMaxCh; m++) vv[u][m] = make_float2(0.0f, 0.0f);
+				if(!live[u]) continue;
+				const Job &J = BATCH ? jobs[s_e[gg[u]].z] : J1;
+				const unsigned int mask = (unsigned int)s_e[gg[u]].y & ((1u << J.mid_n) - 1u);
+				const bool have_a = J.in_alpha < J.in_nphys && J.df_atab != nullptr;
+				bool need_a = false;
+#pragma unroll
+				for(int m = 0; m < dev::kMaxCh; m++) {
+					if(m >= J.mid_n || !((mask >> m) & 1u)) continue;
+					need_a = need_a || J.mid[m].unassoc;
+					vv[u][m] = J.mid[m].in_ch < J.in_nphys ? __ldg(J.df_tab[m] + pick4(cc[u], J.mid[m].in_ch)) : make_float2(1.0f, 0.0f);
+				}
+				if(need_a && have_a) av[u] = __ldg(J.df_atab + pick4(cc[u], J.in_alpha));
+			}
+#pragma unroll
+			for(int u = 0; u < kFixStageTasks; u++) {
+				if(!in[u]) continue;
+				const int g = gg[u];
+				const Job &J = BATCH ? jobs[s_e[g].z] : J1;
+				const unsigned int mask = (unsigned int)s_e[g].y & ((1u << J.mid_n) - 1u);
+				const bool have_a = J.in_alpha < J.in_nphys && J.df_atab != nullptr;
+				const dfl w = df_of(s_vw[g * maxv + rr[u]]);
+				const dfl aw = df_mul(df_of(av[u]), w);
+#pragma unroll
+				for(int m = 0; m < dev::kMaxCh; m++) {
+					if(m >= J.mid_n || !((mask >> m) & 1u)) continue;
+					dfl tm = {0.0f, 0.0f};   // an edge row adds +0
+					if(live[u]) tm = df_mul(df_of(vv[u][m]), (J.mid[m].unassoc && have_a) ? aw : w);
+					s_term[((size_t)(g * dev::kMaxCh + m) * maxv + rr[u]) * maxt + tt[u]] = make_float2(tm.hi, tm.lo);
+				}
+			}
+		}
+		__syncthreads();
+		// ---- step 2: certified column sums ----
+		{
+			const int g = threadIdx.x / (dev::kMaxCh * maxt), k = threadIdx.x - g * dev::kMaxCh * maxt;
+			const int t = k / dev::kMaxCh, m = k - t * dev::kMaxCh;
+			if(g < pb && f0 + g < n && !s_bad[g] && t < s_nh[g] && s_hsrc[g * maxt + t] >= 0) {
+				const Job &J = BATCH ? jobs[s_e[g].z] : J1;
+				const unsigned int mask = (unsigned int)s_e[g].y & ((1u << J.mid_n) - 1u);
+				if(m < J.mid_n && ((mask >> m) & 1u)) {
+					const int nv = s_nv[g];
+					const float2 *col = s_term + (size_t)(g * dev::kMaxCh + m) * TV + t;
+					dfl acc = {0.0f, 0.0f};
+					float A = 0.0f;
+					for(int r = 0; r < nv; r++) {
+						const float2 v = col[r * maxt];
+						acc = df_add_sloppy(acc, df_of(v));
+						A = __fadd_rn(A, fabsf(v.x));
+					}
+					s_val[(g * dev::kMaxCh + m) * maxt + t] = acc.hi;
+					const float kd = (float)(24 * nv) * 3.5527137e-15f + (float)(2 * nv + 2) * 1.1102231e-16f;
+					const float delta = __fmaf_rn(A * 1.01f, kd, 1e-30f);
+					// A == 0: every term is exactly zero (see interm_df_all)
+					if(!(A == 0.0f || rounds_to_hi(acc, delta))) s_bad[g] = 1;
+				}
+			}
+		}
+		__syncthreads();
+		// ---- step 3: finish ----
+		if(threadIdx.x < 32) {
+			const int g = threadIdx.x >> 2;
+			const bool live = g < pb && f0 + g < n && !s_bad[g];
+			const int4 e = s_e[g];
+			const Job &J = BATCH ? jobs[e.z] : J1;   // read only when live
+			unsigned int mask = 0u;
+			int i = 0, j = 0;
+			if(live) {
+				mask = (unsigned int)e.y & ((1u << J.mid_n) - 1u);
+				i = e.x % J.out_w;
+				j = e.x / J.out_w;
+			}
+			const bool ok = fix_df_finish_g<dev::kMaxCh>(J, i, j, mask, s_val + g * dev::kMaxCh * maxt, maxt, threadIdx.x,
+				live, s_hsrc + g * maxt, s_hw + g * maxt, live ? s_nh[g] : 1);
+			if((threadIdx.x & 3) == 0 && live && !ok) s_bad[g] = 1;
+		}
+		__syncthreads();
+		// ---- step 4: FP64 path ----
+		for(int g = 0; g < pb && f0 + g < n; g++) {
+			if(!s_bad[g]) continue;   // block-uniform
+			const int4 e = s_e[g];
+			if(threadIdx.x == 0) atomicAdd(count + 1, 1);   // pixels that needed the FP64 path
+			fix_pixel_fp64_block(BATCH ? jobs[e.z] : J1, e, s_val, maxt);
+		}
+		__syncthreads();   // the shared arrays are reused by the next pixels
+	}
+}
+
+// Re-evaluation of flagged pixels, a few pixels per block with a thread for
+// every (pixel, horizontal tap, channel), so that each thread's chain of
+// dependent loads is one vertical sum long:
+// phase 1: thread (p, t, m) takes the certified double-float vertical sum of
+//   channel m at the column of pixel p's horizontal tap t -- the terms
+//   v * (a * w_v) of the tap's nv rows, eight rows' loads in flight
+//   together, summed with df_add_sloppy and certified as interm_df_all
+//   certifies (bound (13 + 2.01 nv) u^2 A <= 24 nv u^2 A) -- into shared
+//   memory;
+// phase 2: four lanes of warp 0 per pixel finish it (fix_df_finish_g);
+// phase 3: a pixel either phase could not certify takes the FP64 path in
+//   place, the whole block on one pixel (fix_pixel_fp64_block).
+// Shared memory: per_block * kMaxCh * maxt floats; per_block <= 8 and
+// per_block * kMaxCh * maxt <= blockDim.x.  At most 'listcap' entries are read.
+constexpr int kFixTileThreads = 320;
+
+template<bool BATCH>
+__global__ void __launch_bounds__(kFixTileThreads, 2) k_fix_tile(Job J1, const Job *jobs, int *count, const int *list, int maxt,
+	int per_block, int listcap)
+{
+	extern __shared__ float fixt_smem[];
+	__shared__ int s_bad[8];
+	const int n = min(*count, listcap);
+	const int T = dev::kMaxCh * maxt;
+	for(int f0 = blockIdx.x * per_block; f0 < n; f0 += gridDim.x * per_block) {
+		if(threadIdx.x < 8) s_bad[threadIdx.x] = 0;
+		__syncthreads();
+		// ---- phase 1 ----
+		const int p = threadIdx.x / T;
+		if(p < per_block && f0 + p < n) {
+			const int k = threadIdx.x - p * T, t = k / dev::kMaxCh, m = k - t * dev::kMaxCh;
+			const int4 e = reinterpret_cast<const int4 *>(list)[f0 + p];
+			const Job &J = BATCH ? jobs[e.z] : J1;
+			const unsigned int mask = (unsigned int)e.y & ((1u << J.mid_n) - 1u);
+			const int i = e.x % J.out_w, j = e.x / J.out_w;
+			const DWeights &WH = J.wh[J.mid[0].wh], &WV = J.wv[J.mid[0].wv];
+			const int ht0 = WH.kind == 1 ? i : WH.off[i], nh = WH.kind == 1 ? 1 : WH.off[i + 1] - ht0;
+			const int vt0 = WV.kind == 1 ? j : WV.off[j], nv = WV.kind == 1 ? 1 : WV.off[j + 1] - vt0;
+			const int sh = t < nh ? WH.src[ht0 + t] : -1;
+			if(m == 0 && sh >= 0 && J.orient == 0 && J.in_depth >= 8) {
+				// start the column's rows towards L2 (a hint; the loop below
+				// takes them eight rows at a time)
+				const uint8_t *colp = J.in + (unsigned long long)(J.crop_x + sh) * J.in_nphys * (J.in_depth / 8);
+				for(int r = 0; r < nv; r++) {
+					const int sv = WV.src[vt0 + r];
+					if(sv >= 0) asm volatile("prefetch.global.L2 [%0];" ::"l"(colp + (unsigned long long)(J.crop_y + sv) * J.in_bpr));
+				}
+			}
+			if(J.df_wv == nullptr) s_bad[p] = 1;
+			else if(sh >= 0 && m < J.mid_n && ((mask >> m) & 1u)) {
+				const DMid &mc = J.mid[m];
+				const bool use_a = mc.unassoc && J.in_alpha < J.in_nphys && J.df_atab != nullptr;
+				const bool has_ch = mc.in_ch < J.in_nphys;
+				const bool wide = J.in_nphys == 4 && (J.in_depth == 16 || J.in_depth == 8) &&
+					(((uintptr_t)J.in | (uintptr_t)J.in_bpr) & (J.in_depth == 16 ? 7u : 3u)) == 0;
+				const int px = J.crop_x + sh;
+				const float2 *tab = J.df_tab[m];
+				dfl acc = {0.0f, 0.0f};
+				float A = 0.0f;
+				for(int r0 = 0; r0 < nv; r0 += 8) {
+					int sv[8];
+#pragma unroll
+					for(int u = 0; u < 8; u++) sv[u] = r0 + u < nv ? WV.src[vt0 + r0 + u] : -1;
+					unsigned int cv[8], ca[8];
+#pragma unroll
+					for(int u = 0; u < 8; u++) {
+						cv[u] = ca[u] = 0u;
+						if(sv[u] >= 0) {
+							unsigned int cc[dev::kMaxCh];
+							pixel_codes(J, px, J.crop_y + sv[u], wide, cc);
+							cv[u] = pick4(cc, mc.in_ch);
+							ca[u] = pick4(cc, J.in_alpha);
+						}
+					}
+					float2 vv[8], av[8], wv[8];
+#pragma unroll
+					for(int u = 0; u < 8; u++) {
+						vv[u] = av[u] = wv[u] = make_float2(1.0f, 0.0f);
+						if(sv[u] >= 0) {
+							if(has_ch) vv[u] = __ldg(tab + cv[u]);
+							if(use_a) av[u] = __ldg(J.df_atab + ca[u]);
+							if(WV.kind != 1) wv[u] = __ldg(J.df_wv + vt0 + r0 + u);
+						}
+					}
+#pragma unroll
+					for(int u = 0; u < 8; u++) {
+						if(sv[u] < 0) continue;   // edge taps add 0
+						const dfl w = df_of(wv[u]);
+						const dfl tm = df_mul(df_of(vv[u]), use_a ? df_mul(df_of(av[u]), w) : w);
+						acc = df_add_sloppy(acc, tm);
+						A = __fadd_rn(A, fabsf(tm.hi));
+					}
+				}
+				fixt_smem[p * T + m * maxt + t] = acc.hi;
+				const float kd = (float)(24 * nv) * 3.5527137e-15f + (float)(2 * nv + 2) * 1.1102231e-16f;
+				const float delta = __fmaf_rn(A * 1.01f, kd, 1e-30f);
+				// A == 0: every term is exactly zero (see interm_df_all)
+				if(!(A == 0.0f || rounds_to_hi(acc, delta))) s_bad[p] = 1;
+			}
+		}
+		__syncthreads();
+		// ---- phase 2 ----
+		if(threadIdx.x < 32) {
+			const int g = threadIdx.x >> 2;
+			const bool live = g < per_block && f0 + g < n && !s_bad[g];
+			int4 e = make_int4(0, 0, 0, 0);
+			if(live) e = reinterpret_cast<const int4 *>(list)[f0 + g];
+			const Job &J = BATCH ? jobs[e.z] : J1;   // read only when live
+			unsigned int mask = 0u;
+			int i = 0, j = 0;
+			if(live) {
+				mask = (unsigned int)e.y & ((1u << J.mid_n) - 1u);
+				i = e.x % J.out_w;
+				j = e.x / J.out_w;
+			}
+			const int *hsrc = nullptr;
+			const float2 *hw = nullptr;
+			int nh = 1;
+			if(live) h_taps(J, i, hsrc, hw, nh);
+			const bool ok = fix_df_finish_g<dev::kMaxCh>(J, i, j, mask, fixt_smem + g * T, maxt, threadIdx.x, live, hsrc, hw, nh);
+			if((threadIdx.x & 3) == 0 && g < per_block && f0 + g < n && !ok) s_bad[g] = 1;
+		}
+		__syncthreads();
+		// ---- phase 3 ----
+		for(int g = 0; g < per_block && f0 + g < n; g++) {
+			if(!s_bad[g]) continue;   // block-uniform
+			const int4 e = reinterpret_cast<const int4 *>(list)[f0 + g];
+			if(threadIdx.x == 0) atomicAdd(count + 1, 1);   // pixels that needed the FP64 path
+			fix_pixel_fp64_block(BATCH ? jobs[e.z] : J1, e, fixt_smem, maxt);
+		}
+		__syncthreads();   // s_bad and the shared values are reused by the next pixels
+	}
+}
+
+// The FP64 path for the pixels listed at the tail of the flag list (count[3]
+// entries from its end), one block per pixel.
 template<bool BATCH>
 __global__ void __launch_bounds__(256) k_fix_leftover(Job J1, const Job *jobs, const int *count, const int *list, int maxt,
 	int cap)
 {
 	extern __shared__ float fix_cache[];
-	const int n = min(*count, cap), left = min(count[1], cap - n);
+	const int n = min(*count, cap), left = min(count[3], cap - n);
 	for(int L = blockIdx.x; L < left; L += gridDim.x) {
 		const int4 e = reinterpret_cast<const int4 *>(list)[cap - 1 - L];
 		fix_pixel_fp64_block(BATCH ? jobs[e.z] : J1, e, fix_cache, maxt);
@@ -1380,7 +1589,7 @@ __global__ void __launch_bounds__(256) k_fix_leftover(Job J1, const Job *jobs, c
 // more), one block per pixel: the block's threads (one per horizontal tap)
 // compute the certified double-float intermediate values the pixel reads --
 // each a vertical sum over the pixel's rows, its loads in flight together
-// with those of the other taps -- then warp 0 finishes as fix_pixel_df does.
+// with those of the other taps -- then warp 0 finishes (fix_df_finish).
 // A pixel the double-float tier cannot decide is listed at the tail of the
 // flag list for k_fix_leftover while there is room, else its FP64 path runs
 // here.  Scratch: kMaxCh * maxt floats of shared memory.
@@ -1433,7 +1642,10 @@ __global__ void __launch_bounds__(256, 1) k_fix_wide_df(Job J1, const Job *jobs,
 		}
 		__syncthreads();
 		if(!s_ok) {
-			if(threadIdx.x == 0) s_slot = cap - 1 - atomicAdd(count + 1, 1);   // pixels that needed the FP64 path
+			if(threadIdx.x == 0) {
+				atomicAdd(count + 1, 1);                  // pixels that needed the FP64 path
+				s_slot = cap - 1 - atomicAdd(count + 3, 1);   // their entries at the list's tail
+			}
 			__syncthreads();
 			const int slot = s_slot;
 			if(slot >= n) {
@@ -1460,48 +1672,52 @@ __global__ void k_fix_flagged_thread(Job J1, const Job *jobs, int *count, const 
 	}
 }
 
-// Launches the exact re-evaluation of flagged pixels on 'st': a warp per
-// pixel (double-float, then FP64), and a block per pixel for those listed at
-// the tail of the flag list (capacity 'cap' entries).  Returns the launches.
+// Launches the exact re-evaluation of flagged pixels on 'st' (flag list of
+// capacity 'cap' entries).  Returns the launches.
 template<bool BATCH>
 static int launch_fix(cudaStream_t st, const Job &J, const Job *jobs, int maxv, int maxt, int *count, int *list, int cap)
 {
-	const size_t per_warp = (size_t)dev::kMaxCh * maxt * sizeof(float);
+	int sms = 152;
+	cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
+	const int T = dev::kMaxCh * maxt;
 	{
-		// narrow windows: every lane busy (k_fix_df2), four warps per block
-		const size_t per_warp2 = ((size_t)dev::kMaxCh * maxv * maxt + (size_t)dev::kMaxCh * maxt / 2 + 2) * sizeof(float2);
-		if(maxt <= kFix2MaxTaps && maxv <= kFix2MaxTaps && per_warp2 * 4 <= 96 * 1024) {
+		// small windows: every input pixel decoded once, in shared memory
+		// (k_fix_stage); the most pixels per block that fit
+		constexpr size_t kSmem = 96 * 1024;
+		int pb = 8;
+		while(pb > 0 && (pb * T > kFixStageThreads || pb * maxv * maxt > kFixStageTasks * kFixStageThreads ||
+			fix_stage_bytes(pb, maxv, maxt) > kSmem))
+			pb--;
+		if(pb > 0) {
 			static bool attr_done[2] = {false, false};
 			if(!attr_done[BATCH]) {
-				cudaFuncSetAttribute(k_fix_df2<BATCH>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024);
+				cudaFuncSetAttribute(k_fix_stage<BATCH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmem);
 				attr_done[BATCH] = true;
 			}
-			int sms2 = 152;
-			cudaDeviceGetAttribute(&sms2, cudaDevAttrMultiProcessorCount, 0);
-			k_fix_df2<BATCH><<<16 * sms2, 128, per_warp2 * 4, st>>>(J, jobs, count, list, maxv, maxt, cap);
+			const int need = std::max(pb * T, (pb * maxv * maxt + kFixStageTasks - 1) / kFixStageTasks);
+			const int threads = (need + 31) / 32 * 32;
+			k_fix_stage<BATCH><<<8 * sms, threads, fix_stage_bytes(pb, maxv, maxt), st>>>(J, jobs, count, list, maxv, maxt, pb,
+				cap);
 			return 1;
 		}
 	}
-	int wpb = 4;
-	while(wpb > 1 && per_warp * wpb > 48 * 1024) wpb >>= 1;
-	int sms = 152;
-	cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
-	// Flagged pixels are independent and each is a latency-bound chain:
-	// launch enough warps to take them all at once (idle warps exit at once).
-	// With narrow windows a pixel's FP64 path is short and runs in place,
-	// hidden behind the other warps; from 48 taps on it goes to a block.
-	if(maxt >= 48 && per_warp <= 48 * 1024) {
-		// wide windows: a block per pixel, one thread per horizontal tap
-		const int tpb = std::min(256, (maxt + 31) / 32 * 32);
-		k_fix_wide_df<BATCH><<<8 * sms, tpb, per_warp, st>>>(J, jobs, count, list, maxt, cap);
-		k_fix_leftover<BATCH><<<4 * sms, 256, per_warp, st>>>(J, jobs, count, list, maxt, cap);
-		return 2;
+	if(T <= kFixTileThreads) {
+		// a thread per (pixel, horizontal tap, channel), up to eight pixels
+		// per block (about 288 threads); a grid of eight blocks per SM takes
+		// the usual few thousand flagged pixels in one pass
+		const int per_block = std::max(1, std::min(8, 288 / T));
+		const int threads = (per_block * T + 31) / 32 * 32;
+		k_fix_tile<BATCH><<<8 * sms, threads, (size_t)per_block * T * sizeof(float), st>>>(J, jobs, count, list, maxt,
+			per_block, cap);
+		return 1;
 	}
-	if(per_warp * wpb <= 48 * 1024) {
-		const bool tail = maxt >= 48;
-		k_fix_flagged_warp<BATCH><<<24 * sms, 32 * wpb, per_warp * wpb, st>>>(J, jobs, count, list, maxt, tail ? cap : 0, cap);
-		if(!tail) return 1;
-		k_fix_leftover<BATCH><<<4 * sms, 256, per_warp, st>>>(J, jobs, count, list, maxt, cap);
+	const size_t per_block = (size_t)T * sizeof(float);
+	if(per_block <= 48 * 1024) {
+		// wide windows: a block per pixel, one thread per horizontal tap; the
+		// pixels left to FP64 are listed at the tail of the flag list
+		const int tpb = std::min(256, (maxt + 31) / 32 * 32);
+		k_fix_wide_df<BATCH><<<8 * sms, tpb, per_block, st>>>(J, jobs, count, list, maxt, cap);
+		k_fix_leftover<BATCH><<<4 * sms, 256, per_block, st>>>(J, jobs, count, list, maxt, cap);
 		return 2;
 	}
 	k_fix_flagged_thread<BATCH><<<24 * sms, 64, 0, st>>>(J, jobs, count, list, cap);
@@ -1927,11 +2143,12 @@ void preload_kernels()
 		cudaFuncAttributes a;
 		for(const void *k : {(const void *)k_vpass_exact, (const void *)k_hpass_exact, (const void *)k_scan,
 			(const void *)k_finalize, (const void *)kb_vpass_exact, (const void *)kb_hpass_exact, (const void *)kb_scan,
-			(const void *)kb_finalize, (const void *)k_fix_flagged_warp<true>, (const void *)k_fix_flagged_warp<false>,
+			(const void *)kb_finalize, (const void *)k_fix_tile<true>, (const void *)k_fix_tile<false>,
+			(const void *)k_fix_stage<true>, (const void *)k_fix_stage<false>,
 			(const void *)k_fix_wide_df<true>, (const void *)k_fix_wide_df<false>, (const void *)k_out_props,
 			(const void *)k_fix_leftover<true>, (const void *)k_fix_leftover<false>,
 			(const void *)k_fix_flagged_thread<true>, (const void *)k_fix_flagged_thread<false>,
-			(const void *)k_fix_df2<true>, (const void *)k_fix_df2<false>, (const void *)k_pull,
+			(const void *)k_pull,
 			(const void *)k_pull_many})
 			cudaFuncGetAttributes(&a, k);
 		preload_fast_kernels();
@@ -2168,6 +2385,7 @@ static bool make_job(iw_context *ctx, const Plan &P, DeviceState &S, Packer &pk,
 		D.q.rev = cached_table(S, q.rev);
 		D.q.nc = cached_table(S, q.nc);
 		D.q.rec = cached_table(S, q.rec);
+		D.q.lut = nullptr;
 		if(!D.q.U || !D.q.X || !D.q.code || !D.q.rev || (q.use_nc && !D.q.nc) || (q.rec && !D.q.rec)) {
 			iw_set_error(ctx, "Out of GPU memory (tables)");
 			return false;
@@ -2722,7 +2940,7 @@ bool run_batch(const std::vector<iw_context *> &ctxs, const std::vector<Plan *> 
 		cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, S.device);
 		k_pull_many<<<(unsigned)std::min(m, 8 * sms), 256, 0, st>>>((const PullItem *)(tbase + o_pull), m);
 	}
-	cudaMemsetAsync(flag_count, 0, 3 * sizeof(int), st);
+	cudaMemsetAsync(flag_count, 0, 4 * sizeof(int), st);
 	cudaEvent_t ev_h, ev_f;
 	cudaEventCreate(&ev_h);
 	cudaEventCreate(&ev_f);

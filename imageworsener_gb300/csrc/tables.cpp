@@ -179,7 +179,8 @@ void nc_fill(int cstype, double gamma, double *nc)
 	}
 }
 
-// Decision records of error diffusion (src/imagew-main.c:727-748): in
+// Decision records of a bracket (src/imagew-main.c:727-748; error diffusion
+// and the exact re-evaluation of the fast form read them): in
 // bracket k a sample v below X[k] is exact (no error sent); above it the
 // reference compares d_ceil = rev_hi - v with d_floor = v - rev_lo, each
 // rounded.  The first is non-increasing in v and the second non-decreasing,
@@ -228,7 +229,9 @@ void build_quant(Quant &q)
 	q.X = it->second.X;
 	q.code = it->second.code;
 	q.rev = it->second.rev;
-	if(q.dfam == IW_DITHERFAMILY_ERRDIFF) {
+	// records for error diffusion, and for the outputs the fast form takes
+	// (at most 4096 levels), whose re-evaluation reads one record per decision
+	if(q.dfam == IW_DITHERFAMILY_ERRDIFF || (!q.float_out && q.maxcc <= 4095)) {
 		auto rit = rec_cache.find(key);
 		if(rit == rec_cache.end()) {
 			auto rec = std::make_shared<std::vector<long long>>(8 * (size_t)(q.P + 1));
