@@ -671,7 +671,7 @@ def main():
     peak, peak_src = peaks()
     parts = list(st.ms_part)
     names = ["vertical pass (k_vbulk / k_vstream_px)", "horizontal pass + guarded quantisation (k_hpass_fast)",
-             "re-evaluation of flagged pixels, double-float then FP64 (k_fix_tile)"]
+             "re-evaluation of flagged pixels, double-float then FP64 (k_fix_stage)"]
     slowest = max(range(3), key=lambda k: parts[k])
     # The roofline is reported for the vertical pass: it moves the compulsory
     # bytes (the input image) and is the HBM-bound kernel of the pipeline.

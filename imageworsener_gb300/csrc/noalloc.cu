@@ -309,8 +309,7 @@ extern "C" int iwg_resize_u8_noalloc(const unsigned char *src, int src_w, int sr
 		return 0;
 	}
 	// Once per device: resolve the scratch array's device address (this may
-	// load the module on that device, so the first call per device belongs
-	// before any stream capture).
+	// load the module on that device).
 	if(!g_scratch_ptr[dev]) {
 		void *p = nullptr;
 		cudaError_t e = cudaGetSymbolAddress(&p, g_scratch);

@@ -1701,7 +1701,9 @@ static int launch_fix(cudaStream_t st, const Job &J, const Job *jobs, int maxv, 
 			return 1;
 		}
 	}
-	if(T <= kFixTileThreads) {
+	// windows of 48+ taps: a block per pixel of one thread per tap (many
+	// pixels in flight per SM) is faster than k_fix_tile's four threads per tap
+	if(T <= kFixTileThreads && maxt < 48) {
 		// a thread per (pixel, horizontal tap, channel), up to eight pixels
 		// per block (about 288 threads); a grid of eight blocks per SM takes
 		// the usual few thousand flagged pixels in one pass

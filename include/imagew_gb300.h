@@ -189,9 +189,9 @@ IW_EXPORT(void) iwg_server_destroy(struct iwg_server *s);
  * (one stream, or synchronised between streams); overlapping calls on
  * unsynchronised streams race.  The first call on each device resolves the
  * scratch array's address (which may load the library's module on that
- * device); make it before any stream capture.  That address is kept for the
- * life of the process: after cudaDeviceReset() on a device, this entry point
- * must not be called on that device again in the same process.
+ * device).  That address is kept for the life of the process: after
+ * cudaDeviceReset() on a device, this entry point must not be called on that
+ * device again in the same process.
  * Returns 1 on success; 0 on error, with a message in errmsg (at most
  * errmsg_len bytes, NUL-terminated) when errmsg is not NULL. */
 IW_EXPORT(int) iwg_resize_u8_noalloc(const unsigned char *src, int src_w, int src_h, long long src_bpr,
