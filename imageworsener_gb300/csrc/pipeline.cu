@@ -1437,140 +1437,6 @@ __global__ void __launch_bounds__(kFixStageThreads, 2) k_fix_stage(Job J1, const
 	}
 }
 
-// Re-evaluation of flagged pixels, a few pixels per block with a thread for
-// every (pixel, horizontal tap, channel), so that each thread's chain of
-// dependent loads is one vertical sum long:
-// phase 1: thread (p, t, m) takes the certified double-float vertical sum of
-//   channel m at the column of pixel p's horizontal tap t -- the terms
-//   v * (a * w_v) of the tap's nv rows, eight rows' loads in flight
-//   together, summed with df_add_sloppy and certified as interm_df_all
-//   certifies (bound (13 + 2.01 nv) u^2 A <= 24 nv u^2 A) -- into shared
-//   memory;
-// phase 2: four lanes of warp 0 per pixel finish it (fix_df_finish_g);
-// phase 3: a pixel either phase could not certify takes the FP64 path in
-//   place, the whole block on one pixel (fix_pixel_fp64_block).
-// Shared memory: per_block * kMaxCh * maxt floats; per_block <= 8 and
-// per_block * kMaxCh * maxt <= blockDim.x.  At most 'listcap' entries are read.
-constexpr int kFixTileThreads = 320;
-
-template<bool BATCH>
-__global__ void __launch_bounds__(kFixTileThreads, 2) k_fix_tile(Job J1, const Job *jobs, int *count, const int *list, int maxt,
-	int per_block, int listcap)
-{
-	extern __shared__ float fixt_smem[];
-	__shared__ int s_bad[8];
-	const int n = min(*count, listcap);
-	const int T = dev::kMaxCh * maxt;
-	for(int f0 = blockIdx.x * per_block; f0 < n; f0 += gridDim.x * per_block) {
-		if(threadIdx.x < 8) s_bad[threadIdx.x] = 0;
-		__syncthreads();
-		// ---- phase 1 ----
-		const int p = threadIdx.x / T;
-		if(p < per_block && f0 + p < n) {
-			const int k = threadIdx.x - p * T, t = k / dev::kMaxCh, m = k - t * dev::kMaxCh;
-			const int4 e = reinterpret_cast<const int4 *>(list)[f0 + p];
-			const Job &J = BATCH ? jobs[e.z] : J1;
-			const unsigned int mask = (unsigned int)e.y & ((1u << J.mid_n) - 1u);
-			const int i = e.x % J.out_w, j = e.x / J.out_w;
-			const DWeights &WH = J.wh[J.mid[0].wh], &WV = J.wv[J.mid[0].wv];
-			const int ht0 = WH.kind == 1 ? i : WH.off[i], nh = WH.kind == 1 ? 1 : WH.off[i + 1] - ht0;
-			const int vt0 = WV.kind == 1 ? j : WV.off[j], nv = WV.kind == 1 ? 1 : WV.off[j + 1] - vt0;
-			const int sh = t < nh ? WH.src[ht0 + t] : -1;
-			if(m == 0 && sh >= 0 && J.orient == 0 && J.in_depth >= 8) {
-				// start the column's rows towards L2 (a hint; the loop below
-				// takes them eight rows at a time)
-				const uint8_t *colp = J.in + (unsigned long long)(J.crop_x + sh) * J.in_nphys * (J.in_depth / 8);
-				for(int r = 0; r < nv; r++) {
-					const int sv = WV.src[vt0 + r];
-					if(sv >= 0) asm volatile("prefetch.global.L2 [%0];" ::"l"(colp + (unsigned long long)(J.crop_y + sv) * J.in_bpr));
-				}
-			}
-			if(J.df_wv == nullptr) s_bad[p] = 1;
-			else if(sh >= 0 && m < J.mid_n && ((mask >> m) & 1u)) {
-				const DMid &mc = J.mid[m];
-				const bool use_a = mc.unassoc && J.in_alpha < J.in_nphys && J.df_atab != nullptr;
-				const bool has_ch = mc.in_ch < J.in_nphys;
-				const bool wide = J.in_nphys == 4 && (J.in_depth == 16 || J.in_depth == 8) &&
-					(((uintptr_t)J.in | (uintptr_t)J.in_bpr) & (J.in_depth == 16 ? 7u : 3u)) == 0;
-				const int px = J.crop_x + sh;
-				const float2 *tab = J.df_tab[m];
-				dfl acc = {0.0f, 0.0f};
-				float A = 0.0f;
-				for(int r0 = 0; r0 < nv; r0 += 8) {
-					int sv[8];
-#pragma unroll
-					for(int u = 0; u < 8; u++) sv[u] = r0 + u < nv ? WV.src[vt0 + r0 + u] : -1;
-					unsigned int cv[8], ca[8];
-#pragma unroll
-					for(int u = 0; u < 8; u++) {
-						cv[u] = ca[u] = 0u;
-						if(sv[u] >= 0) {
-							unsigned int cc[dev::kMaxCh];
-							pixel_codes(J, px, J.crop_y + sv[u], wide, cc);
-							cv[u] = pick4(cc, mc.in_ch);
-							ca[u] = pick4(cc, J.in_alpha);
-						}
-					}
-					float2 vv[8], av[8], wv[8];
-#pragma unroll
-					for(int u = 0; u < 8; u++) {
-						vv[u] = av[u] = wv[u] = make_float2(1.0f, 0.0f);
-						if(sv[u] >= 0) {
-							if(has_ch) vv[u] = __ldg(tab + cv[u]);
-							if(use_a) av[u] = __ldg(J.df_atab + ca[u]);
-							if(WV.kind != 1) wv[u] = __ldg(J.df_wv + vt0 + r0 + u);
-						}
-					}
-#pragma unroll
-					for(int u = 0; u < 8; u++) {
-						if(sv[u] < 0) continue;   // edge taps add 0
-						const dfl w = df_of(wv[u]);
-						const dfl tm = df_mul(df_of(vv[u]), use_a ? df_mul(df_of(av[u]), w) : w);
-						acc = df_add_sloppy(acc, tm);
-						A = __fadd_rn(A, fabsf(tm.hi));
-					}
-				}
-				fixt_smem[p * T + m * maxt + t] = acc.hi;
-				const float kd = (float)(24 * nv) * 3.5527137e-15f + (float)(2 * nv + 2) * 1.1102231e-16f;
-				const float delta = __fmaf_rn(A * 1.01f, kd, 1e-30f);
-				// A == 0: every term is exactly zero (see interm_df_all)
-				if(!(A == 0.0f || rounds_to_hi(acc, delta))) s_bad[p] = 1;
-			}
-		}
-		__syncthreads();
-		// ---- phase 2 ----
-		if(threadIdx.x < 32) {
-			const int g = threadIdx.x >> 2;
-			const bool live = g < per_block && f0 + g < n && !s_bad[g];
-			int4 e = make_int4(0, 0, 0, 0);
-			if(live) e = reinterpret_cast<const int4 *>(list)[f0 + g];
-			const Job &J = BATCH ? jobs[e.z] : J1;   // read only when live
-			unsigned int mask = 0u;
-			int i = 0, j = 0;
-			if(live) {
-				mask = (unsigned int)e.y & ((1u << J.mid_n) - 1u);
-				i = e.x % J.out_w;
-				j = e.x / J.out_w;
-			}
-			const int *hsrc = nullptr;
-			const float2 *hw = nullptr;
-			int nh = 1;
-			if(live) h_taps(J, i, hsrc, hw, nh);
-			const bool ok = fix_df_finish_g<dev::kMaxCh>(J, i, j, mask, fixt_smem + g * T, maxt, threadIdx.x, live, hsrc, hw, nh);
-			if((threadIdx.x & 3) == 0 && g < per_block && f0 + g < n && !ok) s_bad[g] = 1;
-		}
-		__syncthreads();
-		// ---- phase 3 ----
-		for(int g = 0; g < per_block && f0 + g < n; g++) {
-			if(!s_bad[g]) continue;   // block-uniform
-			const int4 e = reinterpret_cast<const int4 *>(list)[f0 + g];
-			if(threadIdx.x == 0) atomicAdd(count + 1, 1);   // pixels that needed the FP64 path
-			fix_pixel_fp64_block(BATCH ? jobs[e.z] : J1, e, fixt_smem, maxt);
-		}
-		__syncthreads();   // s_bad and the shared values are reused by the next pixels
-	}
-}
-
 // The FP64 path for the pixels listed at the tail of the flag list (count[3]
 // entries from its end), one block per pixel.
 template<bool BATCH>
@@ -1688,7 +1554,9 @@ static int launch_fix(cudaStream_t st, const Job &J, const Job *jobs, int maxv, 
 		while(pb > 0 && (pb * T > kFixStageThreads || pb * maxv * maxt > kFixStageTasks * kFixStageThreads ||
 			fix_stage_bytes(pb, maxv, maxt) > kSmem))
 			pb--;
-		if(pb > 0) {
+		// one pixel per block leaves two pixels in flight per SM (registers):
+		// the block-per-pixel kernel below keeps several times more
+		if(pb >= 2) {
 			static bool attr_done[2] = {false, false};
 			if(!attr_done[BATCH]) {
 				cudaFuncSetAttribute(k_fix_stage<BATCH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmem);
@@ -1701,22 +1569,11 @@ static int launch_fix(cudaStream_t st, const Job &J, const Job *jobs, int maxv, 
 			return 1;
 		}
 	}
-	// windows of 48+ taps: a block per pixel of one thread per tap (many
-	// pixels in flight per SM) is faster than k_fix_tile's four threads per tap
-	if(T <= kFixTileThreads && maxt < 48) {
-		// a thread per (pixel, horizontal tap, channel), up to eight pixels
-		// per block (about 288 threads); a grid of eight blocks per SM takes
-		// the usual few thousand flagged pixels in one pass
-		const int per_block = std::max(1, std::min(8, 288 / T));
-		const int threads = (per_block * T + 31) / 32 * 32;
-		k_fix_tile<BATCH><<<8 * sms, threads, (size_t)per_block * T * sizeof(float), st>>>(J, jobs, count, list, maxt,
-			per_block, cap);
-		return 1;
-	}
 	const size_t per_block = (size_t)T * sizeof(float);
 	if(per_block <= 48 * 1024) {
-		// wide windows: a block per pixel, one thread per horizontal tap; the
-		// pixels left to FP64 are listed at the tail of the flag list
+		// larger windows: a block per pixel, one thread per horizontal tap
+		// (small blocks, many pixels in flight per SM); the pixels left to
+		// FP64 are listed at the tail of the flag list
 		const int tpb = std::min(256, (maxt + 31) / 32 * 32);
 		k_fix_wide_df<BATCH><<<8 * sms, tpb, per_block, st>>>(J, jobs, count, list, maxt, cap);
 		k_fix_leftover<BATCH><<<4 * sms, 256, per_block, st>>>(J, jobs, count, list, maxt, cap);
@@ -2145,7 +2002,7 @@ void preload_kernels()
 		cudaFuncAttributes a;
 		for(const void *k : {(const void *)k_vpass_exact, (const void *)k_hpass_exact, (const void *)k_scan,
 			(const void *)k_finalize, (const void *)kb_vpass_exact, (const void *)kb_hpass_exact, (const void *)kb_scan,
-			(const void *)kb_finalize, (const void *)k_fix_tile<true>, (const void *)k_fix_tile<false>,
+			(const void *)kb_finalize,
 			(const void *)k_fix_stage<true>, (const void *)k_fix_stage<false>,
 			(const void *)k_fix_wide_df<true>, (const void *)k_fix_wide_df<false>, (const void *)k_out_props,
 			(const void *)k_fix_leftover<true>, (const void *)k_fix_leftover<false>,
