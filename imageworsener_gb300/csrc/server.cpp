@@ -232,10 +232,17 @@ void dispatcher_loop(iwg_server *S)
 // scans concurrently, each request handed on as its own scan ends).  Large
 // scans take seconds and a worker holds its lane until its batch ends, so a
 // request that arrives while lanes are idle gets one alone; only a backlog
-// fills batches, up to four per lane.  (Measured with two: the serving
-// configuration's error-diffused upscales need about 34 lane-seconds per
-// second against 27 large lanes, and their queue still grew.)
+// fills batches, up to four per lane, of similar sizes.  (Measured with two
+// in arrival order: the serving configuration's error-diffused upscales need
+// about 30 lane-seconds per second against 27 large lanes, and their queue
+// still grew.)
 constexpr int kScanBatch[2] = {16, 4};
+constexpr size_t kMatchWindow = 64;
+
+long long out_samples(const iwg::Request *r)
+{
+	return (long long)r->plan.out_w * r->plan.out_h * r->plan.out_n;
+}
 
 void slow_loop(iwg_server *S, int lane, int cls)
 {
@@ -251,12 +258,22 @@ void slow_loop(iwg_server *S, int lane, int cls)
 					(!q.empty() && (S->slow_bytes == 0 || S->slow_bytes + q.front()->bytes <= S->budget));
 			});
 			if(q.empty()) return;
-			while(!q.empty() && (int)batch.size() < max_batch) {
-				iwg::Request *r = q.front();
+			// the oldest request, then queued ones of a similar size (output
+			// within a factor of two of its own, among the next kMatchWindow):
+			// the batch holds the lane until its largest scan ends, so
+			// similar sizes keep every scan of it busy that long
+			const long long s0 = out_samples(q.front());
+			for(size_t i = 0; i < q.size() && i < kMatchWindow && (int)batch.size() < max_batch;) {
+				iwg::Request *r = q[i];
+				const long long sr = out_samples(r);
+				if(!batch.empty() && (2 * sr < s0 || sr > 2 * s0)) {
+					i++;
+					continue;
+				}
 				if((!batch.empty() || S->slow_bytes > 0) && S->slow_bytes + bytes + r->bytes > S->budget) break;
 				bytes += r->bytes;
 				batch.push_back(r);
-				q.pop_front();
+				q.erase(q.begin() + (std::ptrdiff_t)i);
 			}
 			S->slow_bytes += bytes;
 		}
