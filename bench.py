@@ -703,6 +703,7 @@ def main():
                      "frac": (achieved / peak) if achieved else None, "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)",
                      "traffic": ROOFLINE_TRAFFIC.get(args.workload), "algorithmic_bytes_per_launch": comp[dom],
                      "pipeline_GBps": (in_bytes + out_bytes) / (ms / 1000.0) / 1e9,
+                     "pipeline_frac": (in_bytes + out_bytes) / (ms / 1000.0) / 1e9 / peak,
                      "slowest_kernel": names[slowest], "slowest_share": parts[slowest] / sum(parts) if sum(parts) else None},
         "kernel_ms": {"vertical": parts[0], "horizontal": parts[1], "fixup": parts[2]},
         "flagged_pixels": st.flagged, "flagged_fraction": st.flagged / out_px,
